@@ -1,0 +1,376 @@
+"""Benchmark of the execute hot path: batched fftwf c2c, N = 4096 x 65536.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c2c4096|c2c1024d|r2c16384|c2c1m|c3d512|r2c2d8192]
+
+One step = one fftwf_execute_dft of the whole batch (65536 transforms of 4096
+complex64 points, 2 GiB in, 2 GiB out, both larger than the 129 MB L2 so
+every step streams from HBM).  Reported on one JSON line:
+
+  value      Gflop/s, 5 N log2 N per transform (libbench2/mflops.c:21-27),
+             device-resident arrays, CUDA events around K steps on the
+             launching stream
+  e2e        the same metric through fftwf_execute_dft on page-locked HOST
+             arrays (fftwf_malloc): host->device copy, passes, device->host
+             copy all inside the timed region
+  roofline   HBM: algorithmic bytes (one read + one write of the batch) per
+             launch / average launch time, against MEASURED_PEAKS.json
+  cpu_baseline  the reference algorithm on the host cores (bounded sample)
+
+--impl reference times the reference's CPU implementation on the host cores:
+oracle/_ref (the reference FFTW, codelet-free) when it was built here, else
+the oracle's C restatement; all host threads; a bounded sample per step.
+Under torchrun, every rank runs the whole batch on its own GPU (weak
+scaling, no collective: the transforms are independent) and rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (kind, shape, howmany, prec, inplace)
+    "c2c4096": ("c2c", [4096], 65536, "f", False),
+    "c2c1024d": ("c2c", [1024], 4096, "d", False),
+    "r2c16384": ("r2c", [16384], 16384, "f", False),
+    "c2c1m": ("c2c", [1 << 20], 64, "f", False),
+    "c3d512": ("c2c", [512, 512, 512], 1, "f", True),
+    "r2c2d8192": ("r2c", [8192, 8192], 1, "f", False),
+}
+METRIC = "FFT Gflop/s (5N log2N/t) & HBM %peak: split-FP16 TC vs FP32, rel err<=1e-6"
+
+
+def flops_per_step(kind, shape, howmany):
+    n = math.prod(shape)
+    f = 5.0 * n * math.log2(n) * howmany
+    return f / 2 if kind in ("r2c", "c2r") else f
+
+
+def bytes_per_step(kind, shape, howmany, prec):
+    n = math.prod(shape)
+    cs = 8 if prec == "f" else 16
+    if kind == "c2c":
+        return 2 * n * cs * howmany
+    nc = n // shape[-1] * (shape[-1] // 2 + 1)
+    return (n * cs // 2 + nc * cs) * howmany
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            sm = [float(r[0]) for r in rows]
+            mx = [float(r[1]) for r in rows]
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[2 + i] and "Not" not in r[2 + i]})
+            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": reasons, "samples": len(rows)}
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def committed_traffic(workload):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{workload}_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def cpu_sample(workload, nthreads, budget_s=10.0, prefer_ref=True):
+    """Time the reference algorithm on the host: oracle/_ref (reference FFTW)
+    if it was built on this machine, else the oracle's C restatement."""
+    import numpy as np
+    from oracle.oracle import Reference, Restatement, ref_available
+    kind, shape, howmany, prec, _ = WORKLOADS[workload]
+    n = math.prod(shape)
+    per = max(1, min(howmany, int(2 ** 22 // n)))   # ~32 MB of complex64 per call
+    rng = np.random.default_rng(0)
+    cdt = np.complex64 if prec == "f" else np.complex128
+    use_ref = prefer_ref and ref_available()
+    if kind == "c2c":
+        x = (rng.standard_normal(per * n) + 1j * rng.standard_normal(per * n)).astype(cdt)
+    else:
+        x = rng.standard_normal(per * n).astype(np.float32 if prec == "f" else np.float64)
+    if use_ref:
+        R = Reference(prec)
+        fn = (lambda: R.c2c(x, shape, -1, nthreads=nthreads)) if kind == "c2c" else (lambda: R.r2c(x, shape, nthreads=nthreads))
+        kind_s = "reference"
+    else:
+        R = Restatement()
+        fn = (lambda: R.c2c(x, shape, -1, prec, nthreads)) if kind == "c2c" else (lambda: R.r2c(x, shape, prec, nthreads))
+        kind_s = "port"
+    fn()
+    t0 = time.perf_counter()
+    calls = 0
+    while True:
+        fn()
+        calls += 1
+        if time.perf_counter() - t0 >= budget_s or calls >= 64:
+            break
+    dt = time.perf_counter() - t0
+    val = flops_per_step(kind, shape, per) * calls / dt / 1e9
+    return {"value": round(val, 3), "unit": "Gflop/s", "cores": nthreads, "kind": kind_s,
+            "sample": f"{calls} calls x {per} transforms of {'x'.join(map(str, shape))} ({'reference FFTW, codelet-free build' if use_ref else 'oracle C restatement'}), {dt:.1f} s"}
+
+
+def run_reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    kind, shape, howmany, prec, _ = WORKLOADS[args.workload]
+    nthreads = os.cpu_count() or 1
+    vals = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(args.workload, nthreads, budget_s=max(2.0, 20.0 / max(1, args.steps)))
+        if i >= args.warmup:
+            vals.append(r["value"])
+            base = r
+    v = statistics.mean(vals)
+    n = math.prod(shape)
+    out = {
+        "metric": METRIC, "value": round(v, 3), "unit": "Gflop/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(flops_per_step(kind, shape, howmany) / (v * 1e9) * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if prec == "f" else "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {kind} {'x'.join(map(str, shape))} x {howmany} ({'float' if prec == 'f' else 'double'})",
+                   "sample_per_step": base["sample"]},
+        "cpu_baseline": dict(base, value=round(v, 3)),
+        "e2e": {"value": round(v, 3), "unit": "Gflop/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import fftw3_gb300 as g
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from fftw3_gb300 import build as b
+    b.build()
+    lib = g.load()
+    kind, shape, howmany, prec, inplace = WORKLOADS[args.workload]
+    n = math.prod(shape)
+    cdt = torch.complex64 if prec == "f" else torch.complex128
+    rdt = torch.float32 if prec == "f" else torch.float64
+    gen = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    nc = n // shape[-1] * (shape[-1] // 2 + 1)
+    if kind == "c2c":
+        xin = torch.randn(howmany * n, dtype=cdt, device="cuda", generator=gen)
+        yout = xin if inplace else torch.empty_like(xin)
+        p = g.plan_many_dft(shape, howmany, xin.data_ptr(), yout.data_ptr(), -1, g.FFTW_ESTIMATE, prec)
+    else:
+        xin = torch.randn(howmany * n, dtype=rdt, device="cuda", generator=gen)
+        yout = torch.empty(howmany * nc, dtype=cdt, device="cuda")
+        p = g.plan_many_dft_r2c(shape, howmany, xin.data_ptr(), yout.data_ptr(), g.FFTW_ESTIMATE, prec)
+    stream = torch.cuda.current_stream()
+    p.set_stream(stream.cuda_stream)
+    p.set_async(True)
+
+    def step():
+        if kind == "c2c":
+            p.execute_dft(xin.data_ptr(), yout.data_ptr())
+        else:
+            p.execute_dft_r2c(xin.data_ptr(), yout.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    l0 = g.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = g.launch_count() - l0
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    fl = flops_per_step(kind, shape, howmany)
+    value = fl * ws / (ms_step * 1e-3) / 1e9
+
+    # accuracy of this run on a sample of transforms, against the oracle
+    from oracle.oracle import Restatement, rel_l2
+    k = min(howmany, 64) if n <= 65536 else 1
+    xs = xin[: k * n].cpu().numpy()
+    if kind == "c2c":
+        step()
+        torch.cuda.synchronize()
+        ref = Restatement().c2c(xs.astype(np.complex128 if prec == "f" else np.clongdouble), shape, -1,
+                                "d" if prec == "f" else "l", os.cpu_count() or 1)
+        err = rel_l2(yout[: k * n].cpu().numpy(), ref)
+    else:
+        step()
+        torch.cuda.synchronize()
+        ref = Restatement().r2c(xs.astype(np.float64 if prec == "f" else np.longdouble), shape,
+                                "d" if prec == "f" else "l", os.cpu_count() or 1)
+        err = rel_l2(yout[: k * nc].cpu().numpy(), ref)
+
+    # dominant kernel: per-launch time from the events (one pass per step for
+    # single-pass plans; per-pass share otherwise is taken from the ncu list)
+    npass = len(p.passes())
+    hbm, src = peaks()
+    alg = bytes_per_step(kind, shape, howmany, prec)
+    achieved = alg / (ms_step * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": committed_traffic(args.workload),
+            "peak_source": src, "passes_per_step": npass,
+            "note": "achieved = algorithmic bytes per step (one read + one write) / step time"}
+
+    # e2e: host arrays through the public API
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = run_e2e(lib, g, kind, shape, howmany, prec, inplace, args)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_sample(args.workload, os.cpu_count() or 1, budget_s=10.0, prefer_ref=False)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": round(value, 2), "unit": "Gflop/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if prec == "f" else "f64", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: fftw{'f' if prec == 'f' else ''}_plan_many_dft{'_r2c' if kind == 'r2c' else ''} "
+                                   f"{'x'.join(map(str, shape))} x {howmany}, {'in place' if inplace else 'out of place'}, FFTW_ESTIMATE",
+                       "inputs": "N(0,1) from torch.Generator seed 1234+rank; batch larger than L2 (no flush needed)",
+                       "form": "plain FP32 CUDA-core" if prec == "f" else "FP64",
+                       "rel_l2_vs_fp64_oracle": err, "oracle_sample_transforms": k},
+            "gbs": round(achieved, 1),
+            "roofline": roof,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
+    """fftwf_execute_dft on page-locked host arrays: H2D + passes + D2H timed."""
+    import ctypes
+    n = math.prod(shape)
+    cs = 8 if prec == "f" else 16
+    nc = n // shape[-1] * (shape[-1] // 2 + 1)
+    in_bytes = howmany * n * (cs if kind == "c2c" else cs // 2)
+    out_bytes = howmany * (n if kind == "c2c" else nc) * cs
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    hin = getattr(lib, pfx + "malloc")(in_bytes)
+    hout = hin if inplace else getattr(lib, pfx + "malloc")(out_bytes)
+    ctypes.memset(hin, 0, in_bytes)
+    if kind == "c2c":
+        p = g.plan_many_dft(shape, howmany, hin, hout, -1, g.FFTW_ESTIMATE, prec)
+        ex = lambda: p.execute_dft(hin, hout)
+    else:
+        p = g.plan_many_dft_r2c(shape, howmany, hin, hout, g.FFTW_ESTIMATE, prec)
+        ex = lambda: p.execute_dft_r2c(hin, hout)
+    ex()
+    steps = max(2, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ex()
+    dt = (time.perf_counter() - t0) / steps
+    p.destroy()
+    getattr(lib, pfx + "free")(hin)
+    if not inplace:
+        getattr(lib, pfx + "free")(hout)
+    v = flops_per_step(kind, shape, howmany) / dt / 1e9
+    return {"value": round(v, 2), "unit": "Gflop/s", "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": out_bytes,
+            "ms_per_step": round(dt * 1e3, 3), "timer": "host wall clock around fftwf_execute_dft (synchronous)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2c4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * C-ABI launch layer: the host planner (C) reaches every device kernel
+ * through the functions in this file.  No torch types, no C++ in the
+ * signatures.  Also holds the FP64 twiddle / chirp generators, which replace
+ * the reference's plan-time trig tables (kernel/twiddle.c:124-222,
+ * kernel/trig.c:169-227, dft/bluestein.c:37-50) with device generation:
+ * each factor is computed in FP64 with an exact integer argument reduction
+ * and rounded once to the working precision.
+ */
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include "fft_kernels.cuh"
+
+extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir);
+extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
+
+namespace gb {
+
+template <typename C>
+__global__ void k_twiddles(C *dst, long long n, long long count, long long mul)
+{
+     typedef typename real_of<C>::T R;
+     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < count;
+          j += (long long)gridDim.x * blockDim.x) {
+          double c, s;
+          long long m = (long long)(((unsigned long long)j * (unsigned long long)mul) % (unsigned long long)n);
+          cexp_fp64(m, n, -1, &c, &s);
+          dst[j] = mk<C>((R)c, (R)s);
+     }
+}
+
+/* Bluestein chirp w[k] = exp(-sign * i * pi * k^2 / n): the index k^2 is
+ * reduced modulo 2n exactly in 64-bit integers (dft/bluestein.c:37-50). */
+template <typename C>
+__global__ void k_chirp(C *dst, long long n, int sign)
+{
+     typedef typename real_of<C>::T R;
+     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+          k += (long long)gridDim.x * blockDim.x) {
+          unsigned long long n2 = 2ull * (unsigned long long)n;
+          unsigned long long ksq = ((unsigned long long)k * (unsigned long long)k) % n2;
+          double c, s;
+          cexp_fp64((long long)ksq, (long long)n2, -sign, &c, &s);
+          dst[k] = mk<C>((R)c, (R)s);
+     }
+}
+
+/* Padded chirp / nb, the convolution kernel whose spectrum Bluestein
+ * multiplies by (dft/bluestein.c:52-80). */
+template <typename C>
+__global__ void k_chirp_pad(C *dst, const C *w, long long n, long long nb)
+{
+     typedef typename real_of<C>::T R;
+     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nb;
+          k += (long long)gridDim.x * blockDim.x) {
+          C v = mk<C>(0, 0);
+          if (k < n) v = w[k];
+          else if (nb - k < n) v = w[nb - k];
+          dst[k] = mk<C>(v.x / (R)nb, v.y / (R)nb);
+     }
+}
+
+} /* namespace gb */
+
+using namespace gb;
+
+static __thread char gb_errbuf[256];
+static unsigned long long gb_launches = 0;
+
+extern "C" long long gb_launch_count(void) { return (long long)__atomic_load_n(&gb_launches, __ATOMIC_RELAXED); }
+
+extern "C" const char *gb_last_cuda_error(void) { return gb_errbuf; }
+
+static int gb_check(cudaError_t e, const char *what)
+{
+     if (e != cudaSuccess) {
+          snprintf(gb_errbuf, sizeof gb_errbuf, "%s: %s", what, cudaGetErrorString(e));
+          return -1;
+     }
+     return 0;
+}
+
+extern "C" int gb_device_max_smem(void)
+{
+     int dev = 0, v = 0;
+     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+     if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+     return v;
+}
+
+extern "C" int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream)
+{
+     int blocks = (int)((count + 255) / 256);
+     if (blocks > 4096) blocks = 4096;
+     if (blocks < 1) blocks = 1;
+     if (prec == 4) k_twiddles<float2><<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, n, count, mul);
+     else k_twiddles<double2><<<blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, n, count, mul);
+     return gb_check(cudaGetLastError(), "twiddle generation");
+}
+
+extern "C" int gb_chirp(void *dst, int prec, long long n, int sign, void *stream)
+{
+     int blocks = (int)((n + 255) / 256);
+     if (blocks > 4096) blocks = 4096;
+     if (prec == 4) k_chirp<float2><<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, n, sign);
+     else k_chirp<double2><<<blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, n, sign);
+     return gb_check(cudaGetLastError(), "chirp generation");
+}
+
+extern "C" int gb_chirp_pad(void *dst, const void *w, int prec, long long n, long long nb, void *stream)
+{
+     int blocks = (int)((nb + 255) / 256);
+     if (blocks > 4096) blocks = 4096;
+     if (prec == 4) k_chirp_pad<float2><<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, (const float2 *)w, n, nb);
+     else k_chirp_pad<double2><<<blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, (const double2 *)w, n, nb);
+     return gb_check(cudaGetLastError(), "chirp padding");
+}
+
+static const void *pick_kernel(const gb_pass *p)
+{
+     if (p->kind == GB_KIND_COPY)
+          return p->prec == 4 ? (const void *)k_copy<float2> : (const void *)k_copy<double2>;
+     if (p->variant == GB_VAR_REG) {
+          int logn = 0;
+          while ((1 << logn) < p->nfft) ++logn;
+          return p->prec == 4 ? gb_reg_kernel_f(logn, p->kind, p->sign) : gb_reg_kernel_d(logn, p->kind, p->sign);
+     }
+     int dir = p->sign;
+     if (p->kind == GB_KIND_R2C || p->kind == GB_KIND_BLUESTEIN) dir = -1;
+     if (p->kind == GB_KIND_C2R) dir = 1;
+     if (p->prec == 4) return dir < 0 ? (const void *)k_gen<float2, -1> : (const void *)k_gen<float2, 1>;
+     return dir < 0 ? (const void *)k_gen<double2, -1> : (const void *)k_gen<double2, 1>;
+}
+
+/* Number of CTAs launched for a pass: all tiles, capped; kernels stride over
+ * the rest. */
+static unsigned grid_of(const gb_pass *p)
+{
+     long long g = p->nblocks;
+     if (g > (1LL << 30)) g = 1LL << 30;
+     if (g < 1) g = 1;
+     return (unsigned)g;
+}
+
+extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void *stream)
+{
+     const void *fn = pick_kernel(p);
+     if (!fn) {
+          snprintf(gb_errbuf, sizeof gb_errbuf, "no kernel for kind %d variant %d nfft %d prec %d",
+                   p->kind, p->variant, p->nfft, p->prec);
+          return -1;
+     }
+     if (p->nblocks <= 0) return 0;
+     if (p->smem > 48 * 1024) {
+          if (gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, p->smem),
+                       "cudaFuncSetAttribute(max dynamic smem)"))
+               return -1;
+     }
+     gb_pass pv = *p;
+     void *args[3] = {(void *)&pv, (void *)&in, (void *)&out};
+     cudaError_t e = cudaLaunchKernel(fn, dim3(grid_of(p)), dim3(p->threads), args, (size_t)p->smem,
+                                      (cudaStream_t)stream);
+     __atomic_add_fetch(&gb_launches, 1ull, __ATOMIC_RELAXED);
+     return gb_check(e, "kernel launch");
+}
+
+/* Resource usage of the kernel a pass would launch (registers per thread,
+ * static smem, max threads), for the planner's occupancy choices. */
+extern "C" int gb_pass_kernel_attrs(const gb_pass *p, int *regs, int *max_threads)
+{
+     const void *fn = pick_kernel(p);
+     cudaFuncAttributes a;
+     if (!fn) return -1;
+     if (gb_check(cudaFuncGetAttributes(&a, fn), "cudaFuncGetAttributes")) return -1;
+     *regs = a.numRegs;
+     *max_threads = a.maxThreadsPerBlock;
+     return 0;
+}

@@ -1,0 +1,5 @@
+/* k_reg instantiations, single precision (nfft = 2^0 .. 2^14). */
+#define GB_REAL float
+#define GB_MAXLOG 14
+#include "fft_reg_inst.cuh"
+extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir) { return gb::reg_lookup<0>(logn, kind, dir); }

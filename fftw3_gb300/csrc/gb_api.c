@@ -1,0 +1,116 @@
+/*
+ * libfftw3_gb300 public entry points: the reference's fftw3.h API for the
+ * double (fftw_) and float (fftwf_) prefixes, plus the extensions declared
+ * in include/fftw3_gb300.h.  The per-precision bodies are in gb_api_impl.h.
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
+#include "fftw3.h"
+#include "fftw3_gb300.h"
+#include "gb_host.h"
+
+/* ---------------------------------------------------------------- state */
+static double gb_timelimit = -1.0;
+static int gb_nthreads = 1;
+static int gb_fail_count = 0;
+
+void gb_set_timelimit(double t) { gb_timelimit = t; }
+double gb_get_timelimit(void) { return gb_timelimit; }
+void gb_set_nthreads(int n) { gb_nthreads = n < 1 ? 1 : n; }
+int gb_get_nthreads(void) { return gb_nthreads; }
+void gb_note_failure(void) { __atomic_add_fetch(&gb_fail_count, 1, __ATOMIC_RELAXED); }
+void gb_cleanup_tables(void) { if (!gb_dry_run()) gb_tables_free(); }
+
+/* fftw_malloc: page-locked host memory when a GPU is present (host arrays
+ * are staged to the device at DMA speed), 64-byte aligned host memory
+ * otherwise (api/malloc.c:24-50 only promises SIMD alignment). */
+typedef struct { void *base; int pinned; } gb_alloc_hdr;
+
+void *gb_malloc(size_t n)
+{
+     void *base = 0;
+     int pinned = 0;
+     size_t tot = n + 64;
+     char *p;
+     if (!gb_dry_run() && gb_cuda_ready() && !getenv("FFTW_GB300_PAGEABLE")) {
+          if (cudaMallocHost(&base, tot) == cudaSuccess) pinned = 1;
+          else { cudaGetLastError(); base = 0; }
+     }
+     if (!base && posix_memalign(&base, 64, tot) != 0) return 0;
+     p = (char *)base + 64;
+     ((gb_alloc_hdr *)(p - sizeof(gb_alloc_hdr)))->base = base;
+     ((gb_alloc_hdr *)(p - sizeof(gb_alloc_hdr)))->pinned = pinned;
+     return p;
+}
+
+void gb_free(void *p)
+{
+     gb_alloc_hdr h;
+     if (!p) return;
+     h = *(gb_alloc_hdr *)((char *)p - sizeof(gb_alloc_hdr));
+     if (h.pinned) cudaFreeHost(h.base);
+     else free(h.base);
+}
+
+/* version strings (api/version.c:21-40) */
+const char fftw_version[] = "fftw-3.3.10-gb300";
+const char fftwf_version[] = "fftw-3.3.10-gb300";
+const char fftw_cc[] = "nvcc -gencode arch=compute_103a,code=sm_103a; gcc";
+const char fftwf_cc[] = "nvcc -gencode arch=compute_103a,code=sm_103a; gcc";
+const char fftw_codelet_optim[] = "sm_103a register/shared-memory stages";
+const char fftwf_codelet_optim[] = "sm_103a register/shared-memory stages";
+
+/* ---------------------------------------------------------------- API */
+#define C fftw_complex
+#define R double
+#define PFX(name) fftw_##name
+#include "gb_api_impl.h"
+#undef C
+#undef R
+#undef PFX
+
+#define C fftwf_complex
+#define R float
+#define PFX(name) fftwf_##name
+#include "gb_api_impl.h"
+#undef C
+#undef R
+#undef PFX
+
+/* ---------------------------------------------------------------- extensions */
+const char *fftw_gb300_last_error(void) { return gb_last_error(); }
+int fftw_gb300_failures(void) { return __atomic_load_n(&gb_fail_count, __ATOMIC_RELAXED); }
+void fftw_gb300_set_dry_run(int on) { gb_set_dry_run(on); }
+long long fftw_gb300_launch_count(void) { return gb_launch_count(); }
+
+#define GB_EXT(PFX_, PLAN)                                                              \
+     int PFX_##gb300_set_stream(PLAN p, void *stream)                                  \
+     {                                                                                 \
+          if (!p) return -1;                                                           \
+          p->g->stream = stream;                                                       \
+          return 0;                                                                    \
+     }                                                                                 \
+     int PFX_##gb300_set_async(PLAN p, int async)                                      \
+     {                                                                                 \
+          if (!p) return -1;                                                           \
+          p->g->async = async;                                                         \
+          return 0;                                                                    \
+     }                                                                                 \
+     int PFX_##gb300_npasses(PLAN p) { return p ? p->g->nstep : -1; }                  \
+     int PFX_##gb300_pass_info(PLAN p, int i, int *kind, int *nfft, int *variant,      \
+                               int *tb, int *threads, int *smem, long long *blocks)    \
+     {                                                                                 \
+          const gb_pass *P;                                                            \
+          if (!p || i < 0 || i >= p->g->nstep) return -1;                              \
+          P = &p->g->step[i].pass;                                                     \
+          *kind = P->kind; *nfft = P->nfft; *variant = P->variant; *tb = P->tb;        \
+          *threads = P->threads; *smem = P->smem; *blocks = P->nblocks;                \
+          return 0;                                                                    \
+     }                                                                                 \
+     size_t PFX_##gb300_scratch_bytes(PLAN p) { return p ? p->g->scratch_bytes : 0; }
+
+GB_EXT(fftw_, fftw_plan)
+GB_EXT(fftwf_, fftwf_plan)

@@ -1,0 +1,202 @@
+/*
+ * Execution of a compiled plan: pointer classification, host staging, and
+ * the pass launches.  Counterpart of the reference's execute path
+ * (api/execute.c:23-27 -> plan->adt->solve -> plan_dft.apply), which here
+ * becomes a sequence of kernel launches on one CUDA stream.
+ *
+ * Arrays may live in device memory (used in place) or in host memory
+ * (copied to device staging buffers before the passes and back after).  A
+ * device array whose address is not aligned to one complex element is
+ * staged the same way, so every kernel sees naturally aligned data.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+#include "gb_host.h"
+
+typedef struct { long long lo, hi; } extent;   /* element offsets, [lo, hi] */
+
+static extent tensor_extent(const gb_problem *prb, int which, long long *count)
+{
+     /* which: 0 = input tensor, 1 = output tensor */
+     extent e = {0, 0};
+     long long cnt = 1;
+     int i;
+     for (i = 0; i < prb->rank; ++i) {
+          long long n = prb->sz[i].n, s = which ? prb->sz[i].os : prb->sz[i].is;
+          if (i == prb->rank - 1) {
+               if (prb->kind == GB_PROB_R2C && which == 1) n = n / 2 + 1;
+               if (prb->kind == GB_PROB_C2R && which == 0) n = n / 2 + 1;
+          }
+          cnt *= n;
+          if (s >= 0) e.hi += (n - 1) * s; else e.lo += (n - 1) * s;
+     }
+     for (i = 0; i < prb->vrank; ++i) {
+          long long n = prb->vec[i].n, s = which ? prb->vec[i].os : prb->vec[i].is;
+          cnt *= n;
+          if (n == 0) { cnt = 0; continue; }
+          if (s >= 0) e.hi += (n - 1) * s; else e.lo += (n - 1) * s;
+     }
+     *count = cnt;
+     return e;
+}
+
+static int elsize(const gb_problem *prb, int which)
+{
+     int c = 2 * prb->prec;
+     if (prb->kind == GB_PROB_R2C && which == 0) return prb->prec;
+     if (prb->kind == GB_PROB_C2R && which == 1) return prb->prec;
+     return c;
+}
+
+static int device_accessible(const void *ptr)
+{
+     struct cudaPointerAttributes a;
+     if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+          cudaGetLastError();
+          return 0;
+     }
+     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static int ensure(void **buf, size_t *have, size_t need)
+{
+     if (*have >= need) return 0;
+     if (*buf) cudaFree(*buf);
+     *buf = 0;
+     *have = 0;
+     if (cudaMalloc(buf, need) != cudaSuccess) {
+          cudaGetLastError();
+          gb_set_error("cudaMalloc(%zu) for staging failed", need);
+          return -1;
+     }
+     *have = need;
+     return 0;
+}
+
+static int run_step(const gb_plan *p, const gb_step *s, char *bufs[3], int esz[3], int real_pairs_ok[3])
+{
+     gb_pass P = s->pass;
+     long long idx[GB_MAXLOOP];
+     int i, done = 0;
+     const int si = s->src, di = s->dst;
+     if (P.kind == GB_KIND_R2C && !real_pairs_ok[si]) P.real_pairs = 0;
+     else if (P.kind == GB_KIND_R2C) {
+          int ok = (P.is == 1);
+          for (i = 0; i < P.nv; ++i) if (P.vis[i] % 2) ok = 0;
+          if (s->src_off % 2) ok = 0;
+          P.real_pairs = ok;
+     }
+     if (P.kind == GB_KIND_C2R) {
+          int ok = (P.os == 1) && real_pairs_ok[di];
+          for (i = 0; i < P.nv; ++i) if (P.vos[i] % 2) ok = 0;
+          if (s->dst_off % 2) ok = 0;
+          P.real_pairs = ok;
+     }
+     for (i = 0; i < s->nloop; ++i) idx[i] = 0;
+     while (!done) {
+          long long oi = s->src_off, oo = s->dst_off;
+          for (i = 0; i < s->nloop; ++i) { oi += idx[i] * s->loop[i].is; oo += idx[i] * s->loop[i].os; }
+          if (gb_launch_pass(&P, bufs[si] + oi * esz[si], bufs[di] + oo * esz[di], p->stream)) {
+               gb_set_error("pass launch failed: %s", gb_last_cuda_error());
+               return -1;
+          }
+          for (i = s->nloop - 1; i >= 0; --i) {
+               if (++idx[i] < s->loop[i].n) break;
+               idx[i] = 0;
+          }
+          if (i < 0) done = 1;
+     }
+     return 0;
+}
+
+int gb_execute(gb_plan *p, void *in, void *out)
+{
+     const gb_problem *prb = &p->prb;
+     long long cin, cout;
+     extent ein = tensor_extent(prb, 0, &cin), eout = tensor_extent(prb, 1, &cout);
+     int esin = elsize(prb, 0), esout = elsize(prb, 1);
+     int cs = 2 * prb->prec;
+     int inplace = (in == out);
+     int stage_i, stage_o;
+     char *din, *dout;
+     char *bufs[3];
+     int esz[3], rp[3];
+     int k;
+     cudaStream_t st = (cudaStream_t)p->stream;
+
+     if (cin == 0 || cout == 0 || p->nstep == 0) {
+          if (prb->rank == 0 && in != out && cin > 0) { /* rank-0 in-place is a no-op */ }
+          if (p->nstep == 0) return 0;
+     }
+     if (gb_dry_run()) return 0;
+
+     /* stage host arrays and device arrays not aligned to one complex element
+      * (complex arrays) or to one real (real arrays) */
+     stage_i = !device_accessible(in) || ((uintptr_t)in % (esin == cs ? cs : prb->prec));
+     stage_o = !device_accessible(out) || ((uintptr_t)out % (esout == cs ? cs : prb->prec));
+     if (inplace) stage_i = stage_o = (stage_i || stage_o);
+
+     din = (char *)in;
+     dout = (char *)out;
+     if (inplace && stage_i) {
+          long long lo = ein.lo * esin < eout.lo * esout ? ein.lo * esin : eout.lo * esout;
+          long long hi = (ein.hi + 1) * esin > (eout.hi + 1) * esout ? (ein.hi + 1) * esin : (eout.hi + 1) * esout;
+          size_t bytes = (size_t)(hi - lo);
+          if (ensure(&p->stage_in, &p->stage_in_bytes, bytes + 256)) return -1;
+          /* keep the host pointer's offset modulo 16 so alignment-dependent
+           * choices see the same alignment as the planning arrays */
+          if (cudaMemcpyAsync(p->stage_in, (char *)in + lo, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) goto cuerr;
+          din = dout = (char *)p->stage_in - lo;
+     } else {
+          if (stage_i) {
+               size_t bytes = (size_t)((ein.hi - ein.lo + 1) * esin);
+               if (ensure(&p->stage_in, &p->stage_in_bytes, bytes + 256)) return -1;
+               if (cudaMemcpyAsync(p->stage_in, (char *)in + ein.lo * esin, bytes,
+                                   device_accessible(in) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st) != cudaSuccess)
+                    goto cuerr;
+               din = (char *)p->stage_in - ein.lo * esin;
+          }
+          if (stage_o) {
+               size_t bytes = (size_t)((eout.hi - eout.lo + 1) * esout);
+               if (ensure(&p->stage_out, &p->stage_out_bytes, bytes + 256)) return -1;
+               if (cout != eout.hi - eout.lo + 1) {   /* gaps in the output: keep the caller's values */
+                    if (cudaMemcpyAsync(p->stage_out, (char *)out + eout.lo * esout, bytes,
+                                        device_accessible(out) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st) != cudaSuccess)
+                         goto cuerr;
+               }
+               dout = (char *)p->stage_out - eout.lo * esout;
+          }
+     }
+
+     bufs[GB_BUF_IN] = din; bufs[GB_BUF_OUT] = dout; bufs[GB_BUF_SCRATCH] = (char *)p->scratch;
+     esz[GB_BUF_IN] = esin; esz[GB_BUF_OUT] = esout; esz[GB_BUF_SCRATCH] = cs;
+     rp[GB_BUF_IN] = ((uintptr_t)din % cs) == 0;
+     rp[GB_BUF_OUT] = ((uintptr_t)dout % cs) == 0;
+     rp[GB_BUF_SCRATCH] = 1;
+     /* element size of each buffer: r2c reads reals and writes complex;
+      * c2r reads complex (its c2c passes work in place there) and writes
+      * reals; scratch is complex */
+     for (k = 0; k < p->nstep; ++k)
+          if (run_step(p, &p->step[k], bufs, esz, rp)) return -1;
+
+     if (inplace && stage_i) {
+          long long lo = ein.lo * esin < eout.lo * esout ? ein.lo * esin : eout.lo * esout;
+          long long hi = (ein.hi + 1) * esin > (eout.hi + 1) * esout ? (ein.hi + 1) * esin : (eout.hi + 1) * esout;
+          if (cudaMemcpyAsync((char *)out + lo, p->stage_in, (size_t)(hi - lo), cudaMemcpyDeviceToHost, st) != cudaSuccess) goto cuerr;
+     } else if (stage_o) {
+          size_t bytes = (size_t)((eout.hi - eout.lo + 1) * esout);
+          if (cudaMemcpyAsync((char *)out + eout.lo * esout, p->stage_out, bytes,
+                              device_accessible(out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st) != cudaSuccess)
+               goto cuerr;
+     }
+     if (stage_i || stage_o || !p->async) {
+          if (cudaStreamSynchronize(st) != cudaSuccess) goto cuerr;
+     }
+     return 0;
+cuerr:
+     gb_set_error("CUDA error during execute: %s", cudaGetErrorString(cudaGetLastError()));
+     return -1;
+}

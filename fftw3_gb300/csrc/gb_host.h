@@ -1,0 +1,117 @@
+/*
+ * Host-side internals of libfftw3_gb300 (C).
+ *
+ * A problem is stored the way the reference stores one (dft/dft.h:34-38,
+ * rdft/rdft.h:117-124): a transform tensor sz of (n, is, os) dims and a
+ * vector tensor vecsz, plus the array pointers.  Strides here are in
+ * elements of the array they index: complex elements for complex arrays,
+ * real elements for real arrays (the reference counts reals throughout,
+ * api/plan-many-dft.c:44-47; the factor 2 is applied at the boundary).
+ */
+#ifndef GB_HOST_H
+#define GB_HOST_H
+
+#include <stddef.h>
+#include <pthread.h>
+#include "gb_types.h"
+
+#define GB_MAXRANK 16
+#define GB_MAXPASS 16
+#define GB_MAXLOOP 8
+
+enum gb_prob_kind { GB_PROB_DFT = 0, GB_PROB_R2C = 1, GB_PROB_C2R = 2 };
+
+typedef struct { long long n, is, os; } gb_dim;
+
+typedef struct gb_problem {
+     int kind;              /* enum gb_prob_kind */
+     int prec;              /* 4 or 8 */
+     int sign;              /* -1 / +1 (c2c); r2c -1; c2r +1 */
+     int rank;
+     gb_dim sz[GB_MAXRANK];
+     int vrank;
+     gb_dim vec[GB_MAXRANK];
+     void *in, *out;        /* arrays given at planning time */
+} gb_problem;
+
+/* buffer ids a pass reads or writes */
+enum { GB_BUF_IN = 0, GB_BUF_OUT = 1, GB_BUF_SCRATCH = 2 };
+
+typedef struct gb_step {
+     gb_pass pass;
+     int src, dst;                 /* buffer ids */
+     long long src_off, dst_off;   /* element offsets added to the buffer pointer */
+     int nloop;                    /* vector dims beyond GB_MAXV, looped on the host */
+     gb_dim loop[GB_MAXLOOP];
+} gb_step;
+
+struct gb_plan {
+     int refcnt;
+     gb_problem prb;
+     unsigned flags;
+     int nstep;
+     gb_step step[GB_MAXPASS];
+     size_t scratch_bytes;
+     void *scratch;             /* device scratch (four-step intermediates) */
+     /* staging buffers for host arrays */
+     void *stage_in, *stage_out;
+     size_t stage_in_bytes, stage_out_bytes;
+     void *stream;              /* cudaStream_t; 0 = legacy default stream */
+     int async;                 /* 1: execute does not wait for completion */
+     int in_align, out_align;   /* alignment of the planning arrays (bytes, capped at 16) */
+     double add, mul, fma;      /* operation counts */
+     double measured_ms;        /* time of one execute measured by the tuner (0 if not measured) */
+     char desc[1024];           /* what print_plan prints */
+     char key[256];             /* wisdom key */
+};
+typedef struct gb_plan gb_plan;
+
+/* planner / problem (gb_plan.c) */
+gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags);
+void gb_destroy(gb_plan *p);
+int gb_dry_run(void);
+void gb_set_dry_run(int on);
+const char *gb_last_error(void);
+void gb_set_error(const char *fmt, ...);
+void gb_lock(void);
+void gb_unlock(void);
+int gb_cuda_ready(void);
+
+/* library state (gb_api.c) */
+void *gb_malloc(size_t n);
+void gb_free(void *p);
+void gb_set_timelimit(double t);
+double gb_get_timelimit(void);
+void gb_set_nthreads(int n);
+int gb_get_nthreads(void);
+void gb_note_failure(void);
+void gb_cleanup_tables(void);
+
+/* tuner (gb_tune.c) */
+int gb_tune(gb_plan *p, unsigned flags);
+
+/* execution (gb_exec.c) */
+int gb_execute(gb_plan *p, void *in, void *out);
+
+/* wisdom (gb_wisdom.c) */
+typedef struct gb_wisdom_entry {
+     char key[256];
+     int variant, tb, load_mode, store_mode, n1;
+} gb_wisdom_entry;
+const gb_wisdom_entry *gb_wisdom_lookup(const char *key);
+void gb_wisdom_store(const gb_wisdom_entry *e);
+void gb_wisdom_forget(void);
+int gb_wisdom_export(int prec, void (*emit)(char c, void *), void *data);
+int gb_wisdom_import(int prec, int (*getc_fn)(void *), void *data);
+
+/* table cache (gb_plan.c) */
+const void *gb_table_twiddle(int prec, long long n, long long count, long long mul);
+const void *gb_table_chirp(int prec, long long n, int sign);
+const void *gb_table_chirp_spec(int prec, long long n, long long nb, int sign);
+void gb_tables_free(void);
+
+/* launch layer (fft_launch.cu) */
+int gb_chirp_pad(void *dst, const void *w, int prec, long long n, long long nb, void *stream);
+int gb_pass_kernel_attrs(const gb_pass *p, int *regs, int *max_threads);
+
+#endif

@@ -1,0 +1,636 @@
+/*
+ * The planner: turns a problem (transform tensor + vector tensor + arrays)
+ * into a list of GPU passes.
+ *
+ * Reference counterparts and what replaced them:
+ *   kernel/tensor7.c:99-167 (canonicalization: drop n=1 dims, merge
+ *     contiguous vector dims)                    -> gb_canon_vec()
+ *   dft/rank-geq2.c:42-52, :121-172 (multi-d = trailing axes, then the
+ *     leading axes in place on the output)         -> gb_mkplan() axis loop
+ *   rdft/rank-geq2-rdft2.c:40-69 (r2c: last axis then c2c; c2r reversed,
+ *     the c2c part in place on the input)          -> gb_mkplan() r2c/c2r
+ *   dft/vrank-geq1.c:54-65 (loop over the batch) -> the CUDA grid
+ *   dft/ct.c + kernel/primes.c:183-195 (radix choice) -> gb_factor()
+ *   dft/buffered.c, dft/indirect-transpose.c (strided axes) -> COLS tiles
+ *   large n: the reference recurses Cooley-Tukey one memory pass per level;
+ *     here n = n1*n2 runs as two passes with the n1-point outputs twiddled
+ *     by W_n^(n2*k1) in the first pass (four-step)   -> add_fourstep()
+ *   dft/bluestein.c (prime n > 16, conv size 2,3,5-smooth >= 2n-1) ->
+ *     GB_KIND_BLUESTEIN with a power-of-two convolution inside one CTA
+ *   kernel/planner.c search + api/apiplan.c:86-178 patience loop -> the
+ *     configuration heuristics here, refined by measurement (gb_tune) under
+ *     FFTW_MEASURE/PATIENT/EXHAUSTIVE and recorded as wisdom.
+ */
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
+#include "gb_host.h"
+
+/* ------------------------------------------------------------ errors */
+static __thread char gb_err[512];
+const char *gb_last_error(void) { return gb_err; }
+void gb_set_error(const char *fmt, ...)
+{
+     va_list ap;
+     va_start(ap, fmt);
+     vsnprintf(gb_err, sizeof gb_err, fmt, ap);
+     va_end(ap);
+     if (getenv("FFTW_GB300_TRACE")) fprintf(stderr, "[fftw_gb300] %s\n", gb_err);
+}
+
+static pthread_mutex_t gb_mtx = PTHREAD_MUTEX_INITIALIZER;
+void gb_lock(void) { pthread_mutex_lock(&gb_mtx); }
+void gb_unlock(void) { pthread_mutex_unlock(&gb_mtx); }
+
+static int gb_dry = 0;
+int gb_dry_run(void) { return gb_dry; }
+void gb_set_dry_run(int on) { gb_dry = on; }
+
+int gb_cuda_ready(void)
+{
+     static int state = -1;
+     if (state < 0) {
+          int n = 0;
+          state = (cudaGetDeviceCount(&n) == cudaSuccess && n > 0) ? 1 : 0;
+     }
+     return state;
+}
+
+static int smem_max(void)
+{
+     static int v = 0;
+     if (!v) v = (!gb_dry && gb_cuda_ready()) ? gb_device_max_smem() : 232448;
+     if (!v) v = 232448;
+     return v;
+}
+
+/* ------------------------------------------------------------ tables */
+typedef struct tab { int prec, type; long long a, b, c; void *p; struct tab *next; } tab;
+static tab *tabs = 0;
+
+static void *tab_find(int prec, int type, long long a, long long b, long long c)
+{
+     tab *t;
+     for (t = tabs; t; t = t->next)
+          if (t->prec == prec && t->type == type && t->a == a && t->b == b && t->c == c) return t->p;
+     return 0;
+}
+
+static void *tab_add(int prec, int type, long long a, long long b, long long c, size_t bytes)
+{
+     tab *t;
+     void *p = 0;
+     if (gb_dry) {
+          static char dummy[64];
+          return dummy;
+     }
+     if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
+          gb_set_error("cudaMalloc(%zu) for a twiddle table failed", bytes);
+          return 0;
+     }
+     t = (tab *)malloc(sizeof *t);
+     t->prec = prec; t->type = type; t->a = a; t->b = b; t->c = c; t->p = p;
+     t->next = tabs; tabs = t;
+     return p;
+}
+
+/* exp(-2 pi i (j*mul) / n), j < count */
+const void *gb_table_twiddle(int prec, long long n, long long count, long long mul)
+{
+     void *p = tab_find(prec, 0, n, count, mul);
+     if (p) return p;
+     p = tab_add(prec, 0, n, count, mul, (size_t)count * 2 * prec);
+     if (!p || gb_dry) return p;
+     if (gb_twiddles(p, prec, n, count, mul, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("twiddle generation failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     return p;
+}
+
+const void *gb_table_chirp(int prec, long long n, int sign)
+{
+     void *p = tab_find(prec, 1, n, sign, 0);
+     if (p) return p;
+     p = tab_add(prec, 1, n, sign, 0, (size_t)n * 2 * prec);
+     if (!p || gb_dry) return p;
+     if (gb_chirp(p, prec, n, sign, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("chirp generation failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     return p;
+}
+
+static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os,
+                       int nv, const gb_dim *v, int tb_hint, int keep_order);
+
+/* Spectrum of the padded chirp / nb (dft/bluestein.c:52-80), computed on the
+ * device with this library's own forward FFT. */
+const void *gb_table_chirp_spec(int prec, long long n, long long nb, int sign)
+{
+     void *p = tab_find(prec, 2, n, nb, sign);
+     const void *w;
+     gb_pass P;
+     gb_dim d;
+     if (p) return p;
+     w = gb_table_chirp(prec, n, sign);
+     if (!w) return 0;
+     p = tab_add(prec, 2, n, nb, sign, (size_t)nb * 2 * prec);
+     if (!p || gb_dry) return p;
+     if (gb_chirp_pad(p, w, prec, n, nb, 0)) {
+          gb_set_error("chirp padding failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     d.n = 1; d.is = 0; d.os = 0;
+     if (config_pass(&P, prec, GB_KIND_C2C, nb, -1, 1, 1, 1, &d, 0, 0) != 0) return 0;
+     if (gb_launch_pass(&P, p, p, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("chirp spectrum failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     return p;
+}
+
+void gb_tables_free(void)
+{
+     while (tabs) {
+          tab *t = tabs;
+          tabs = t->next;
+          cudaFree(t->p);
+          free(t);
+     }
+}
+
+/* ------------------------------------------------------------ helpers */
+static int is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
+static int ilog2(long long n) { int l = 0; while ((1LL << l) < n) ++l; return l; }
+static long long llabs_(long long a) { return a < 0 ? -a : a; }
+
+/* radix list for k_gen: 16s first, then 8/4/2, then odd primes <= 13 */
+static int gb_factor(long long n, int *rad)
+{
+     int k = 0;
+     static const int odd[] = {3, 5, 7, 11, 13};
+     int i;
+     while (n % 16 == 0 && k < GB_MAXRAD) { rad[k++] = 16; n /= 16; }
+     if (n % 8 == 0) { rad[k++] = 8; n /= 8; }
+     if (n % 4 == 0) { rad[k++] = 4; n /= 4; }
+     if (n % 2 == 0) { rad[k++] = 2; n /= 2; }
+     for (i = 0; i < 5; ++i)
+          while (n % odd[i] == 0 && k < GB_MAXRAD) { rad[k++] = odd[i]; n /= odd[i]; }
+     return n == 1 ? k : -1;
+}
+
+static int csize(int prec) { return 2 * prec; }
+static int reg_max_log(int prec) { return prec == 4 ? 14 : 13; }
+static int reg_e(int nfft) { return nfft < 16 ? nfft : 16; }
+static int reg_sms(int nfft) { return nfft + (nfft >> 4) + 2; }
+static int reg_maxthreads(int nfft) { int t = nfft / reg_e(nfft); return t > 512 ? t : 512; }
+
+/* FFTW's canonical vector tensor: drop n = 1, merge dims that are
+ * contiguous in both input and output (kernel/tensor7.c:99-167). */
+static int gb_canon_vec(gb_dim *v, int nv)
+{
+     int i, j, k = 0;
+     for (i = 0; i < nv; ++i)
+          if (v[i].n != 1) v[k++] = v[i];
+     nv = k;
+     for (i = 0; i < nv; ++i)     /* sort by |is| descending, then |os| */
+          for (j = i + 1; j < nv; ++j)
+               if (llabs_(v[j].is) > llabs_(v[i].is) ||
+                   (llabs_(v[j].is) == llabs_(v[i].is) && llabs_(v[j].os) > llabs_(v[i].os))) {
+                    gb_dim t = v[i]; v[i] = v[j]; v[j] = t;
+               }
+     for (i = nv - 1; i > 0; --i) {   /* v[i-1] outer, v[i] inner */
+          if (v[i - 1].is == v[i].n * v[i].is && v[i - 1].os == v[i].n * v[i].os) {
+               v[i].n *= v[i - 1].n;
+               for (j = i - 1; j < nv - 1; ++j) v[j] = v[j + 1];
+               --nv;
+               i = nv;
+          }
+     }
+     return nv;
+}
+
+/* Configure one pass: kernel variant, tile, moves, launch shape.
+ * Returns 0 on success, 1 if the length needs more than one CTA
+ * (four-step or multi-pass Bluestein), -1 if unsupported. */
+static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os,
+                       int nv, const gb_dim *v_in, int tb_hint, int keep_order)
+{
+     gb_dim v[GB_MAXV + GB_MAXLOOP];
+     int i, best, smax = smem_max();
+     long long nfft;
+     int half = (kind == GB_KIND_R2C || kind == GB_KIND_C2R) && (n % 2 == 0);
+     memset(P, 0, sizeof *P);
+     if (nv > GB_MAXV) nv = GB_MAXV;
+     for (i = 0; i < nv; ++i) v[i] = v_in[i];
+     if (nv == 0) { v[0].n = 1; v[0].is = 0; v[0].os = 0; nv = 1; }
+     P->kind = kind; P->prec = prec; P->sign = sign; P->n = (int)n;
+     nfft = half ? n / 2 : n;
+     P->nfft = (int)nfft;
+     P->is = is; P->os = os;
+
+     /* tile dimension: the vector dim with the smallest stride */
+     best = 0;
+     for (i = 1; i < nv && !keep_order; ++i) {
+          long long si = llabs_(v[i].is) + llabs_(v[i].os), sb = llabs_(v[best].is) + llabs_(v[best].os);
+          if (si < sb) best = i;
+     }
+     if (best) { gb_dim t = v[0]; v[0] = v[best]; v[best] = t; }
+     P->nv = nv;
+     for (i = 0; i < nv; ++i) { P->vn[i] = v[i].n; P->vis[i] = v[i].is; P->vos[i] = v[i].os; }
+
+     if (kind == GB_KIND_COPY) {
+          P->variant = GB_VAR_GEN;
+          P->tb = 256; P->threads = 256; P->smem = 0;
+          P->ntiles0 = (v[0].n + P->tb - 1) / P->tb;
+          P->nblocks = P->ntiles0;
+          for (i = 1; i < nv; ++i) P->nblocks *= v[i].n;
+          return 0;
+     }
+
+     if (is_pow2(nfft) && ilog2(nfft) <= reg_max_log(prec) && kind != GB_KIND_BLUESTEIN &&
+         (kind == GB_KIND_C2C || half)) {
+          int E = reg_e((int)nfft), T = (int)nfft / E, tb, maxt = reg_maxthreads((int)nfft);
+          int cols_in, cols_out;
+          long long sm1 = (long long)reg_sms((int)nfft) * csize(prec);
+          P->variant = GB_VAR_REG;
+          cols_in = llabs_(is) != 1 && llabs_(P->vis[0]) == 1;
+          cols_out = llabs_(os) != 1 && llabs_(P->vos[0]) == 1;
+          if (kind == GB_KIND_R2C) cols_in = llabs_(is) != 1 && llabs_(P->vis[0]) <= 2;
+          if (kind == GB_KIND_C2R) cols_out = llabs_(os) != 1 && llabs_(P->vos[0]) <= 2;
+          tb = 256 / T; if (tb < 1) tb = 1;
+          if (cols_in || cols_out) { int want = prec == 4 ? 16 : 8; if (tb < want) tb = want; }
+          if (tb_hint > 0) tb = tb_hint;
+          while (tb > 1 && (tb * T > maxt || tb * sm1 > smax)) tb >>= 1;
+          while (tb > 1 && (tb >> 1) >= v[0].n) tb >>= 1;
+          if (sm1 > smax) return 1;
+          P->tb = tb;
+          P->threads = tb * T;
+          P->smem = (int)(tb * sm1);
+          if (llabs_(is) == 1 && !(kind == GB_KIND_R2C && is != 1))
+               P->load_mode = (T >= 32 && kind != GB_KIND_C2R) ? GB_MOVE_DIRECT : GB_MOVE_ROWS;
+          else if (cols_in) P->load_mode = GB_MOVE_COLS;
+          else P->load_mode = (kind == GB_KIND_C2R) ? GB_MOVE_ROWS : GB_MOVE_DIRECT;
+          if (llabs_(os) == 1)
+               P->store_mode = (T >= 32 && kind != GB_KIND_R2C) ? GB_MOVE_DIRECT : GB_MOVE_ROWS;
+          else if (cols_out) P->store_mode = GB_MOVE_COLS;
+          else P->store_mode = GB_MOVE_DIRECT;
+          if (kind == GB_KIND_R2C && P->store_mode == GB_MOVE_DIRECT && llabs_(os) == 1 && T < 32)
+               P->store_mode = GB_MOVE_ROWS;
+     } else {
+          int k, tb;
+          long long sm1, L = (kind == GB_KIND_BLUESTEIN) ? nfft : nfft;
+          if (kind == GB_KIND_BLUESTEIN) {
+               long long nb = 1;
+               while (nb < 2 * n - 1) nb <<= 1;
+               nfft = nb; L = nb;
+               P->nfft = (int)nb;
+          }
+          k = gb_factor(nfft, P->rad);
+          if (k < 0) return -1;
+          P->nrad = k;
+          P->variant = GB_VAR_GEN;
+          sm1 = 2 * (L + 1) * csize(prec);
+          if (sm1 > smax) return 1;
+          tb = (int)(1024 / nfft); if (tb < 1) tb = 1;
+          if (llabs_(is) != 1 || llabs_(os) != 1) { int want = prec == 4 ? 16 : 8; if (tb < want) tb = want; }
+          if (tb_hint > 0) tb = tb_hint;
+          while (tb > 1 && tb * sm1 > smax) tb >>= 1;
+          while (tb > 1 && (tb >> 1) >= v[0].n) tb >>= 1;
+          P->tb = tb;
+          {
+               long long th = ((long long)tb * nfft / 4 + 31) / 32 * 32;
+               if (th < 64) th = 64;
+               if (th > 512) th = 512;
+               P->threads = (int)th;
+          }
+          P->smem = (int)(tb * sm1);
+          P->load_mode = (llabs_(is) != 1 && llabs_(P->vis[0]) <= 2) ? GB_MOVE_COLS : GB_MOVE_ROWS;
+          P->store_mode = (llabs_(os) != 1 && llabs_(P->vos[0]) <= 2) ? GB_MOVE_COLS : GB_MOVE_ROWS;
+     }
+     P->ntiles0 = (v[0].n + P->tb - 1) / P->tb;
+     P->nblocks = P->ntiles0;
+     for (i = 1; i < nv; ++i) P->nblocks *= v[i].n;
+     return 0;
+}
+
+/* Fill the device tables a configured pass needs. */
+static int pass_tables(gb_pass *P)
+{
+     int prec = P->prec;
+     if (P->kind == GB_KIND_COPY) return 0;
+     P->tw = gb_table_twiddle(prec, P->nfft, P->nfft, 1);
+     if (!P->tw) return -1;
+     if ((P->kind == GB_KIND_R2C || P->kind == GB_KIND_C2R) && P->n % 2 == 0) {
+          P->tw_half = gb_table_twiddle(prec, P->n, P->n / 2 + 1, 1);
+          if (!P->tw_half) return -1;
+     }
+     if (P->kind == GB_KIND_BLUESTEIN) {
+          P->chirp = gb_table_chirp(prec, P->n, P->sign);
+          P->chirp_spec = gb_table_chirp_spec(prec, P->n, P->nfft, P->sign);
+          if (!P->chirp || !P->chirp_spec) return -1;
+     }
+     if (P->post_N) {
+          long long S = 1;
+          while (S * S < P->post_N) S <<= 1;
+          P->post_S = S;
+          P->post_lo = gb_table_twiddle(prec, P->post_N, S, 1);
+          P->post_hi = gb_table_twiddle(prec, P->post_N, (P->post_N + S - 1) / S, S);
+          if (!P->post_lo || !P->post_hi) return -1;
+     }
+     return 0;
+}
+
+/* ------------------------------------------------------------ plan building */
+typedef struct {
+     gb_plan *p;
+     int err;
+} builder;
+
+static gb_step *new_step(builder *b)
+{
+     gb_step *s;
+     if (b->p->nstep >= GB_MAXPASS) { gb_set_error("too many passes"); b->err = 1; return 0; }
+     s = &b->p->step[b->p->nstep++];
+     memset(s, 0, sizeof *s);
+     return s;
+}
+
+static void count_ops(gb_plan *p, const gb_pass *P, long long howmany)
+{
+     double n = P->nfft, lg = n > 1 ? __builtin_log2(n) : 0;
+     double per = 5.0 * n * lg;   /* the 5 N log2 N convention (libbench2/mflops.c:21-27) */
+     if (P->kind == GB_KIND_BLUESTEIN) per = 2 * per + 12.0 * n;
+     p->add += 0.6 * per * howmany;
+     p->mul += 0.4 * per * howmany;
+}
+
+/* Adds the steps of one batched 1D transform: length n along (is, os), batch
+ * dims v (count nv), from buffer src to dst.  Chooses single-CTA kernels,
+ * the in-CTA Bluestein, or the two-pass four-step decomposition. */
+static void add_1d(builder *b, int kind, long long n, int sign, long long is, long long os,
+                   int nv, const gb_dim *v_in, int src, int dst)
+{
+     gb_plan *p = b->p;
+     int prec = p->prb.prec, rc, i;
+     gb_step *s;
+     gb_dim v[GB_MAXRANK + 2];
+     long long howmany = 1;
+     const gb_wisdom_entry *w = 0;
+     int nvk;
+     if (b->err) return;
+     for (i = 0; i < nv; ++i) v[i] = v_in[i];
+     nvk = gb_canon_vec(v, nv);
+     for (i = 0; i < nvk; ++i) howmany *= v[i].n;
+
+     if (n == 1 && kind == GB_KIND_C2C) {
+          /* size-1 DFT: identity copy (nothing to do in place) */
+          if (src == dst) return;
+          s = new_step(b);
+          if (!s) return;
+          {
+               gb_dim vv[GB_MAXRANK + 2];
+               int k = nvk;
+               for (i = 0; i < nvk; ++i) vv[i] = v[i];
+               if (k > GB_MAXV) {
+                    s->nloop = k - GB_MAXV;
+                    for (i = 0; i < s->nloop; ++i) s->loop[i] = vv[i];
+                    config_pass(&s->pass, prec, GB_KIND_COPY, 1, sign, is, os, GB_MAXV, vv + s->nloop, 0, 0);
+               } else config_pass(&s->pass, prec, GB_KIND_COPY, 1, sign, is, os, k, vv, 0, 0);
+          }
+          s->src = src; s->dst = dst;
+          return;
+     }
+
+     if (kind == GB_KIND_C2C) {
+          char key[128];
+          snprintf(key, sizeof key, "c2c p%d n%lld", prec, n);
+          w = gb_wisdom_lookup(key);
+     }
+
+     s = new_step(b);
+     if (!s) return;
+     s->src = src; s->dst = dst;
+     if (nvk > GB_MAXV) {
+          s->nloop = nvk - GB_MAXV;
+          for (i = 0; i < s->nloop; ++i) s->loop[i] = v[i];
+     }
+     rc = config_pass(&s->pass, prec, kind, n, sign, is, os, nvk - s->nloop, v + s->nloop,
+                      w ? w->tb : 0, 0);
+     if (rc == 0) {
+          if (pass_tables(&s->pass)) { b->err = 1; return; }
+          count_ops(p, &s->pass, howmany);
+          return;
+     }
+     --p->nstep;   /* the single-pass attempt is replaced below */
+
+     if (rc < 0 && kind == GB_KIND_C2C) {
+          /* length with a prime factor > 13: Bluestein in one CTA */
+          s = new_step(b);
+          s->src = src; s->dst = dst;
+          if (nvk > GB_MAXV) { s->nloop = nvk - GB_MAXV; for (i = 0; i < s->nloop; ++i) s->loop[i] = v[i]; }
+          rc = config_pass(&s->pass, prec, GB_KIND_BLUESTEIN, n, sign, is, os, nvk - s->nloop, v + s->nloop, 0, 0);
+          if (rc == 0) {
+               if (pass_tables(&s->pass)) { b->err = 1; return; }
+               count_ops(p, &s->pass, howmany);
+               return;
+          }
+          --p->nstep;
+          gb_set_error("length %lld: prime factor too large for a one-CTA Bluestein convolution", n);
+          b->err = 1;
+          return;
+     }
+
+     if (kind == GB_KIND_C2C && rc == 1) {
+          /* four-step: n = n1 * n2, pass A over n1 (stride n2) into scratch
+           * laid out [v][n2][k1] with the W_n^(n2 k1) twiddle, pass B over n2
+           * from scratch into dst at k1 + n1*k2. */
+          long long n1 = 0, n2, d, best = 0, sz;
+          gb_dim va[GB_MAXRANK + 3], vb[GB_MAXRANK + 3];
+          int na = 0, nb = 0, r1, r2;
+          for (d = 2; d * d <= n; ++d) {   /* the most balanced split whose factors fit */
+               if (n % d) continue;
+               {
+                    gb_pass t1, t2;
+                    gb_dim one = {1, 0, 0};
+                    if (config_pass(&t1, prec, GB_KIND_C2C, d, sign, 1, 1, 1, &one, 0, 0) == 0 &&
+                        config_pass(&t2, prec, GB_KIND_C2C, n / d, sign, 1, 1, 1, &one, 0, 0) == 0)
+                         best = d;
+               }
+          }
+          if (!best) {
+               gb_set_error("length %lld is not supported (no two-pass split)", n);
+               b->err = 1;
+               return;
+          }
+          n1 = best; n2 = n / n1;
+          if (w && w->n1 > 0 && n % w->n1 == 0) { n1 = w->n1; n2 = n / n1; }
+          sz = n * howmany;
+          if ((size_t)sz * csize(prec) > p->scratch_bytes) p->scratch_bytes = (size_t)sz * csize(prec);
+          /* pass A: transform over n1 with element stride n2*is; dim0 = n2 */
+          va[na].n = n2; va[na].is = is; va[na].os = n1; ++na;
+          {
+               long long dense = n;
+               for (i = nvk - 1; i >= 0; --i) {
+                    va[na].n = v[i].n; va[na].is = v[i].is; va[na].os = dense; ++na;
+                    dense *= v[i].n;
+               }
+          }
+          s = new_step(b);
+          if (!s) return;
+          s->src = src; s->dst = GB_BUF_SCRATCH;
+          if (na > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
+          /* dim 0 stays n2: the twiddle W_n^(n2 k1) indexes it */
+          r1 = config_pass(&s->pass, prec, GB_KIND_C2C, n1, sign, n2 * is, 1, na, va, 0, 1);
+          s->pass.post_N = n;
+          if (r1 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass A config failed"); b->err = 1; return; }
+          count_ops(p, &s->pass, howmany * n2);
+          /* pass B: transform over n2 (scratch stride n1), dim0 = k1 */
+          vb[nb].n = n1; vb[nb].is = 1; vb[nb].os = os; ++nb;
+          {
+               long long dense = n;
+               for (i = nvk - 1; i >= 0; --i) {
+                    vb[nb].n = v[i].n; vb[nb].is = dense; vb[nb].os = v[i].os; ++nb;
+                    dense *= v[i].n;
+               }
+          }
+          s = new_step(b);
+          if (!s) return;
+          s->src = GB_BUF_SCRATCH; s->dst = dst;
+          if (nb > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
+          r2 = config_pass(&s->pass, prec, GB_KIND_C2C, n2, sign, n1, n1 * os, nb, vb, 0, 1);
+          if (r2 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass B config failed"); b->err = 1; return; }
+          count_ops(p, &s->pass, howmany * n1);
+          return;
+     }
+     gb_set_error("length %lld is not supported for this transform kind", n);
+     b->err = 1;
+}
+
+static void describe(gb_plan *p)
+{
+     int i, off = 0;
+     const char *kn[] = {"dft", "rdft2-r2c", "rdft2-c2r"};
+     off += snprintf(p->desc + off, sizeof p->desc - off, "(gb300-%s-%s",
+                     kn[p->prb.kind], p->prb.prec == 4 ? "f32" : "f64");
+     for (i = 0; i < p->nstep && off < (int)sizeof p->desc - 64; ++i) {
+          const gb_pass *P = &p->step[i].pass;
+          static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy"};
+          static const char *mv[] = {"direct", "rows", "cols"};
+          off += snprintf(p->desc + off, sizeof p->desc - off,
+                          "\n  (pass %s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
+                          kk[P->kind], P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : "gen", P->tb,
+                          P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
+                          P->vn[0], P->post_N ? " +twiddle" : "");
+     }
+     snprintf(p->desc + off, sizeof p->desc - off, ")");
+}
+
+/* Build the steps of a problem.  Returns NULL (with gb_last_error set) when
+ * the problem is invalid or not supported. */
+gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
+{
+     gb_plan *p;
+     builder b;
+     int r = prb->rank, a, i;
+     if (!gb_dry && !gb_cuda_ready()) {
+          gb_set_error("no CUDA device: libfftw3_gb300 runs transforms on the GPU only");
+          return 0;
+     }
+     p = (gb_plan *)calloc(1, sizeof *p);
+     p->refcnt = 1;
+     p->prb = *prb;
+     p->flags = flags;
+     b.p = p; b.err = 0;
+
+     if (prb->kind == GB_PROB_DFT) {
+          if (r == 0) {
+               gb_dim v[GB_MAXRANK];
+               int nv = prb->vrank;
+               for (i = 0; i < nv; ++i) v[i] = prb->vec[i];
+               if (prb->in != prb->out || gb_dry)
+                    add_1d(&b, GB_KIND_C2C, 1, prb->sign, 0, 0, nv, v, GB_BUF_IN, GB_BUF_OUT);
+          }
+          for (a = r - 1; a >= 0 && !b.err; --a) {
+               /* axis a; first pass reads the input, later ones work in place on the output */
+               int first = (a == r - 1);
+               gb_dim v[2 * GB_MAXRANK];
+               int nv = 0;
+               for (i = 0; i < r; ++i)
+                    if (i != a) { v[nv].n = prb->sz[i].n; v[nv].is = first ? prb->sz[i].is : prb->sz[i].os; v[nv].os = prb->sz[i].os; ++nv; }
+               for (i = 0; i < prb->vrank; ++i) {
+                    v[nv].n = prb->vec[i].n; v[nv].is = first ? prb->vec[i].is : prb->vec[i].os; v[nv].os = prb->vec[i].os; ++nv;
+               }
+               add_1d(&b, GB_KIND_C2C, prb->sz[a].n, prb->sign, first ? prb->sz[a].is : prb->sz[a].os,
+                      prb->sz[a].os, nv, v, first ? GB_BUF_IN : GB_BUF_OUT, GB_BUF_OUT);
+          }
+     } else if (prb->kind == GB_PROB_R2C) {
+          /* last axis r2c (in -> out), then c2c forward over the leading axes in place on out */
+          long long nl = prb->sz[r - 1].n;
+          gb_dim v[2 * GB_MAXRANK];
+          int nv = 0;
+          for (i = 0; i < r - 1; ++i) { v[nv] = prb->sz[i]; ++nv; }
+          for (i = 0; i < prb->vrank; ++i) v[nv++] = prb->vec[i];
+          add_1d(&b, GB_KIND_R2C, nl, -1, prb->sz[r - 1].is, prb->sz[r - 1].os, nv, v, GB_BUF_IN, GB_BUF_OUT);
+          for (a = r - 2; a >= 0 && !b.err; --a) {
+               nv = 0;
+               for (i = 0; i < r; ++i) {
+                    if (i == a) continue;
+                    v[nv].n = (i == r - 1) ? nl / 2 + 1 : prb->sz[i].n;
+                    v[nv].is = prb->sz[i].os; v[nv].os = prb->sz[i].os; ++nv;
+               }
+               for (i = 0; i < prb->vrank; ++i) { v[nv].n = prb->vec[i].n; v[nv].is = prb->vec[i].os; v[nv].os = prb->vec[i].os; ++nv; }
+               add_1d(&b, GB_KIND_C2C, prb->sz[a].n, -1, prb->sz[a].os, prb->sz[a].os, nv, v, GB_BUF_OUT, GB_BUF_OUT);
+          }
+     } else {
+          /* c2r: c2c backward over the leading axes in place on the input
+           * (the reference destroys the input here, api/plan-many-dft-c2r.c:41-42),
+           * then the last axis c2r from in to out */
+          long long nl = prb->sz[r - 1].n;
+          gb_dim v[2 * GB_MAXRANK];
+          int nv;
+          for (a = r - 2; a >= 0 && !b.err; --a) {
+               nv = 0;
+               for (i = 0; i < r; ++i) {
+                    if (i == a) continue;
+                    v[nv].n = (i == r - 1) ? nl / 2 + 1 : prb->sz[i].n;
+                    v[nv].is = prb->sz[i].is; v[nv].os = prb->sz[i].is; ++nv;
+               }
+               for (i = 0; i < prb->vrank; ++i) { v[nv].n = prb->vec[i].n; v[nv].is = prb->vec[i].is; v[nv].os = prb->vec[i].is; ++nv; }
+               add_1d(&b, GB_KIND_C2C, prb->sz[a].n, 1, prb->sz[a].is, prb->sz[a].is, nv, v, GB_BUF_IN, GB_BUF_IN);
+          }
+          nv = 0;
+          for (i = 0; i < r - 1; ++i) v[nv++] = prb->sz[i];
+          for (i = 0; i < prb->vrank; ++i) v[nv++] = prb->vec[i];
+          add_1d(&b, GB_KIND_C2R, nl, 1, prb->sz[r - 1].is, prb->sz[r - 1].os, nv, v, GB_BUF_IN, GB_BUF_OUT);
+     }
+     if (b.err) {
+          free(p);
+          return 0;
+     }
+     if (p->scratch_bytes && !gb_dry) {
+          if (cudaMalloc(&p->scratch, p->scratch_bytes) != cudaSuccess) {
+               cudaGetLastError();
+               gb_set_error("cudaMalloc(%zu) for plan scratch failed", p->scratch_bytes);
+               free(p);
+               return 0;
+          }
+     }
+     describe(p);
+     if (getenv("FFTW_GB300_TRACE")) fprintf(stderr, "[fftw_gb300] plan %s\n", p->desc);
+     return p;
+}
+
+void gb_destroy(gb_plan *p)
+{
+     if (!p) return;
+     if (!gb_dry) {
+          if (p->scratch) cudaFree(p->scratch);
+          if (p->stage_in) cudaFree(p->stage_in);
+          if (p->stage_out) cudaFree(p->stage_out);
+     }
+     free(p);
+}

@@ -1,0 +1,99 @@
+/*
+ * Descriptors shared by the host planner (C) and the device kernels (CUDA).
+ *
+ * A plan compiles to a list of passes.  One pass is one kernel launch that
+ * runs a batch of 1D transforms of one length, each read once from HBM and
+ * written once, with the whole transform resident in shared memory/registers.
+ * The batch is described the way the reference describes vector loops: a
+ * list of (n, is, os) dimensions (the reference's vecsz tensor,
+ * dft/dft.h:34-38), strides in elements.
+ */
+#ifndef GB_TYPES_H
+#define GB_TYPES_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_MAXV 4      /* vector dimensions per pass */
+#define GB_MAXRAD 24   /* radix stages per transform */
+
+/* What a pass computes. */
+enum gb_kind {
+     GB_KIND_C2C = 0,       /* complex n -> complex n */
+     GB_KIND_R2C = 1,       /* real n -> complex n/2+1 */
+     GB_KIND_C2R = 2,       /* complex n/2+1 -> real n */
+     GB_KIND_BLUESTEIN = 3, /* complex n -> complex n through a chirp convolution of length nfft */
+     GB_KIND_COPY = 4       /* rank-0 problem: element copy */
+};
+
+/* How the transform is computed inside one CTA. */
+enum gb_variant {
+     GB_VAR_REG = 0,   /* power-of-two length, register-resident Stockham stages of radix <= 16 */
+     GB_VAR_GEN = 1    /* any smooth length, shared-memory Stockham stages, runtime radix list */
+};
+
+/* How a tile of transforms moves between HBM and the CTA. */
+enum gb_move {
+     GB_MOVE_DIRECT = 0,  /* each thread loads/stores its own elements (coalesced when stride is 1) */
+     GB_MOVE_ROWS = 1,    /* cooperative copy through shared memory, element index fastest */
+     GB_MOVE_COLS = 2     /* cooperative copy through shared memory, transform index fastest */
+};
+
+typedef struct gb_pass {
+     int kind;          /* enum gb_kind */
+     int prec;          /* sizeof(real): 4 or 8 */
+     int sign;          /* -1 forward, +1 backward */
+     int n;             /* logical length (real length for r2c/c2r) */
+     int nfft;          /* length of the complex FFT run by the kernel */
+     int variant;       /* enum gb_variant */
+     int tb;            /* transforms per CTA (along vector dimension 0) */
+     int threads;       /* threads per CTA */
+     int smem;          /* dynamic shared memory bytes */
+     int load_mode;     /* enum gb_move */
+     int store_mode;    /* enum gb_move */
+     int real_pairs;    /* r2c input / c2r output: stride 1 and 8-/16-byte aligned pairs */
+     long long is, os;  /* element stride along the transform (complex or real elements) */
+     int nv;            /* number of vector dimensions */
+     long long vn[GB_MAXV], vis[GB_MAXV], vos[GB_MAXV];
+     long long ntiles0;  /* ceil(vn[0] / tb) */
+     long long nblocks;  /* total CTAs */
+     int nrad;
+     int rad[GB_MAXRAD];
+     /* device tables (owned by the plan) */
+     const void *tw;      /* exp(-2 pi i j / nfft), j < nfft */
+     const void *tw_half; /* r2c/c2r: exp(-2 pi i k / n), k <= n/2 */
+     /* four-step: multiply output k of the transform whose index along
+      * vector dimension 0 is v by exp(sign 2 pi i v k / post_N).  The
+      * factor is read from two tables: post_lo[m % post_S] * post_hi[m / post_S]. */
+     long long post_N;
+     long long post_S;
+     const void *post_lo;
+     const void *post_hi;
+     /* Bluestein: chirp w[k] (k < n) and the spectrum of the padded chirp / nfft */
+     const void *chirp;
+     const void *chirp_spec;
+     /* status word for bounded-wait and bounds reporting (device, owned by the library) */
+     int *status;
+} gb_pass;
+
+/* Device status codes written to gb_pass.status. */
+#define GB_STATUS_OK 0
+#define GB_STATUS_BAD_DESCRIPTOR 1
+#define GB_STATUS_QUEUE_TIMEOUT 2
+
+/* Launchers implemented in the .cu files (plain C ABI). */
+int gb_launch_pass(const gb_pass *p, const void *in, void *out, void *stream);
+int gb_pass_configure(gb_pass *p, int max_smem_optin);
+int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream);
+int gb_chirp(void *dst, int prec, long long n, int sign, void *stream);
+int gb_device_max_smem(void);
+const char *gb_last_cuda_error(void);
+long long gb_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

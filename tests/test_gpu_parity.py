@@ -1,0 +1,311 @@
+"""Parity of the CUDA path against the oracle, through the C ABI.
+
+Every transform here is planned and executed with the fftw3.h entry points of
+libfftw3_gb300 on device (or host) arrays, and compared with the oracle: the
+reference's own outputs (golden vectors) or the C restatement of the
+reference algorithms run in long double (double results) / double (float
+results).  Bounds: relative L2 error <= 1e-6 for float, <= 1e-14 for double,
+as the accuracy target of this path states.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"f": 1e-6, "d": 1e-14}
+CT = {"f": np.complex64, "d": np.complex128}
+RT = {"f": np.float32, "d": np.float64}
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _host(t):
+    return t.cpu().numpy()
+
+
+def oracle_c2c(restatement, x, shape, sign, prec):
+    return restatement.c2c(x.astype(np.clongdouble if prec == "d" else np.complex128), shape, sign,
+                           "l" if prec == "d" else "d", nthreads=4)
+
+
+def run_c2c(torch, x, shape, sign, prec, howmany):
+    import fftw3_gb300 as g
+    xi = _dev(torch, x.astype(CT[prec]))
+    yo = torch.empty_like(xi)
+    p = g.plan_many_dft(list(shape), howmany, xi.data_ptr(), yo.data_ptr(), sign, g.FFTW_ESTIMATE, prec)
+    p.execute()
+    torch.cuda.synchronize()
+    return _host(yo), p
+
+
+GC = golden_cases()
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("case", GC, ids=[f"{c['kind']}-{'x'.join(map(str, c['shape']))}-s{c['sign']}" for c in GC])
+def test_golden(lib, torch_cuda, case, prec):
+    """Our library against the reference FFTW's own outputs (golden vectors)."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    kind, shape, hm, x = case["kind"], case["shape"], case["howmany"], case["x"]
+    if kind == "c2c":
+        y, _ = run_c2c(torch, x, shape, case["sign"], prec, hm)
+    elif kind == "r2c":
+        xi = _dev(torch, x.astype(RT[prec]))
+        nc = int(np.prod(shape[:-1])) * (shape[-1] // 2 + 1)
+        yo = torch.empty(hm * nc, dtype=torch.complex64 if prec == "f" else torch.complex128, device="cuda")
+        p = g.plan_many_dft_r2c(list(shape), hm, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE, prec)
+        p.execute()
+        y = _host(yo)
+    else:
+        xi = _dev(torch, x.astype(CT[prec]))
+        yo = torch.empty(hm * int(np.prod(shape)), dtype=torch.float32 if prec == "f" else torch.float64, device="cuda")
+        p = g.plan_many_dft_c2r(list(shape), hm, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE, prec)
+        p.execute()
+        y = _host(yo)
+    err = rel_l2(y, case["yl"])
+    assert err <= TOL[prec], f"rel L2 {err:.3e} > {TOL[prec]}"
+
+
+POW2 = [1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("n", POW2)
+def test_c2c_pow2(lib, torch_cuda, restatement, n, prec):
+    rng = np.random.default_rng(n)
+    hm = max(1, min(64, 65536 // n))
+    x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
+    for sign in (-1, 1):
+        y, _ = run_c2c(torch_cuda, x, [n], sign, prec, hm)
+        assert rel_l2(y, oracle_c2c(restatement, x, [n], sign, prec)) <= TOL[prec]
+
+
+MIXED = [3, 5, 6, 7, 9, 10, 11, 12, 13, 14, 15, 20, 60, 100, 143, 210, 360, 1000, 1001, 2310, 3000, 6561, 10000]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("n", MIXED)
+def test_c2c_mixed_radix(lib, torch_cuda, restatement, n, prec):
+    rng = np.random.default_rng(n + 1)
+    hm = max(1, min(32, 65536 // n))
+    x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
+    for sign in (-1, 1):
+        y, _ = run_c2c(torch_cuda, x, [n], sign, prec, hm)
+        assert rel_l2(y, oracle_c2c(restatement, x, [n], sign, prec)) <= TOL[prec]
+
+
+PRIMES = [17, 19, 31, 101, 173, 257, 1021, 2039, 4093]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("n", PRIMES)
+def test_c2c_bluestein(lib, torch_cuda, restatement, n, prec):
+    if prec == "d" and n > 2048:
+        pytest.skip("double Bluestein convolution above 4096 points is a two-pass plan")
+    rng = np.random.default_rng(n + 2)
+    hm = 4
+    x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
+    for sign in (-1, 1):
+        y, _ = run_c2c(torch_cuda, x, [n], sign, prec, hm)
+        assert rel_l2(y, oracle_c2c(restatement, x, [n], sign, prec)) <= TOL[prec]
+
+
+LARGE = [(1 << 15, "f"), (1 << 16, "f"), (1 << 18, "f"), (1 << 20, "f"), (3 << 14, "f"), (60000, "f"),
+         (1 << 14, "d"), (1 << 16, "d"), (3 * 5 * 7 * 256, "d")]
+
+
+@pytest.mark.parametrize("n,prec", LARGE)
+def test_c2c_fourstep(lib, torch_cuda, restatement, n, prec):
+    rng = np.random.default_rng(n + 3)
+    hm = 2
+    x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
+    for sign in (-1, 1):
+        y, p = run_c2c(torch_cuda, x, [n], sign, prec, hm)
+        assert rel_l2(y, oracle_c2c(restatement, x, [n], sign, prec)) <= TOL[prec]
+
+
+MULTI = [[16, 16], [8, 12], [32, 64], [4, 6, 10], [8, 8, 8], [64, 64, 64], [128, 256], [5, 7, 9], [2, 3, 4, 5]]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("shape", MULTI, ids=["x".join(map(str, s)) for s in MULTI])
+def test_c2c_multid(lib, torch_cuda, restatement, shape, prec):
+    rng = np.random.default_rng(len(shape) * 100 + shape[0])
+    tot = int(np.prod(shape))
+    hm = 2
+    x = rng.standard_normal(tot * hm) + 1j * rng.standard_normal(tot * hm)
+    for sign in (-1, 1):
+        y, _ = run_c2c(torch_cuda, x, shape, sign, prec, hm)
+        assert rel_l2(y, oracle_c2c(restatement, x, shape, sign, prec)) <= TOL[prec]
+
+
+def test_c2c_inplace_3d(lib, torch_cuda, restatement):
+    """plan_dft_3d in place, forward then backward (the 3D in-place workload's layout)."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    shape = [32, 48, 64]
+    rng = np.random.default_rng(5)
+    x = (rng.uniform(-1, 1, int(np.prod(shape))) + 1j * rng.uniform(-1, 1, int(np.prod(shape)))).astype(np.complex64)
+    a = _dev(torch, x)
+    lib_ = g.load()
+    pf = g.Plan(lib_.fftwf_plan_dft_3d(*shape, a.data_ptr(), a.data_ptr(), -1, g.FFTW_ESTIMATE), "f")
+    pb = g.Plan(lib_.fftwf_plan_dft_3d(*shape, a.data_ptr(), a.data_ptr(), 1, g.FFTW_ESTIMATE), "f")
+    pf.execute()
+    yf = _host(a)
+    assert rel_l2(yf, restatement.c2c(x.astype(np.complex128), shape, -1, "d")) <= 1e-6
+    pb.execute()
+    back = _host(a) / np.prod(shape)
+    assert rel_l2(back, x) <= 1e-6
+
+
+def test_strided_embedded(lib, torch_cuda, restatement):
+    """plan_many_dft with istride/idist/inembed/onembed (the advanced layout)."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    rng = np.random.default_rng(9)
+    n, hm = 64, 12
+    # input: howmany interleaved (istride = hm, idist = 1); output: padded rows
+    x = (rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)).astype(np.complex64)
+    xi = _dev(torch, x)
+    odist = n + 5
+    yo = torch.zeros(hm * odist, dtype=torch.complex64, device="cuda")
+    p = g.plan_many_dft([n], hm, xi.data_ptr(), yo.data_ptr(), -1, g.FFTW_ESTIMATE, "f",
+                        inembed=[n], istride=hm, idist=1, onembed=[odist], ostride=1, odist=odist)
+    p.execute()
+    y = _host(yo).reshape(hm, odist)
+    ref = restatement.c2c(x.reshape(n, hm).T.copy().astype(np.complex128), [n], -1, "d").reshape(hm, n)
+    assert rel_l2(y[:, :n], ref) <= 1e-6
+    assert np.all(y[:, n:] == 0), "gaps in the output must stay untouched"
+    # 2D with embedded input rows
+    n0, n1, emb = 12, 20, 24
+    x2 = (rng.standard_normal(n0 * emb) + 1j * rng.standard_normal(n0 * emb)).astype(np.complex64)
+    xi = _dev(torch, x2)
+    yo = torch.zeros(n0 * n1, dtype=torch.complex64, device="cuda")
+    p = g.plan_many_dft([n0, n1], 1, xi.data_ptr(), yo.data_ptr(), 1, g.FFTW_ESTIMATE, "f",
+                        inembed=[n0, emb], istride=1, idist=0, onembed=[n0, n1], ostride=1, odist=0)
+    p.execute()
+    ref = restatement.c2c(x2.reshape(n0, emb)[:, :n1].copy().astype(np.complex128), [n0, n1], 1, "d")
+    assert rel_l2(_host(yo), ref) <= 1e-6
+
+
+R2C_SIZES = [2, 4, 6, 15, 16, 30, 64, 100, 1024, 1000, 4096, 16384, 32768]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("n", R2C_SIZES)
+def test_r2c_c2r_1d(lib, torch_cuda, restatement, n, prec):
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    if prec == "d" and n > 16384:
+        pytest.skip("double r2c above 16384 points is a two-pass plan")
+    rng = np.random.default_rng(n + 4)
+    hm = max(1, min(16, 65536 // n))
+    nc = n // 2 + 1
+    x = rng.standard_normal(n * hm)
+    xi = _dev(torch, x.astype(RT[prec]))
+    yo = torch.empty(hm * nc, dtype=torch.complex64 if prec == "f" else torch.complex128, device="cuda")
+    p = g.plan_many_dft_r2c([n], hm, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE, prec)
+    p.execute()
+    op = "l" if prec == "d" else "d"
+    ref = restatement.r2c(x.astype(np.longdouble if prec == "d" else np.float64), [n], op)
+    assert rel_l2(_host(yo), ref) <= TOL[prec]
+    z = rng.standard_normal(nc * hm) + 1j * rng.standard_normal(nc * hm)
+    zi = _dev(torch, z.astype(CT[prec]))
+    ro = torch.empty(hm * n, dtype=torch.float32 if prec == "f" else torch.float64, device="cuda")
+    q = g.plan_many_dft_c2r([n], hm, zi.data_ptr(), ro.data_ptr(), g.FFTW_ESTIMATE, prec)
+    q.execute()
+    ref = restatement.c2r(z.astype(np.clongdouble if prec == "d" else np.complex128), [n], op)
+    assert rel_l2(_host(ro), ref) <= TOL[prec]
+
+
+@pytest.mark.parametrize("shape", [[8, 6], [64, 64], [5, 7, 9], [16, 32, 30], [256, 512]], ids=str)
+def test_r2c_c2r_multid(lib, torch_cuda, restatement, shape):
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    rng = np.random.default_rng(sum(shape))
+    tot = int(np.prod(shape))
+    nc = tot // shape[-1] * (shape[-1] // 2 + 1)
+    x = rng.standard_normal(tot)
+    xi = _dev(torch, x.astype(np.float32))
+    yo = torch.empty(nc, dtype=torch.complex64, device="cuda")
+    p = g.plan_many_dft_r2c(shape, 1, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE, "f")
+    p.execute()
+    assert rel_l2(_host(yo), restatement.r2c(x, shape, "d")) <= 1e-6
+    z = rng.standard_normal(nc) + 1j * rng.standard_normal(nc)
+    zi = _dev(torch, z.astype(np.complex64))
+    ro = torch.empty(tot, dtype=torch.float32, device="cuda")
+    q = g.plan_many_dft_c2r(shape, 1, zi.data_ptr(), ro.data_ptr(), g.FFTW_ESTIMATE, "f")
+    q.execute()
+    assert rel_l2(_host(ro), restatement.c2r(z, shape, "d")) <= 1e-6
+
+
+def test_r2c_inplace_padded(lib, torch_cuda, restatement):
+    """In-place r2c with rows padded to 2*(n/2+1) reals (api/rdft2-pad.c:33)."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    n, hm = 30, 5
+    pad = 2 * (n // 2 + 1)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((hm, n))
+    buf = np.zeros((hm, pad), dtype=np.float32)
+    buf[:, :n] = x
+    a = _dev(torch, buf.ravel())
+    p = g.plan_many_dft_r2c([n], hm, a.data_ptr(), a.data_ptr(), g.FFTW_ESTIMATE, "f")
+    p.execute()
+    y = _host(a).view(np.complex64)
+    assert rel_l2(y, restatement.r2c(x.ravel(), [n], "d")) <= 1e-6
+
+
+def test_host_arrays_staged(lib, torch_cuda, restatement):
+    """Host (numpy / fftwf_malloc) arrays go through device staging."""
+    import ctypes
+    import fftw3_gb300 as g
+    rng = np.random.default_rng(12)
+    n, hm = 1024, 8
+    x = (rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)).astype(np.complex64)
+    y = np.zeros_like(x)
+    p = g.plan_many_dft([n], hm, x.ctypes.data, y.ctypes.data, -1, g.FFTW_ESTIMATE, "f")
+    p.execute()
+    assert rel_l2(y, restatement.c2c(x.astype(np.complex128), [n], -1, "d")) <= 1e-6
+    # fftwf_malloc memory (page-locked), in place
+    lib_ = g.load()
+    ptr = lib_.fftwf_malloc(x.nbytes)
+    buf = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_float)), shape=(2 * n * hm,))
+    buf[:] = x.view(np.float32)
+    q = g.plan_many_dft([n], hm, ptr, ptr, 1, g.FFTW_ESTIMATE, "f")
+    q.execute()
+    got = buf.view(np.complex64).copy()
+    assert rel_l2(got, restatement.c2c(x.astype(np.complex128), [n], 1, "d")) <= 1e-6
+    q.destroy()
+    lib_.fftwf_free(ptr)
+
+
+def test_new_array_execute_and_roundtrip(lib, torch_cuda):
+    """execute_dft on new arrays; backward(forward(x)) / N == x."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    n, hm = 4096, 64
+    rng = np.random.default_rng(1)
+    x = (rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)).astype(np.complex64)
+    a, b = _dev(torch, x), torch.empty(n * hm, dtype=torch.complex64, device="cuda")
+    c = torch.empty_like(b)
+    pf = g.plan_many_dft([n], hm, a.data_ptr(), b.data_ptr(), -1, g.FFTW_ESTIMATE, "f")
+    pb = g.plan_many_dft([n], hm, a.data_ptr(), b.data_ptr(), 1, g.FFTW_ESTIMATE, "f")
+    pf.execute_dft(a.data_ptr(), b.data_ptr())
+    pb.execute_dft(b.data_ptr(), c.data_ptr())
+    assert rel_l2(_host(c) / n, x) <= 1e-6
+    before = g.launch_count()
+    pf.execute()
+    assert g.launch_count() == before + 1
