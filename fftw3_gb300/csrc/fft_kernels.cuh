@@ -6,13 +6,14 @@
  *             elements in registers; stages of radix <= 16 exchange through
  *             padded shared memory.  Kinds: c2c (with the optional four-step
  *             output twiddle), r2c (hc2c post-pass fused after the last
- *             stage), c2r (hc2c pre-pass fused before the first stage).
+ *             stage), c2r (hc2c pre-pass fused before the first stage),
+ *             Bluestein (any n with a power-of-two convolution length: chirp
+ *             multiply, FFT, spectrum multiply, inverse FFT, chirp multiply,
+ *             all inside one CTA).
  *   k_gen  -- any length whose factors are in {2,3,4,5,7,8,11,13,16}: stages
  *             ping-pong between two shared-memory buffers with a runtime
  *             radix list.  Kinds: c2c, r2c, c2r (even n through the half-length
- *             complex FFT, odd n through the full-length one), and Bluestein
- *             (chirp multiply, FFT, spectrum multiply, inverse FFT, chirp
- *             multiply, all inside one CTA).
+ *             complex FFT, odd n through the full-length one).
  *
  * These replace, on the reference side: dft/ct.c + dft/dftw-direct.c +
  * dft/direct.c with their codelets (the stages), dft/vrank-geq1.c (the batch
@@ -223,6 +224,57 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
           const long long bi = tile.bi + v * P.vis[0];
           const long long bo = tile.bo + v * P.vos[0];
           C x[E];
+
+          if constexpr (KIND == GB_KIND_BLUESTEIN) {
+               /* dft/bluestein.c:82-128 in one CTA: b = x conj(w) zero-padded to
+                * N, FFT, times the chirp spectrum, inverse FFT, times conj(w) */
+               const C *__restrict__ w = (const C *)P.chirp;
+               const int nn = P.n;
+               if (P.load_mode == GB_MOVE_DIRECT) {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                         const int k = tid + T * e;
+                         C a = mk<C>(0, 0);
+                         if (valid && k < nn) a = cmul(io<C>::ldc(in, bi, k, P.is), cconj(__ldg(w + k)));
+                         x[e] = a;
+                    }
+               } else {
+                    coop_load<C, true, false>(P, in, sm, SMS, tile, nn, P.load_mode);
+                    __syncthreads();
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                         const int k = tid + T * e;
+                         x[e] = (k < nn) ? cmul(smt[pad_idx(k)], cconj(__ldg(w + k))) : mk<C>(0, 0);
+                    }
+                    __syncthreads();
+               }
+               reg_stages<C, N, -1, 1>(x, tid, smt, tw);
+               const C *__restrict__ spec = (const C *)P.chirp_spec;
+#pragma unroll
+               for (int e = 0; e < E; ++e) x[e] = cmul(x[e], __ldg(spec + tid + T * e));
+               reg_stages<C, N, 1, 1>(x, tid, smt, tw);
+#pragma unroll
+               for (int e = 0; e < E; ++e) {
+                    const int k = tid + T * e;
+                    if (k < nn) x[e] = cmul(x[e], cconj(__ldg(w + k)));
+               }
+               if (P.store_mode == GB_MOVE_DIRECT) {
+                    if (valid) {
+#pragma unroll
+                         for (int e = 0; e < E; ++e) {
+                              const int k = tid + T * e;
+                              if (k < nn) io<C>::stc(out, bo, k, P.os, x[e]);
+                         }
+                    }
+               } else {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) smt[pad_idx(tid + T * e)] = x[e];
+                    __syncthreads();
+                    coop_store<C, true, false>(P, out, sm, SMS, tile, nn, P.store_mode);
+                    __syncthreads();
+               }
+               continue;
+          }
 
           /* ---------------- load (and c2r pre-pass) ---------------- */
           if constexpr (KIND == GB_KIND_C2R) {
@@ -445,36 +497,12 @@ __global__ void __launch_bounds__(1024) k_gen(const gb_pass P, const void *__res
                          b0[t * sms + k] = a;
                     }
                }
-          } else { /* Bluestein: b = x * conj(w), zero-padded to nfft */
-               const C *__restrict__ w = (const C *)P.chirp;
-               for (int idx = threadIdx.x; idx < P.tb * N; idx += blockDim.x) {
-                    int t, j;
-                    if (P.load_mode == GB_MOVE_COLS) { t = idx % P.tb; j = idx / P.tb; }
-                    else { t = idx / N; j = idx - t * N; }
-                    const long long v = tile.v0 + t;
-                    C x = mk<C>(0, 0);
-                    if (j < n && v < P.vn[0]) {
-                         x = io<C>::ldc(in, tile.bi + v * P.vis[0], j, P.is);
-                         x = cmul(x, cconj(__ldg(w + j)));
-                    }
-                    b0[t * sms + j] = x;
-               }
           }
           __syncthreads();
 
           /* ---------------- stages ---------------- */
           C *res;
-          if (kind == GB_KIND_BLUESTEIN) {
-               res = gen_fft<C, -1>(b0, b1, P, N, sms, tw);
-               const C *__restrict__ W = (const C *)P.chirp_spec;
-               for (int idx = threadIdx.x; idx < P.tb * N; idx += blockDim.x) {
-                    const int t = idx / N, j = idx - t * N;
-                    res[t * sms + j] = cmul(res[t * sms + j], __ldg(W + j));
-               }
-               __syncthreads();
-               C *other = (res == b0) ? b1 : b0;
-               res = gen_fft<C, 1>(res, other, P, N, sms, tw);
-          } else if (DIR < 0) {
+          if (DIR < 0) {
                res = gen_fft<C, -1>(b0, b1, P, N, sms, tw);
           } else {
                res = gen_fft<C, 1>(b0, b1, P, N, sms, tw);
@@ -520,16 +548,6 @@ __global__ void __launch_bounds__(1024) k_gen(const gb_pass P, const void *__res
                          const long long v = tile.v0 + t;
                          if (v < P.vn[0]) ((R *)out)[tile.bo + v * P.vos[0] + j * P.os] = res[t * sms + j].x;
                     }
-               }
-          } else { /* Bluestein: X[k] = conv[k] * conj(w[k]), k < n */
-               const C *__restrict__ w = (const C *)P.chirp;
-               for (int idx = threadIdx.x; idx < P.tb * n; idx += blockDim.x) {
-                    int t, k;
-                    if (P.store_mode == GB_MOVE_COLS) { t = idx % P.tb; k = idx / P.tb; }
-                    else { t = idx / n; k = idx - t * n; }
-                    const long long v = tile.v0 + t;
-                    if (v < P.vn[0])
-                         io<C>::stc(out, tile.bo + v * P.vos[0], k, P.os, cmul(res[t * sms + k], cconj(__ldg(w + k))));
                }
           }
           __syncthreads();

@@ -127,7 +127,7 @@ static const void *pick_kernel(const gb_pass *p)
           return p->prec == 4 ? gb_reg_kernel_f(logn, p->kind, p->sign) : gb_reg_kernel_d(logn, p->kind, p->sign);
      }
      int dir = p->sign;
-     if (p->kind == GB_KIND_R2C || p->kind == GB_KIND_BLUESTEIN) dir = -1;
+     if (p->kind == GB_KIND_R2C) dir = -1;
      if (p->kind == GB_KIND_C2R) dir = 1;
      if (p->prec == 4) return dir < 0 ? (const void *)k_gen<float2, -1> : (const void *)k_gen<float2, 1>;
      return dir < 0 ? (const void *)k_gen<double2, -1> : (const void *)k_gen<double2, 1>;
@@ -152,6 +152,25 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           return -1;
      }
      if (p->nblocks <= 0) return 0;
+     /* descriptor checks: a pass that would read a missing table or exceed
+      * the launch limits is refused on the host instead of run */
+     {
+          const char *bad = 0;
+          if (p->kind != GB_KIND_COPY && !p->tw) bad = "twiddle table missing";
+          else if ((p->kind == GB_KIND_R2C || p->kind == GB_KIND_C2R) && p->n % 2 == 0 && !p->tw_half)
+               bad = "half-length twiddle table missing";
+          else if (p->kind == GB_KIND_BLUESTEIN && (!p->chirp || !p->chirp_spec)) bad = "chirp tables missing";
+          else if (p->kind == GB_KIND_BLUESTEIN && p->variant != GB_VAR_REG) bad = "Bluestein needs the register variant";
+          else if (p->post_N && (!p->post_lo || !p->post_hi || p->post_S <= 0)) bad = "four-step twiddle tables missing";
+          else if (p->threads < 1 || p->threads > 1024 || p->tb < 1 || p->nv < 1 || p->nv > GB_MAXV) bad = "bad launch shape";
+          else if (p->variant == GB_VAR_REG && p->kind != GB_KIND_COPY &&
+                   p->threads != p->tb * (p->nfft / reg_e(p->nfft))) bad = "thread count does not match the tile";
+          else if (p->variant == GB_VAR_REG && p->threads > reg_maxthreads(p->nfft)) bad = "tile exceeds the kernel's launch bounds";
+          if (bad) {
+               snprintf(gb_errbuf, sizeof gb_errbuf, "refused pass (kind %d nfft %d): %s", p->kind, p->nfft, bad);
+               return -1;
+          }
+     }
      if (p->smem > 48 * 1024) {
           if (gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, p->smem),
                        "cudaFuncSetAttribute(max dynamic smem)"))

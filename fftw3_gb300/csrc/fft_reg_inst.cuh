@@ -12,6 +12,7 @@ static const void *reg_pick(int kind, int dir)
                                              : (const void *)k_reg<GB_CT, L, 1, GB_KIND_C2C>;
      if (kind == GB_KIND_R2C) return (const void *)k_reg<GB_CT, L, -1, GB_KIND_R2C>;
      if (kind == GB_KIND_C2R) return (const void *)k_reg<GB_CT, L, 1, GB_KIND_C2R>;
+     if (kind == GB_KIND_BLUESTEIN && L >= 5) return (const void *)k_reg<GB_CT, L, -1, GB_KIND_BLUESTEIN>;
      return 0;
 }
 

@@ -125,6 +125,7 @@ const void *gb_table_chirp(int prec, long long n, int sign)
 
 static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os,
                        int nv, const gb_dim *v, int tb_hint, int keep_order);
+static int pass_tables(gb_pass *P);
 
 /* Spectrum of the padded chirp / nb (dft/bluestein.c:52-80), computed on the
  * device with this library's own forward FFT. */
@@ -144,7 +145,10 @@ const void *gb_table_chirp_spec(int prec, long long n, long long nb, int sign)
           return 0;
      }
      d.n = 1; d.is = 0; d.os = 0;
-     if (config_pass(&P, prec, GB_KIND_C2C, nb, -1, 1, 1, 1, &d, 0, 0) != 0) return 0;
+     if (config_pass(&P, prec, GB_KIND_C2C, nb, -1, 1, 1, 1, &d, 0, 0) != 0 || pass_tables(&P) != 0) {
+          gb_set_error("chirp spectrum: no forward FFT of length %lld", nb);
+          return 0;
+     }
      if (gb_launch_pass(&P, p, p, 0) || cudaDeviceSynchronize() != cudaSuccess) {
           gb_set_error("chirp spectrum failed: %s", gb_last_cuda_error());
           return 0;
@@ -251,8 +255,14 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
           return 0;
      }
 
-     if (is_pow2(nfft) && ilog2(nfft) <= reg_max_log(prec) && kind != GB_KIND_BLUESTEIN &&
-         (kind == GB_KIND_C2C || half)) {
+     if (kind == GB_KIND_BLUESTEIN) {   /* convolution length: power of two >= 2n-1 */
+          long long nb = 1;
+          while (nb < 2 * n - 1) nb <<= 1;
+          nfft = nb;
+          P->nfft = (int)nb;
+     }
+     if (is_pow2(nfft) && ilog2(nfft) <= reg_max_log(prec) &&
+         (kind == GB_KIND_C2C || kind == GB_KIND_BLUESTEIN || half) && !(kind == GB_KIND_BLUESTEIN && nfft < 32)) {
           int E = reg_e((int)nfft), T = (int)nfft / E, tb, maxt = reg_maxthreads((int)nfft);
           int cols_in, cols_out;
           long long sm1 = (long long)reg_sms((int)nfft) * csize(prec);
@@ -282,13 +292,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                P->store_mode = GB_MOVE_ROWS;
      } else {
           int k, tb;
-          long long sm1, L = (kind == GB_KIND_BLUESTEIN) ? nfft : nfft;
-          if (kind == GB_KIND_BLUESTEIN) {
-               long long nb = 1;
-               while (nb < 2 * n - 1) nb <<= 1;
-               nfft = nb; L = nb;
-               P->nfft = (int)nb;
-          }
+          long long sm1, L = nfft;
           k = gb_factor(nfft, P->rad);
           if (k < 0) return -1;
           P->nrad = k;

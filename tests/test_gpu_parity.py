@@ -262,7 +262,7 @@ def test_r2c_inplace_padded(lib, torch_cuda, restatement):
     buf = np.zeros((hm, pad), dtype=np.float32)
     buf[:, :n] = x
     a = _dev(torch, buf.ravel())
-    p = g.plan_many_dft_r2c([n], hm, a.data_ptr(), a.data_ptr(), g.FFTW_ESTIMATE, "f")
+    p = g.plan_many_dft_r2c([n], hm, a.data_ptr(), a.data_ptr(), g.FFTW_ESTIMATE, "f", idist=pad, odist=pad // 2)
     p.execute()
     y = _host(a).view(np.complex64)
     assert rel_l2(y, restatement.r2c(x.ravel(), [n], "d")) <= 1e-6

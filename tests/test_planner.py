@@ -1,0 +1,127 @@
+"""Host planner logic, checked without a GPU (dry-run plans): how problems
+become passes (per-axis multi-d, four-step split for long transforms,
+Bluestein for large primes, tile/move choices for strided axes), and the
+wisdom text format."""
+import ctypes
+
+import pytest
+
+import fftw3_gb300 as g
+
+
+@pytest.fixture(autouse=True)
+def dry(lib):
+    g.set_dry_run(True)
+    yield
+    g.set_dry_run(False)
+
+
+def passes(p):
+    return p.passes()
+
+
+def test_batched_1d_is_one_pass():
+    p = g.plan_many_dft([4096], 65536, 1 << 20, 1 << 30, prec="f")
+    (ps,) = passes(p)
+    assert ps["nfft"] == 4096 and ps["variant"] == 0 and ps["blocks"] * ps["tb"] >= 65536
+
+
+def test_double_precision_pass():
+    p = g.plan_many_dft([1024], 4096, 1 << 20, 1 << 30, prec="d")
+    (ps,) = passes(p)
+    assert ps["nfft"] == 1024 and ps["variant"] == 0
+
+
+def test_long_transform_is_two_passes_with_scratch(lib):
+    p = g.plan_many_dft([1 << 20], 64, 1 << 20, 1 << 30, prec="f")
+    ps = passes(p)
+    assert len(ps) == 2
+    assert ps[0]["nfft"] * ps[1]["nfft"] == 1 << 20
+    assert lib.fftwf_gb300_scratch_bytes(p.ptr) == (1 << 20) * 64 * 8
+
+
+def test_smooth_nonpow2_uses_generic_stages():
+    p = g.plan_many_dft([60], 100, 1 << 20, 1 << 30, prec="f")
+    (ps,) = passes(p)
+    assert ps["variant"] == 1 and ps["nfft"] == 60
+
+
+def test_prime_uses_bluestein_power_of_two():
+    p = g.plan_many_dft([1021], 10, 1 << 20, 1 << 30, prec="f")
+    (ps,) = passes(p)
+    assert ps["kind"] == 3 and ps["nfft"] == 2048
+
+
+def test_3d_is_one_pass_per_axis():
+    p = g.plan_many_dft([512, 512, 512], 1, 1 << 20, 1 << 20, prec="f")
+    ps = passes(p)
+    assert [x["nfft"] for x in ps] == [512, 512, 512]
+    d = p.describe()
+    assert d.count("ld=cols") == 2   # the two strided axes move tiles of columns
+
+
+def test_r2c_2d_is_r2c_then_c2c():
+    p = g.plan_many_dft_r2c([8192, 8192], 1, 1 << 20, 1 << 30, prec="f")
+    ps = passes(p)
+    assert ps[0]["kind"] == 1 and ps[0]["nfft"] == 4096
+    assert ps[1]["kind"] == 0 and ps[1]["nfft"] == 8192
+
+
+def test_c2r_multid_does_c2c_first():
+    p = g.plan_many_dft_c2r([64, 64], 1, 1 << 20, 1 << 30, prec="f")
+    ps = passes(p)
+    assert ps[0]["kind"] == 0 and ps[1]["kind"] == 2
+
+
+def test_vector_dims_merge():
+    """Contiguous howmany dims collapse into one (kernel/tensor7.c)."""
+    lib = g.load()
+    IOD = g.IODim * 1
+    H = g.IODim * 2
+    dims = IOD(g.IODim(256, 1, 1))
+    hm = H(g.IODim(10, 256 * 20, 256 * 20), g.IODim(20, 256, 256))
+    p = g.Plan(lib.fftwf_plan_guru_dft(1, dims, 2, hm, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE), "f")
+    (ps,) = passes(p)
+    assert ps["blocks"] * ps["tb"] >= 200
+
+
+def test_rank0_copy_and_inplace_noop():
+    lib = g.load()
+    n = (ctypes.c_int * 1)(1)
+    p = lib.fftwf_plan_many_dft(0, n, 5, 1 << 20, None, 1, 1, 1 << 21, None, 1, 1, -1, g.FFTW_ESTIMATE)
+    assert p
+    lib.fftwf_destroy_plan(p)
+
+
+def test_wisdom_roundtrip_and_rejection(lib):
+    lib.fftwf_forget_wisdom()
+    w = b'(fftw-3.3.10-gb300 fftwf_wisdom #x67623330304c4942\n  (gb300-pass "c2c p4 n4096" #x0 #x2 #x0 #x0 #x0)\n)\n'
+    assert lib.fftwf_import_wisdom_from_string(w) == 1
+    out = ctypes.string_at(lib.fftwf_export_wisdom_to_string())
+    assert b'"c2c p4 n4096" #x0 #x2' in out
+    # the reference's own wisdom format is rejected, and existing wisdom kept
+    ref_style = b"(fftw-3.3.10 fftwf_wisdom #x4be12fff #x7b2df9b2 #xa5975329 #x385b0041\n)\n"
+    assert lib.fftwf_import_wisdom_from_string(ref_style) == 0
+    assert lib.fftwf_import_wisdom_from_string(b"(fftw-3.3.10-gb300 fftwf_wisdom #x1\n)") == 0
+    assert lib.fftwf_import_wisdom_from_string(w[:-10]) == 0     # truncated
+    assert lib.fftw_import_wisdom_from_string(w) == 0            # other precision
+    out2 = ctypes.string_at(lib.fftwf_export_wisdom_to_string())
+    assert out2 == out
+    # tb from wisdom is used by the planner
+    p = g.plan_many_dft([4096], 64, 1 << 20, 1 << 30, prec="f")
+    assert passes(p)[0]["tb"] == 2
+    lib.fftwf_forget_wisdom()
+    assert b"gb300-pass" not in ctypes.string_at(lib.fftwf_export_wisdom_to_string())
+
+
+def test_wisdom_only_without_wisdom_is_null(lib):
+    lib.fftwf_forget_wisdom()
+    n = (ctypes.c_int * 1)(4096)
+    p = lib.fftwf_plan_many_dft(1, n, 1, 1 << 20, None, 1, 4096, 1 << 21, None, 1, 4096, -1, g.FFTW_WISDOM_ONLY)
+    assert not p
+
+
+def test_print_plan_names_passes():
+    p = g.plan_many_dft([4096], 16, 1 << 20, 1 << 30, prec="f")
+    s = p.describe()
+    assert s.startswith("(gb300-dft-f32") and "nfft=4096" in s
