@@ -49,6 +49,47 @@ WORKLOADS = {
 METRIC = "FFT Gflop/s (5N log2N/t) & HBM %peak: split-FP16 TC vs FP32, rel err<=1e-6"
 
 
+def smooth_set(lo=60, hi=60000):
+    """{2^a 3^b 5^c 7^d} within [lo, hi]."""
+    out = set()
+    a = 1
+    while a <= hi:
+        b = a
+        while b <= hi:
+            c = b
+            while c <= hi:
+                d = c
+                while d <= hi:
+                    if d >= lo:
+                        out.add(d)
+                    d *= 7
+                c *= 5
+            b *= 3
+        a *= 2
+    return sorted(out)
+
+
+def primes_in(lo, hi):
+    return [p for p in range(max(2, lo), hi + 1) if all(p % q for q in range(2, int(p ** 0.5) + 1))]
+
+
+def uneven_lengths(rng, count, max_pow2=16, max_smooth=60000, max_prime=4093):
+    """Seeded uneven batch: 60% powers of two 2^6..2^max_pow2 (log-uniform),
+    30% smooth composites 2^a3^b5^c7^d in [60, max_smooth], 10% primes in
+    [17, max_prime]."""
+    sm = smooth_set(60, max_smooth)
+    pr = primes_in(17, max_prime)
+    out = []
+    for u in rng.random(count):
+        if u < 0.6:
+            out.append(1 << int(rng.integers(6, max_pow2 + 1)))
+        elif u < 0.9:
+            out.append(int(sm[int(rng.integers(0, len(sm)))]))
+        else:
+            out.append(int(pr[int(rng.integers(0, len(pr)))]))
+    return out
+
+
 def flops_per_step(kind, shape, howmany):
     n = math.prod(shape)
     f = 5.0 * n * math.log2(n) * howmany
@@ -214,6 +255,8 @@ def run_ours(args):
     b.build()
     lib = g.load()
     kind, shape, howmany, prec, inplace = WORKLOADS[args.workload]
+    if args.howmany:
+        howmany = args.howmany
     n = math.prod(shape)
     cdt = torch.complex64 if prec == "f" else torch.complex128
     rdt = torch.float32 if prec == "f" else torch.float64
@@ -321,6 +364,107 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_uneven(args):
+    """10,000 independent fftwf c2c forward transforms of seeded uneven
+    lengths as one plan set: one work-queue kernel in one CUDA graph launch
+    per step; beside it the same plans executed one after another."""
+    import ctypes
+    import numpy as np
+    import torch
+    import fftw3_gb300 as g
+    from fftw3_gb300 import build as b
+    from oracle.oracle import Restatement, rel_l2
+    b.build()
+    lib = g.load()
+    torch.cuda.set_device(0)
+    count = args.howmany or 10000
+    lengths = uneven_lengths(np.random.default_rng(2024), count)
+    offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    gen = torch.Generator(device="cuda").manual_seed(1234)
+    xin = torch.randn(int(offs[-1]), dtype=torch.complex64, device="cuda", generator=gen)
+    yout = torch.zeros_like(xin)
+    es = xin.element_size()
+    t0 = time.perf_counter()
+    plans = [g.plan_many_dft([int(n)], 1, xin.data_ptr() + int(offs[i]) * es, yout.data_ptr() + int(offs[i]) * es,
+                             -1, g.FFTW_ESTIMATE, "f") for i, n in enumerate(lengths)]
+    plan_s = time.perf_counter() - t0
+    arr = (ctypes.c_void_p * len(plans))(*[p.ptr for p in plans])
+    lib.fftwf_gb300_plan_set.restype = ctypes.c_void_p
+    lib.fftwf_gb300_plan_set.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint]
+    lib.fftwf_gb300_execute_set.argtypes = [ctypes.c_void_p]
+    lib.fftwf_gb300_set_stream_set.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    lib.fftwf_gb300_set_info.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 5
+    t0 = time.perf_counter()
+    s = lib.fftwf_gb300_plan_set(len(plans), arr, g.FFTW_ESTIMATE)
+    set_s = time.perf_counter() - t0
+    if not s:
+        raise RuntimeError("plan set failed: " + g.last_error())
+    stream = torch.cuda.current_stream()
+    lib.fftwf_gb300_set_stream_set(s, stream.cuda_stream, 1)
+    info = [ctypes.c_int() for _ in range(5)]
+    lib.fftwf_gb300_set_info(s, *[ctypes.byref(v) for v in info])
+    fl = sum(5.0 * n * math.log2(n) for n in lengths if n > 1)
+    for _ in range(args.warmup):
+        lib.fftwf_gb300_execute_set(s)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            lib.fftwf_gb300_execute_set(s)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    # the same plans one after another (async, one launch or more each)
+    for p in plans:
+        p.set_stream(stream.cuda_stream)
+        p.set_async(True)
+    for p in plans:
+        p.execute()
+    torch.cuda.synchronize()
+    l0 = g.launch_count()
+    ev0.record(stream)
+    for _ in range(max(1, args.steps // 4)):
+        for p in plans:
+            p.execute()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_loop = ev0.elapsed_time(ev1) / max(1, args.steps // 4)
+    loop_launches = (g.launch_count() - l0) // max(1, args.steps // 4)
+    lib.fftwf_gb300_execute_set(s)
+    torch.cuda.synchronize()
+    # per-transform error against the FP64 oracle on a sample
+    R = Restatement()
+    xh, yh = xin.cpu().numpy(), yout.cpu().numpy()
+    rng = np.random.default_rng(5)
+    sample = sorted(set(rng.integers(0, len(lengths), 200).tolist()))
+    errs = []
+    for i in sample:
+        a, c = int(offs[i]), int(offs[i + 1])
+        errs.append(rel_l2(yh[a:c], R.c2c(xh[a:c].astype(np.complex128), [c - a], -1, "d")))
+    alg = 2 * int(offs[-1]) * 8
+    hbm, src = peaks()
+    out = {
+        "metric": METRIC, "value": round(fl / (ms * 1e-3) / 1e9, 2), "unit": "Gflop/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"uneven{count}: {count} fftwf c2c forward plans, seeded lengths (60% 2^6..2^16, 30% 2^a3^b5^c7^d in [60,60000], 10% primes in [17,4093]) as one plan set",
+                   "distinct_lengths": len(set(lengths)), "points": int(offs[-1]),
+                   "queue_items": info[0].value, "long_transforms": info[2].value, "grid": info[3].value,
+                   "smem": info[4].value, "plan_s": round(plan_s, 2), "set_build_s": round(set_s, 2),
+                   "rel_l2_max_sample": max(errs), "rel_l2_median_sample": float(np.median(errs)),
+                   "sampled_transforms": len(sample)},
+        "gbs": round(alg / (ms * 1e-3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "achieved": round(alg / (ms * 1e-3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(alg / (ms * 1e-3) / 1e9 / hbm, 4), "traffic": None, "peak_source": src},
+        "gpu_launches": args.steps, "launch_note": "one CUDA graph launch (one work-queue kernel) per step",
+        "loop_baseline": {"value": round(fl / (ms_loop * 1e-3) / 1e9, 2), "ms_per_step": round(ms_loop, 3),
+                          "kernel_launches_per_step": loop_launches},
+        "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,
+    }
+    print(json.dumps(out))
+
+
 def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
     """fftwf_execute_dft on page-locked host arrays: H2D + passes + D2H timed."""
     import ctypes
@@ -360,7 +504,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2c4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2c4096", choices=sorted(WORKLOADS) + ["uneven10k"])
+    ap.add_argument("--howmany", type=int, default=0, help="override the batch (profiling runs only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -368,6 +513,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.workload == "uneven10k":
+        run_uneven(args)
     else:
         run_ours(args)
 

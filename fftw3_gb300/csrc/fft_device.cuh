@@ -208,4 +208,59 @@ __device__ __forceinline__ void cexp_fp64(long long m, long long n, int sign, do
      *s_out = sign < 0 ? -s : s;
 }
 
+/* ---- asynchronous bulk copies (TMA engine) and mbarriers, inline PTX ---- */
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+/* make the initialised barriers visible to the async proxy */
+__device__ __forceinline__ void mbar_fence_init()
+{
+     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+/* global -> shared bulk copy; bytes multiple of 16, both addresses 16-byte aligned */
+__device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src_gmem, unsigned bytes, unsigned long long *bar)
+{
+     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                  ::"r"(smem_u32(dst_smem)), "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+/* order this thread's earlier generic-proxy shared accesses before later async-proxy ones */
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+     unsigned long long t;
+     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+     return t;
+}
+
+/* Wait until the barrier's phase with the given parity completes.  Bounded:
+ * gives up after limit_ns of wall time and returns false. */
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, unsigned long long limit_ns)
+{
+     unsigned done = 0;
+     unsigned long long t0 = 0;
+     for (unsigned it = 0;; ++it) {
+          asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                       : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+          if (done) return true;
+          if (it == 0) t0 = globaltimer_ns();
+          else if ((it & 63) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
+     }
+}
+
 } /* namespace gb */

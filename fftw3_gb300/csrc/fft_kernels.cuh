@@ -13,14 +13,18 @@
  *   k_gen  -- any length whose factors are in {2,3,4,5,7,8,11,13,16}: stages
  *             ping-pong between two shared-memory buffers with a runtime
  *             radix list.  Kinds: c2c, r2c, c2r (even n through the half-length
- *             complex FFT, odd n through the full-length one).
+ *             complex FFT, odd n through the full-length one), Rader
+ *             (prime n with a smooth n-1: permute by generator powers,
+ *             convolve with omega through FFT(n-1), unpermute) and
+ *             Bluestein; the tile body (gen_tile) is shared with the
+ *             work-queue kernel.
  *
  * These replace, on the reference side: dft/ct.c + dft/dftw-direct.c +
  * dft/direct.c with their codelets (the stages), dft/vrank-geq1.c (the batch
  * is the grid), dft/buffered.c and dft/indirect*.c (strided tiles are staged
  * through shared memory), rdft/ct-hc2c.c + rdft/ct-hc2c-direct.c (fused
  * pre/post-passes), dft/generic.c (small prime radices as register
- * butterflies) and dft/bluestein.c (fused convolution).
+ * butterflies), dft/bluestein.c and dft/rader.c (fused convolutions).
  */
 #pragma once
 #include "fft_device.cuh"
@@ -28,10 +32,22 @@
 
 namespace gb {
 
-__host__ __device__ constexpr int pad_idx(int p) { return p + (p >> 4); }
+/* Shared-memory swizzle of k_reg: one (or two) padding elements after every
+ * 16.  Two when the first stage is radix 16, so its 16 consecutive outputs
+ * stay 16-byte aligned and go out as 128-bit stores; both choices keep the
+ * strided stage accesses free of bank conflicts (checked by enumerating the
+ * addresses of every warp). */
+__host__ __device__ constexpr int pad_mult(int nfft)
+{
+     int r = nfft;
+     while (r > 16) r /= 16;
+     return (r == 16 && nfft >= 256) ? 2 : 1;
+}
+__host__ __device__ constexpr int pad_for(int nfft, int p) { return p + pad_mult(nfft) * (p >> 4); }
 
-/* Shared-memory stride (in complex elements) of one transform in k_reg. */
-__host__ __device__ constexpr int reg_sms(int nfft) { return pad_idx(nfft) + 2; }
+/* Shared-memory stride (in complex elements) of one transform in k_reg
+ * (the host planner's gb_reg_sms computes the same value). */
+__host__ __device__ constexpr int reg_sms(int nfft) { return (nfft + pad_mult(nfft) * (nfft >> 4) + 3) & ~1; }
 
 __host__ __device__ constexpr int reg_e(int nfft) { return nfft < 16 ? nfft : 16; }
 
@@ -115,7 +131,7 @@ template <typename C> __device__ __forceinline__ C post_twiddle(const gb_pass &P
  * array).  PADDED applies the k_reg shared-memory swizzle. */
 template <typename C, bool PADDED, bool PAIRS_REAL>
 __device__ __forceinline__ void coop_load(const gb_pass &P, const void *in, C *sm, int sms, const tile_t &tl,
-                                          int L, int mode)
+                                          int L, int mode, int nfft = 0)
 {
      const int tb = P.tb;
      const int total = tb * L;
@@ -127,14 +143,14 @@ __device__ __forceinline__ void coop_load(const gb_pass &P, const void *in, C *s
           if (v < P.vn[0]) {
                long long base = tl.bi + v * P.vis[0];
                C x = PAIRS_REAL ? io<C>::ldpair(in, base, j, P.is, P.real_pairs) : io<C>::ldc(in, base, j, P.is);
-               sm[t * sms + (PADDED ? pad_idx(j) : j)] = x;
+               sm[t * sms + (PADDED ? pad_for(nfft, j) : j)] = x;
           }
      }
 }
 
 template <typename C, bool PADDED, bool PAIRS_REAL>
 __device__ __forceinline__ void coop_store(const gb_pass &P, void *out, const C *sm, int sms, const tile_t &tl,
-                                           int L, int mode)
+                                           int L, int mode, int nfft = 0)
 {
      const int tb = P.tb;
      const int total = tb * L;
@@ -145,7 +161,7 @@ __device__ __forceinline__ void coop_store(const gb_pass &P, void *out, const C 
           long long v = tl.v0 + t;
           if (v < P.vn[0]) {
                long long base = tl.bo + v * P.vos[0];
-               C x = sm[t * sms + (PADDED ? pad_idx(j) : j)];
+               C x = sm[t * sms + (PADDED ? pad_for(nfft, j) : j)];
                if (PAIRS_REAL) io<C>::stpair(out, base, j, P.os, P.real_pairs, x);
                else io<C>::stc(out, base, j, P.os, x);
           }
@@ -156,6 +172,41 @@ __device__ __forceinline__ void coop_store(const gb_pass &P, void *out, const C 
  * k_reg: power-of-two, register-resident
  * ==================================================================== */
 
+/* Twiddles of one radix-RAD butterfly: v[r] *= W_N^(r*m), r = 1..RAD-1,
+ * from the table tw (exp(-2 pi i j/N), conjugated for DIR > 0).  Only the
+ * powers 1, 2, 4, 8 are read; the others are products of at most two read
+ * or derived factors (each factor then carries at most three roundings). */
+template <int DIR, int RAD, typename C>
+__device__ __forceinline__ void apply_twiddles(C *v, const C *__restrict__ tw, int m)
+{
+     if constexpr (RAD == 2) {
+          v[1] = cmul(v[1], twid<DIR>(tw, m));
+     } else if constexpr (RAD == 4) {
+          const C w1 = twid<DIR>(tw, m), w2 = twid<DIR>(tw, 2 * m);
+          v[1] = cmul(v[1], w1);
+          v[2] = cmul(v[2], w2);
+          v[3] = cmul(v[3], cmul(w1, w2));
+     } else if constexpr (RAD == 8) {
+          const C w1 = twid<DIR>(tw, m), w2 = twid<DIR>(tw, 2 * m), w4 = twid<DIR>(tw, 4 * m);
+          const C w3 = cmul(w1, w2);
+          v[1] = cmul(v[1], w1); v[2] = cmul(v[2], w2); v[3] = cmul(v[3], w3); v[4] = cmul(v[4], w4);
+          v[5] = cmul(v[5], cmul(w4, w1)); v[6] = cmul(v[6], cmul(w4, w2)); v[7] = cmul(v[7], cmul(w4, w3));
+     } else if constexpr (RAD == 16) {
+          const C w1 = twid<DIR>(tw, m), w2 = twid<DIR>(tw, 2 * m), w4 = twid<DIR>(tw, 4 * m),
+                  w8 = twid<DIR>(tw, 8 * m);
+          const C w3 = cmul(w1, w2), w12 = cmul(w8, w4);
+          v[1] = cmul(v[1], w1); v[2] = cmul(v[2], w2); v[3] = cmul(v[3], w3); v[4] = cmul(v[4], w4);
+          v[5] = cmul(v[5], cmul(w4, w1)); v[6] = cmul(v[6], cmul(w4, w2)); v[7] = cmul(v[7], cmul(w4, w3));
+          v[8] = cmul(v[8], w8);
+          v[9] = cmul(v[9], cmul(w8, w1)); v[10] = cmul(v[10], cmul(w8, w2)); v[11] = cmul(v[11], cmul(w8, w3));
+          v[12] = cmul(v[12], w12);
+          v[13] = cmul(v[13], cmul(w12, w1)); v[14] = cmul(v[14], cmul(w12, w2)); v[15] = cmul(v[15], cmul(w12, w3));
+     } else {
+#pragma unroll
+          for (int r = 1; r < RAD; ++r) v[r] = cmul(v[r], twid<DIR>(tw, r * m));
+     }
+}
+
 template <typename C, int N, int DIR, int NS>
 __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, const C *__restrict__ tw)
 {
@@ -164,6 +215,9 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
      constexpr int RAD = (NS == 1) ? reg_r0(N) : E;
      constexpr int B = E / RAD;
      constexpr bool LAST = (NS * RAD == N);
+     /* first radix-16 stage of a float transform: 16 consecutive outputs,
+      * written as eight 128-bit stores (the swizzle keeps them aligned) */
+     constexpr bool VEC = (NS == 1) && (RAD == 16) && !LAST && (sizeof(C) == 8) && (pad_mult(N) == 2);
 #pragma unroll
      for (int b = 0; b < B; ++b) {
           const int j = tid + b * T;
@@ -171,24 +225,26 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
           C v[RAD];
 #pragma unroll
           for (int r = 0; r < RAD; ++r) v[r] = x[b + r * B];
-          if (NS > 1) {
-#pragma unroll
-               for (int r = 1; r < RAD; ++r) v[r] = cmul(v[r], twid<DIR>(tw, r * k * (N / (NS * RAD))));
-          }
+          if (NS > 1) apply_twiddles<DIR, RAD>(v, tw, k * (N / (NS * RAD)));
           bfly<RAD, DIR>::run(v);
           if (LAST) {
 #pragma unroll
                for (int q = 0; q < RAD; ++q) x[b + q * B] = v[q];
+          } else if constexpr (VEC) {
+               float4 *d = (float4 *)(smt + pad_for(N, j * 16));
+#pragma unroll
+               for (int q = 0; q < 8; ++q)
+                    d[q] = make_float4(v[2 * q].x, v[2 * q].y, v[2 * q + 1].x, v[2 * q + 1].y);
           } else {
                const int base = (j / NS) * NS * RAD + k;
 #pragma unroll
-               for (int q = 0; q < RAD; ++q) smt[pad_idx(base + q * NS)] = v[q];
+               for (int q = 0; q < RAD; ++q) smt[pad_for(N, base + q * NS)] = v[q];
           }
      }
      if constexpr (!LAST) {
           __syncthreads();
 #pragma unroll
-          for (int e = 0; e < E; ++e) x[e] = smt[pad_idx(tid + T * e)];
+          for (int e = 0; e < E; ++e) x[e] = smt[pad_for(N, tid + T * e)];
           __syncthreads();
           reg_stages<C, N, DIR, NS * RAD>(x, tid, smt, tw);
      }
@@ -239,12 +295,12 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
                          x[e] = a;
                     }
                } else {
-                    coop_load<C, true, false>(P, in, sm, SMS, tile, nn, P.load_mode);
+                    coop_load<C, true, false>(P, in, sm, SMS, tile, nn, P.load_mode, N);
                     __syncthreads();
 #pragma unroll
                     for (int e = 0; e < E; ++e) {
                          const int k = tid + T * e;
-                         x[e] = (k < nn) ? cmul(smt[pad_idx(k)], cconj(__ldg(w + k))) : mk<C>(0, 0);
+                         x[e] = (k < nn) ? cmul(smt[pad_for(N, k)], cconj(__ldg(w + k))) : mk<C>(0, 0);
                     }
                     __syncthreads();
                }
@@ -268,9 +324,9 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
                     }
                } else {
 #pragma unroll
-                    for (int e = 0; e < E; ++e) smt[pad_idx(tid + T * e)] = x[e];
+                    for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
                     __syncthreads();
-                    coop_store<C, true, false>(P, out, sm, SMS, tile, nn, P.store_mode);
+                    coop_store<C, true, false>(P, out, sm, SMS, tile, nn, P.store_mode, N);
                     __syncthreads();
                }
                continue;
@@ -280,13 +336,13 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
           if constexpr (KIND == GB_KIND_C2R) {
                /* X[0..N] -> shared, then Z'[k] = (X[k] + conj X[N-k])
                 *                 + i conj(W_2N^k) (X[k] - conj X[N-k])  */
-               coop_load<C, true, false>(P, in, sm, SMS, tile, N + 1, P.load_mode);
+               coop_load<C, true, false>(P, in, sm, SMS, tile, N + 1, P.load_mode, N);
                __syncthreads();
                const C *__restrict__ th = (const C *)P.tw_half;
 #pragma unroll
                for (int e = 0; e < E; ++e) {
                     const int k = tid + T * e;
-                    C a = smt[pad_idx(k)], b = smt[pad_idx(N - k)];
+                    C a = smt[pad_for(N, k)], b = smt[pad_for(N, N - k)];
                     if (k == 0) { a.y = 0; b.y = 0; }
                     b.y = -b.y;
                     C s = cadd(a, b), d = csub(a, b);
@@ -309,10 +365,10 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
                     for (int e = 0; e < E; ++e) x[e] = mk<C>(0, 0);
                }
           } else {
-               coop_load<C, true, KIND == GB_KIND_R2C>(P, in, sm, SMS, tile, N, P.load_mode);
+               coop_load<C, true, KIND == GB_KIND_R2C>(P, in, sm, SMS, tile, N, P.load_mode, N);
                __syncthreads();
 #pragma unroll
-               for (int e = 0; e < E; ++e) x[e] = smt[pad_idx(tid + T * e)];
+               for (int e = 0; e < E; ++e) x[e] = smt[pad_for(N, tid + T * e)];
                __syncthreads();
           }
 
@@ -323,13 +379,13 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
           if constexpr (KIND == GB_KIND_R2C) {
                /* X[k] = (Z[k] + conj Z[N-k])/2 + W_2N^k (Z[k] - conj Z[N-k])/(2i), k = 0..N */
 #pragma unroll
-               for (int e = 0; e < E; ++e) smt[pad_idx(tid + T * e)] = x[e];
+               for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
                __syncthreads();
                const C *__restrict__ th = (const C *)P.tw_half;
 #pragma unroll
                for (int e = 0; e < E; ++e) {
                     const int k = tid + T * e;
-                    C a = smt[pad_idx(k)], b = smt[pad_idx((N - k) & (N - 1))];
+                    C a = smt[pad_for(N, k)], b = smt[pad_for(N, (N - k) & (N - 1))];
                     b.y = -b.y;
                     C ev = cscale(cadd(a, b), (R)0.5);
                     C dd = csub(a, b);
@@ -337,7 +393,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
                     C w = __ldg(th + k);
                     x[e] = cadd(ev, cmul(w, od));
                }
-               C last = smt[pad_idx(0)];
+               C last = smt[pad_for(N, 0)];
                __syncthreads();
                if (P.store_mode == GB_MOVE_DIRECT) {
                     if (valid) {
@@ -347,10 +403,10 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
                     }
                } else {
 #pragma unroll
-                    for (int e = 0; e < E; ++e) smt[pad_idx(tid + T * e)] = x[e];
-                    if (tid == 0) smt[pad_idx(N)] = mk<C>(last.x - last.y, 0);
+                    for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
+                    if (tid == 0) smt[pad_for(N, N)] = mk<C>(last.x - last.y, 0);
                     __syncthreads();
-                    coop_store<C, true, false>(P, out, sm, SMS, tile, N + 1, P.store_mode);
+                    coop_store<C, true, false>(P, out, sm, SMS, tile, N + 1, P.store_mode, N);
                     __syncthreads();
                }
           } else {
@@ -372,11 +428,104 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
                     }
                } else {
 #pragma unroll
-                    for (int e = 0; e < E; ++e) smt[pad_idx(tid + T * e)] = x[e];
+                    for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
                     __syncthreads();
-                    coop_store<C, true, RP>(P, out, sm, SMS, tile, N, P.store_mode);
+                    coop_store<C, true, RP>(P, out, sm, SMS, tile, N, P.store_mode, N);
                     __syncthreads();
                }
+          }
+     }
+}
+
+/* ======================================================================
+ * k_reg_tma: persistent variant of k_reg for unit-stride c2c batches whose
+ * transforms start on 16-byte boundaries.  Each CTA walks its tiles with a
+ * two-slot pipeline: while the tile in one shared-memory slot is being
+ * transformed, the TMA engine copies the next tile into the other slot
+ * (cp.async.bulk, completion tracked by an mbarrier), so HBM reads overlap
+ * the arithmetic.  Results are stored straight from registers.
+ * ==================================================================== */
+
+__host__ __device__ constexpr int tma_sms(int nfft) { return reg_sms(nfft); }
+
+template <typename C, int N>
+__device__ __forceinline__ void tma_issue(const gb_pass &P, const void *in, long long blk, C *dst,
+                                          unsigned long long *bar)
+{
+     const tile_t tl = tile_of(P, blk);
+     const long long rem = P.vn[0] - tl.v0;
+     const int ntr = rem < P.tb ? (int)rem : P.tb;
+     const unsigned bytes = (unsigned)(N * sizeof(C));
+     mbar_expect_tx(bar, bytes * (unsigned)ntr);
+     for (int t = 0; t < ntr; ++t)
+          bulk_g2s(dst + t * tma_sms(N), (const C *)in + tl.bi + (tl.v0 + t) * P.vis[0], bytes, bar);
+}
+
+#define GB_WAIT_NS 2000000000ull   /* bound on any wait for a copy: 2 s */
+
+template <typename C, int LOGN, int DIR>
+__global__ void __launch_bounds__(256, 3) k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+{
+     constexpr int N = 1 << LOGN;
+     constexpr int E = reg_e(N);
+     constexpr int T = N / E;
+     constexpr int SMS = tma_sms(N);
+     extern __shared__ __align__(128) unsigned char gb_smem[];
+     __shared__ __align__(8) unsigned long long bar[2];
+     C *const buf0 = (C *)gb_smem;
+     C *const buf1 = buf0 + P.tb * SMS;
+     const int tl = threadIdx.x / T;
+     const int tid = threadIdx.x - tl * T;
+     const C *__restrict__ tw = (const C *)P.tw;
+
+     if (threadIdx.x == 0) {
+          mbar_init(&bar[0], 1);
+          mbar_init(&bar[1], 1);
+          mbar_fence_init();
+     }
+     __syncthreads();
+     const long long stride = gridDim.x;
+     long long blk = blockIdx.x;
+     if (threadIdx.x == 0 && blk < P.nblocks) tma_issue<C, N>(P, in, blk, buf0, &bar[0]);
+     unsigned parity = 0;   /* bit b: parity of the next phase of bar[b] */
+
+     for (int it = 0; blk < P.nblocks; blk += stride, ++it) {
+          const int b = it & 1;
+          C *const cur = b ? buf1 : buf0;
+          const long long nxt = blk + stride;
+          const bool issued = nxt < P.nblocks;
+          if (threadIdx.x == 0 && issued) {
+               fence_proxy_async_smem();
+               tma_issue<C, N>(P, in, nxt, b ? buf0 : buf1, &bar[b ^ 1]);
+          }
+          const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u, GB_WAIT_NS);
+          if (!__syncthreads_and(ok)) {
+               /* the copy never completed: report, drain the other slot, leave */
+               if (threadIdx.x == 0) {
+                    if (issued) mbar_wait(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u, GB_WAIT_NS);
+                    if (P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
+               }
+               return;
+          }
+          parity ^= 1u << b;
+
+          const tile_t tile = tile_of(P, blk);
+          const long long v = tile.v0 + tl;
+          const bool valid = v < P.vn[0];
+          const long long bo = tile.bo + v * P.vos[0];
+          C *smt = cur + tl * SMS;
+          C x[E];
+#pragma unroll
+          for (int e = 0; e < E; ++e) x[e] = smt[tid + T * e];
+          __syncthreads();
+          reg_stages<C, N, DIR, 1>(x, tid, smt, tw);
+          if (P.post_N) {
+#pragma unroll
+               for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
+          }
+          if (valid) {
+#pragma unroll
+               for (int e = 0; e < E; ++e) io<C>::stc(out, bo, tid + T * e, P.os, x[e]);
           }
      }
 }
@@ -438,119 +587,226 @@ __device__ C *gen_fft(C *b0, C *b1, const gb_pass &P, int N, int sms, const C *_
      return src;
 }
 
-template <typename C, int DIR>
-__global__ void __launch_bounds__(1024) k_gen(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+/* Transform base addresses of one tile: strided (tile.bi + v * vis[0]) or,
+ * for work-queue items that group transforms of different arrays, one
+ * pointer per transform (pin/pout, element 0 of each transform). */
+struct gen_addr {
+     const void *in;
+     void *out;
+     const void *const *pin;
+     void *const *pout;
+};
+
+template <typename C> __device__ __forceinline__ const C *src_of(const gb_pass &P, const tile_t &tl, const gen_addr &A, int t)
+{
+     const long long v = tl.v0 + t;
+     if (A.pin) return (const C *)A.pin[v];
+     return (const C *)A.in + tl.bi + v * P.vis[0];
+}
+template <typename C> __device__ __forceinline__ C *dst_of(const gb_pass &P, const tile_t &tl, const gen_addr &A, int t)
+{
+     const long long v = tl.v0 + t;
+     if (A.pout) return (C *)A.pout[v];
+     return (C *)A.out + tl.bo + v * P.vos[0];
+}
+__device__ __forceinline__ void tile_index(int idx, int tb, int L, int mode, int &t, int &j)
+{
+     if (mode == GB_MOVE_COLS) { t = idx % tb; j = idx / tb; }
+     else { t = idx / L; j = idx - t * L; }
+}
+
+/* One tile of k_gen: load, stages (direction from P.sign), store.  Also the
+ * body of the work-queue kernel.  b0/b1: two shared buffers of tb*(nfft+1). */
+template <typename C>
+__device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A, C *b0, C *b1)
 {
      typedef typename real_of<C>::T R;
-     extern __shared__ __align__(16) unsigned char gb_smem[];
      const int N = P.nfft;
      const int sms = N + 1;
-     C *b0 = (C *)gb_smem;
-     C *b1 = b0 + P.tb * sms;
+     const int tb = P.tb;
      const C *__restrict__ tw = (const C *)P.tw;
      const int n = P.n;
      const int kind = P.kind;
      const bool half = (kind == GB_KIND_R2C || kind == GB_KIND_C2R) && (n % 2 == 0);
+     const long long vn0 = P.vn[0];
 
+     /* ---------------- load ---------------- */
+     if (kind == GB_KIND_C2C || kind == GB_KIND_RADER || (kind == GB_KIND_C2R) || (kind == GB_KIND_R2C && half)) {
+          /* complex elements (real pairs for even r2c) into b0, or into b1
+           * for the kinds that rearrange them afterwards */
+          C *dst = (kind == GB_KIND_C2C || kind == GB_KIND_R2C) ? b0 : b1;
+          const int L = (kind == GB_KIND_RADER) ? n : (kind == GB_KIND_C2R) ? n / 2 + 1 : N;
+          for (int idx = threadIdx.x; idx < tb * L; idx += blockDim.x) {
+               int t, j;
+               tile_index(idx, tb, L, P.load_mode, t, j);
+               if (tile.v0 + t < vn0) {
+                    C x;
+                    if (kind == GB_KIND_R2C) {
+                         const R *r = (const R *)src_of<R>(P, tile, A, t);
+                         x = P.real_pairs ? ((const C *)r)[j] : mk<C>(r[2 * j * P.is], r[(2 * j + 1) * P.is]);
+                    } else x = src_of<C>(P, tile, A, t)[j * P.is];
+                    dst[t * sms + j] = x;
+               }
+          }
+     } else if (kind == GB_KIND_R2C) {
+          /* odd n: real sequence as complex with zero imaginary part */
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+               int t, j;
+               tile_index(idx, tb, N, P.load_mode, t, j);
+               if (tile.v0 + t < vn0) b0[t * sms + j] = mk<C>(src_of<R>(P, tile, A, t)[j * P.is], 0);
+          }
+     } else if (kind == GB_KIND_BLUESTEIN) {
+          /* b = x conj(w), zero-padded to nfft (dft/bluestein.c:82-95) */
+          const C *__restrict__ w = (const C *)P.chirp;
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+               int t, j;
+               tile_index(idx, tb, N, P.load_mode, t, j);
+               C x = mk<C>(0, 0);
+               if (j < n && tile.v0 + t < vn0) x = cmul(src_of<C>(P, tile, A, t)[j * P.is], cconj(__ldg(w + j)));
+               b0[t * sms + j] = x;
+          }
+     }
+     __syncthreads();
+     if (kind == GB_KIND_RADER) {
+          /* dft/rader.c:95-165: b[k] = x[g^k], k < n-1; x[0] kept in the unused
+           * slot N of buffer 0 */
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+               const int t = idx / N, k = idx - t * N;
+               b0[t * sms + k] = b1[t * sms + __ldg(P.perm + k)];
+               if (k == 0) b0[t * sms + N] = b1[t * sms];
+          }
+          __syncthreads();
+     } else if (kind == GB_KIND_C2R) {
+          const int nc = n / 2 + 1;
+          if (half) {
+               /* hc2c pre-pass (rdft/ct-hc2c.c:72-83) */
+               const C *__restrict__ th = (const C *)P.tw_half;
+               for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+                    const int t = idx / N, k = idx - t * N;
+                    C a = b1[t * sms + k], b = b1[t * sms + N - k];
+                    if (k == 0) { a.y = 0; b.y = 0; }
+                    b.y = -b.y;
+                    C s = cadd(a, b), d = csub(a, b);
+                    C w = __ldg(th + k);
+                    C cd = mk<C>(w.x * d.x + w.y * d.y, w.x * d.y - w.y * d.x);
+                    b0[t * sms + k] = mk<C>(s.x - cd.y, s.y + cd.x);
+               }
+          } else {
+               /* odd n: Hermitian extension of X[0..(n-1)/2] */
+               for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+                    const int t = idx / N, k = idx - t * N;
+                    C a = (k < nc) ? b1[t * sms + k] : cconj(b1[t * sms + (N - k)]);
+                    if (k == 0) a.y = 0;
+                    b0[t * sms + k] = a;
+               }
+          }
+          __syncthreads();
+     }
+
+     /* ---------------- stages ---------------- */
+     C *res;
+     if (kind == GB_KIND_RADER || kind == GB_KIND_BLUESTEIN) {
+          /* convolution: forward FFT, spectrum multiply, inverse FFT.  Rader
+           * also records X[0] = x[0] + B[0] in slot N of buffer 1. */
+          res = gen_fft<C, -1>(b0, b1, P, N, sms, tw);
+          const C *__restrict__ W = (const C *)P.chirp_spec;
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+               const int t = idx / N, k = idx - t * N;
+               const C bk = res[t * sms + k];
+               if (kind == GB_KIND_RADER && k == 0) b1[t * sms + N] = cadd(b0[t * sms + N], bk);
+               res[t * sms + k] = cmul(bk, __ldg(W + k));
+          }
+          __syncthreads();
+          res = gen_fft<C, 1>(res, res == b0 ? b1 : b0, P, N, sms, tw);
+     } else if (P.sign < 0) {
+          res = gen_fft<C, -1>(b0, b1, P, N, sms, tw);
+     } else {
+          res = gen_fft<C, 1>(b0, b1, P, N, sms, tw);
+     }
+
+     /* ---------------- store ---------------- */
+     if (kind == GB_KIND_C2C) {
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+               int t, k;
+               tile_index(idx, tb, N, P.store_mode, t, k);
+               const long long v = tile.v0 + t;
+               if (v < vn0) {
+                    C y = res[t * sms + k];
+                    if (P.post_N) y = cmul(y, post_twiddle<C>(P, v * (long long)k));
+                    dst_of<C>(P, tile, A, t)[k * P.os] = y;
+               }
+          }
+     } else if (kind == GB_KIND_BLUESTEIN) {
+          /* X[k] = conv[k] conj(w[k]), k < n */
+          const C *__restrict__ w = (const C *)P.chirp;
+          for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x) {
+               int t, k;
+               tile_index(idx, tb, n, P.store_mode, t, k);
+               if (tile.v0 + t < vn0)
+                    dst_of<C>(P, tile, A, t)[k * P.os] = cmul(res[t * sms + k], cconj(__ldg(w + k)));
+          }
+     } else if (kind == GB_KIND_RADER) {
+          /* X[0] from slot N of buffer 1; X[g^-k] = x[0] + conv[k] */
+          const int *__restrict__ lg = P.perm + N;
+          for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x) {
+               int t, j;
+               tile_index(idx, tb, n, P.store_mode, t, j);
+               if (tile.v0 + t < vn0) {
+                    const C y = (j == 0) ? b1[t * sms + N] : cadd(b0[t * sms + N], res[t * sms + __ldg(lg + j - 1)]);
+                    dst_of<C>(P, tile, A, t)[j * P.os] = y;
+               }
+          }
+     } else if (kind == GB_KIND_R2C) {
+          const int nc = n / 2 + 1;
+          C *src = res;
+          if (half) {
+               /* hc2c post-pass (rdft/ct-hc2c.c:197-210) into the free buffer */
+               C *dst = (res == b0) ? b1 : b0;
+               const C *__restrict__ th = (const C *)P.tw_half;
+               for (int idx = threadIdx.x; idx < tb * nc; idx += blockDim.x) {
+                    const int t = idx / nc, k = idx - t * nc;
+                    C a = res[t * sms + (k % N)], b = res[t * sms + ((N - k) % N)];
+                    b.y = -b.y;
+                    C ev = cscale(cadd(a, b), (R)0.5);
+                    C dd = csub(a, b);
+                    C od = mk<C>(dd.y * (R)0.5, -dd.x * (R)0.5);
+                    dst[t * sms + k] = cadd(ev, cmul(__ldg(th + k), od));
+               }
+               __syncthreads();
+               src = dst;
+          }
+          for (int idx = threadIdx.x; idx < tb * nc; idx += blockDim.x) {
+               int t, k;
+               tile_index(idx, tb, nc, P.store_mode, t, k);
+               if (tile.v0 + t < vn0) dst_of<C>(P, tile, A, t)[k * P.os] = src[t * sms + k];
+          }
+     } else if (kind == GB_KIND_C2R) {
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
+               int t, j;
+               tile_index(idx, tb, N, P.store_mode, t, j);
+               if (tile.v0 + t < vn0) {
+                    R *r = dst_of<R>(P, tile, A, t);
+                    const C y = res[t * sms + j];
+                    if (!half) r[j * P.os] = y.x;
+                    else if (P.real_pairs) ((C *)r)[j] = y;
+                    else { r[2 * j * P.os] = y.x; r[(2 * j + 1) * P.os] = y.y; }
+               }
+          }
+     }
+     __syncthreads();
+}
+
+template <typename C>
+__global__ void __launch_bounds__(512) k_gen(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+{
+     extern __shared__ __align__(16) unsigned char gb_smem[];
+     C *b0 = (C *)gb_smem;
+     C *b1 = b0 + P.tb * (P.nfft + 1);
+     gen_addr A;
+     A.in = in; A.out = out; A.pin = 0; A.pout = 0;
      for (long long blk = blockIdx.x; blk < P.nblocks; blk += gridDim.x) {
           const tile_t tile = tile_of(P, blk);
-          /* ---------------- load ---------------- */
-          if (kind == GB_KIND_C2C) {
-               coop_load<C, false, false>(P, in, b0, sms, tile, N, P.load_mode);
-          } else if (kind == GB_KIND_R2C) {
-               if (half) coop_load<C, false, true>(P, in, b0, sms, tile, N, P.load_mode);
-               else {
-                    /* odd n: real sequence as complex with zero imaginary part */
-                    for (int idx = threadIdx.x; idx < P.tb * N; idx += blockDim.x) {
-                         int t, j;
-                         if (P.load_mode == GB_MOVE_COLS) { t = idx % P.tb; j = idx / P.tb; }
-                         else { t = idx / N; j = idx - t * N; }
-                         const long long v = tile.v0 + t;
-                         if (v < P.vn[0]) {
-                              const R *r = (const R *)in + tile.bi + v * P.vis[0];
-                              b0[t * sms + j] = mk<C>(r[j * P.is], 0);
-                         }
-                    }
-               }
-          } else if (kind == GB_KIND_C2R) {
-               const int nc = n / 2 + 1;
-               coop_load<C, false, false>(P, in, b1, sms, tile, nc, P.load_mode);
-               __syncthreads();
-               if (half) {
-                    const C *__restrict__ th = (const C *)P.tw_half;
-                    for (int idx = threadIdx.x; idx < P.tb * N; idx += blockDim.x) {
-                         const int t = idx / N, k = idx - t * N;
-                         C a = b1[t * sms + k], b = b1[t * sms + N - k];
-                         if (k == 0) { a.y = 0; b.y = 0; }
-                         b.y = -b.y;
-                         C s = cadd(a, b), d = csub(a, b);
-                         C w = __ldg(th + k);
-                         C cd = mk<C>(w.x * d.x + w.y * d.y, w.x * d.y - w.y * d.x);
-                         b0[t * sms + k] = mk<C>(s.x - cd.y, s.y + cd.x);
-                    }
-               } else {
-                    /* odd n: Hermitian extension of X[0..(n-1)/2] */
-                    for (int idx = threadIdx.x; idx < P.tb * N; idx += blockDim.x) {
-                         const int t = idx / N, k = idx - t * N;
-                         C a = (k < nc) ? b1[t * sms + k] : cconj(b1[t * sms + (N - k)]);
-                         if (k == 0) a.y = 0;
-                         b0[t * sms + k] = a;
-                    }
-               }
-          }
-          __syncthreads();
-
-          /* ---------------- stages ---------------- */
-          C *res;
-          if (DIR < 0) {
-               res = gen_fft<C, -1>(b0, b1, P, N, sms, tw);
-          } else {
-               res = gen_fft<C, 1>(b0, b1, P, N, sms, tw);
-          }
-
-          /* ---------------- store ---------------- */
-          if (kind == GB_KIND_C2C) {
-               if (P.post_N) {
-                    for (int idx = threadIdx.x; idx < P.tb * N; idx += blockDim.x) {
-                         const int t = idx / N, k = idx - t * N;
-                         const long long v = tile.v0 + t;
-                         res[t * sms + k] = cmul(res[t * sms + k], post_twiddle<C>(P, v * (long long)k));
-                    }
-                    __syncthreads();
-               }
-               coop_store<C, false, false>(P, out, res, sms, tile, N, P.store_mode);
-          } else if (kind == GB_KIND_R2C) {
-               const int nc = n / 2 + 1;
-               C *dst = (res == b0) ? b1 : b0;
-               if (half) {
-                    const C *__restrict__ th = (const C *)P.tw_half;
-                    for (int idx = threadIdx.x; idx < P.tb * nc; idx += blockDim.x) {
-                         const int t = idx / nc, k = idx - t * nc;
-                         C a = res[t * sms + (k % N)], b = res[t * sms + ((N - k) % N)];
-                         b.y = -b.y;
-                         C ev = cscale(cadd(a, b), (R)0.5);
-                         C dd = csub(a, b);
-                         C od = mk<C>(dd.y * (R)0.5, -dd.x * (R)0.5);
-                         dst[t * sms + k] = cadd(ev, cmul(__ldg(th + k), od));
-                    }
-                    __syncthreads();
-                    coop_store<C, false, false>(P, out, dst, sms, tile, nc, P.store_mode);
-               } else {
-                    coop_store<C, false, false>(P, out, res, sms, tile, nc, P.store_mode);
-               }
-          } else if (kind == GB_KIND_C2R) {
-               if (half) coop_store<C, false, true>(P, out, res, sms, tile, N, P.store_mode);
-               else {
-                    for (int idx = threadIdx.x; idx < P.tb * N; idx += blockDim.x) {
-                         int t, j;
-                         if (P.store_mode == GB_MOVE_COLS) { t = idx % P.tb; j = idx / P.tb; }
-                         else { t = idx / N; j = idx - t * N; }
-                         const long long v = tile.v0 + t;
-                         if (v < P.vn[0]) ((R *)out)[tile.bo + v * P.vos[0] + j * P.os] = res[t * sms + j].x;
-                    }
-               }
-          }
-          __syncthreads();
+          gen_tile<C>(P, tile, A, b0, b1);
      }
 }
 

@@ -10,10 +10,13 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
+#include <stdint.h>
 #include "fft_kernels.cuh"
 
 extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir);
 extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
+extern "C" const void *gb_tma_kernel_f(int logn, int dir);
+extern "C" const void *gb_tma_kernel_d(int logn, int dir);
 
 namespace gb {
 
@@ -58,6 +61,21 @@ __global__ void k_chirp_pad(C *dst, const C *w, long long n, long long nb)
           if (k < n) v = w[k];
           else if (nb - k < n) v = w[nb - k];
           dst[k] = mk<C>(v.x / (R)nb, v.y / (R)nb);
+     }
+}
+
+/* Rader's omega[k] = exp(sign 2 pi i g^-k / p) / (p-1), with g^-k read from
+ * the generator-power table as g^((p-1-k) mod (p-1)) (dft/rader.c:45-74). */
+template <typename C>
+__global__ void k_rader_omega(C *dst, const int *gpow, long long p, int sign)
+{
+     typedef typename real_of<C>::T R;
+     const long long m = p - 1;
+     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m;
+          k += (long long)gridDim.x * blockDim.x) {
+          double c, s;
+          cexp_fp64(gpow[(m - k) % m], p, sign, &c, &s);
+          dst[k] = mk<C>((R)(c / (double)m), (R)(s / (double)m));
      }
 }
 
@@ -117,30 +135,71 @@ extern "C" int gb_chirp_pad(void *dst, const void *w, int prec, long long n, lon
      return gb_check(cudaGetLastError(), "chirp padding");
 }
 
+extern "C" int gb_rader_omega(void *dst, const int *gpow, int prec, long long p, int sign, void *stream)
+{
+     int blocks = (int)((p + 255) / 256);
+     if (blocks > 4096) blocks = 4096;
+     if (prec == 4) k_rader_omega<float2><<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, gpow, p, sign);
+     else k_rader_omega<double2><<<blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, gpow, p, sign);
+     return gb_check(cudaGetLastError(), "Rader omega");
+}
+
 static const void *pick_kernel(const gb_pass *p)
 {
      if (p->kind == GB_KIND_COPY)
           return p->prec == 4 ? (const void *)k_copy<float2> : (const void *)k_copy<double2>;
-     if (p->variant == GB_VAR_REG) {
+     if (p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA) {
           int logn = 0;
           while ((1 << logn) < p->nfft) ++logn;
+          if (p->variant == GB_VAR_TMA)
+               return (p->kind == GB_KIND_C2C) ? (p->prec == 4 ? gb_tma_kernel_f(logn, p->sign) : gb_tma_kernel_d(logn, p->sign)) : 0;
           return p->prec == 4 ? gb_reg_kernel_f(logn, p->kind, p->sign) : gb_reg_kernel_d(logn, p->kind, p->sign);
      }
-     int dir = p->sign;
-     if (p->kind == GB_KIND_R2C) dir = -1;
-     if (p->kind == GB_KIND_C2R) dir = 1;
-     if (p->prec == 4) return dir < 0 ? (const void *)k_gen<float2, -1> : (const void *)k_gen<float2, 1>;
-     return dir < 0 ? (const void *)k_gen<double2, -1> : (const void *)k_gen<double2, 1>;
+     return p->prec == 4 ? (const void *)k_gen<float2> : (const void *)k_gen<double2>;
 }
 
 /* Number of CTAs launched for a pass: all tiles, capped; kernels stride over
- * the rest. */
-static unsigned grid_of(const gb_pass *p)
+ * the rest.  Persistent (TMA-fed) passes launch exactly as many CTAs as fit
+ * on the device at once. */
+static unsigned grid_of(const gb_pass *p, const void *fn)
 {
      long long g = p->nblocks;
+     if (p->variant == GB_VAR_TMA) {
+          int dev = 0, sms = 0, per = 0;
+          cudaGetDevice(&dev);
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+          if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, p->threads, (size_t)p->smem) != cudaSuccess) {
+               cudaGetLastError();
+               per = 1;
+          }
+          if (per < 1) per = 1;
+          if (g > (long long)per * sms) g = (long long)per * sms;
+     }
      if (g > (1LL << 30)) g = 1LL << 30;
      if (g < 1) g = 1;
      return (unsigned)g;
+}
+
+/* One device word where kernels report a bounded wait that gave up. */
+static int *gb_status_word = 0;
+
+extern "C" int *gb_device_status_ptr(void)
+{
+     if (!gb_status_word) {
+          if (cudaMalloc((void **)&gb_status_word, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return 0; }
+          cudaMemset(gb_status_word, 0, sizeof(int));
+     }
+     return gb_status_word;
+}
+
+/* Read and clear the device status word (0 = no kernel reported a problem). */
+extern "C" int gb_device_status(void)
+{
+     int v = 0, z = 0;
+     if (!gb_status_word) return 0;
+     if (cudaMemcpy(&v, gb_status_word, sizeof v, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+     cudaMemcpy(gb_status_word, &z, sizeof z, cudaMemcpyHostToDevice);
+     return v;
 }
 
 extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void *stream)
@@ -160,12 +219,19 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if ((p->kind == GB_KIND_R2C || p->kind == GB_KIND_C2R) && p->n % 2 == 0 && !p->tw_half)
                bad = "half-length twiddle table missing";
           else if (p->kind == GB_KIND_BLUESTEIN && (!p->chirp || !p->chirp_spec)) bad = "chirp tables missing";
-          else if (p->kind == GB_KIND_BLUESTEIN && p->variant != GB_VAR_REG) bad = "Bluestein needs the register variant";
+          else if (p->kind == GB_KIND_RADER && (p->variant != GB_VAR_GEN || !p->perm || !p->chirp_spec || p->nfft != p->n - 1))
+               bad = "Rader pass needs its permutation and omega tables";
           else if (p->post_N && (!p->post_lo || !p->post_hi || p->post_S <= 0)) bad = "four-step twiddle tables missing";
           else if (p->threads < 1 || p->threads > 1024 || p->tb < 1 || p->nv < 1 || p->nv > GB_MAXV) bad = "bad launch shape";
-          else if (p->variant == GB_VAR_REG && p->kind != GB_KIND_COPY &&
+          else if ((p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA) && p->kind != GB_KIND_COPY &&
                    p->threads != p->tb * (p->nfft / reg_e(p->nfft))) bad = "thread count does not match the tile";
           else if (p->variant == GB_VAR_REG && p->threads > reg_maxthreads(p->nfft)) bad = "tile exceeds the kernel's launch bounds";
+          else if (reg_sms(p->nfft) != gb_reg_sms(p->nfft)) bad = "host and device shared-memory layouts disagree";
+          else if (p->variant == GB_VAR_REG && p->smem < p->tb * reg_sms(p->nfft) * 2 * p->prec) bad = "shared memory too small for the tile";
+          else if (p->variant == GB_VAR_TMA && (p->threads > 256 || p->kind != GB_KIND_C2C || p->is != 1 ||
+                                                p->smem < 2 * p->tb * tma_sms(p->nfft) * 2 * p->prec))
+               bad = "persistent bulk-copy pass needs unit-stride c2c, <= 256 threads and two smem slots";
+          else if (p->variant == GB_VAR_TMA && ((uintptr_t)in % 16 != 0)) bad = "bulk copies need a 16-byte aligned input";
           if (bad) {
                snprintf(gb_errbuf, sizeof gb_errbuf, "refused pass (kind %d nfft %d): %s", p->kind, p->nfft, bad);
                return -1;
@@ -177,8 +243,9 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
                return -1;
      }
      gb_pass pv = *p;
+     if (!pv.status) pv.status = gb_device_status_ptr();
      void *args[3] = {(void *)&pv, (void *)&in, (void *)&out};
-     cudaError_t e = cudaLaunchKernel(fn, dim3(grid_of(p)), dim3(p->threads), args, (size_t)p->smem,
+     cudaError_t e = cudaLaunchKernel(fn, dim3(grid_of(p, fn)), dim3(p->threads), args, (size_t)p->smem,
                                       (cudaStream_t)stream);
      __atomic_add_fetch(&gb_launches, 1ull, __ATOMIC_RELAXED);
      return gb_check(e, "kernel launch");

@@ -17,6 +17,23 @@ static const void *reg_pick(int kind, int dir)
 }
 
 template <int L>
+static const void *tma_pick(int dir)
+{
+     if constexpr (L < 6 || L > 12) return 0;
+     else return dir < 0 ? (const void *)k_reg_tma<GB_CT, L, -1> : (const void *)k_reg_tma<GB_CT, L, 1>;
+}
+
+template <int L>
+static const void *tma_lookup(int logn, int dir)
+{
+     if constexpr (L > 12) return 0;
+     else {
+          if (logn == L) return tma_pick<L>(dir);
+          return tma_lookup<L + 1>(logn, dir);
+     }
+}
+
+template <int L>
 static const void *reg_lookup(int logn, int kind, int dir)
 {
      if constexpr (L > GB_MAXLOG) return 0;

@@ -114,3 +114,53 @@ long long fftw_gb300_launch_count(void) { return gb_launch_count(); }
 
 GB_EXT(fftw_, fftw_plan)
 GB_EXT(fftwf_, fftwf_plan)
+
+/* plan sets: one work-queue kernel (one CUDA graph launch) for many plans */
+#define GB_SET_EXT(PFX_, PLAN, SET, PREC)                                               \
+     SET PFX_##gb300_plan_set(int nplans, const PLAN *plans, unsigned flags)           \
+     {                                                                                 \
+          gb_plan **g;                                                                 \
+          gb_set *s;                                                                   \
+          int i;                                                                       \
+          if (nplans < 0 || (nplans > 0 && !plans)) return 0;                          \
+          g = (gb_plan **)malloc(sizeof(gb_plan *) * (size_t)(nplans ? nplans : 1));   \
+          for (i = 0; i < nplans; ++i) g[i] = plans[i] ? plans[i]->g : 0;              \
+          gb_lock();                                                                   \
+          s = gb_mkset(PREC, nplans, g, flags);                                        \
+          gb_unlock();                                                                 \
+          free(g);                                                                     \
+          return (SET)s;                                                               \
+     }                                                                                 \
+     int PFX_##gb300_execute_set(SET s)                                                \
+     {                                                                                 \
+          if (!s) return -1;                                                           \
+          if (gb_execute_set((gb_set *)s)) {                                           \
+               gb_note_failure();                                                      \
+               return -1;                                                              \
+          }                                                                            \
+          return 0;                                                                    \
+     }                                                                                 \
+     int PFX_##gb300_set_stream_set(SET s, void *stream, int async)                    \
+     {                                                                                 \
+          if (!s) return -1;                                                           \
+          gb_set_stream_of_set((gb_set *)s, stream, async);                            \
+          return 0;                                                                    \
+     }                                                                                 \
+     int PFX_##gb300_set_info(SET s, int *nitems, int *ntransforms, int *nlong,        \
+                              int *grid, int *smem)                                    \
+     {                                                                                 \
+          if (!s) return -1;                                                           \
+          gb_set_info((const gb_set *)s, nitems, ntransforms, nlong, grid, smem);      \
+          return 0;                                                                    \
+     }                                                                                 \
+     void PFX_##gb300_destroy_set(SET s)                                               \
+     {                                                                                 \
+          gb_lock();                                                                   \
+          gb_destroy_set((gb_set *)s);                                                 \
+          gb_unlock();                                                                 \
+     }
+
+GB_SET_EXT(fftw_, fftw_plan, fftw_gb300_set, 8)
+GB_SET_EXT(fftwf_, fftwf_plan, fftwf_gb300_set, 4)
+
+int fftw_gb300_device_status(void) { return gb_device_status(); }

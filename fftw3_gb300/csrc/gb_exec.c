@@ -95,10 +95,19 @@ static int run_step(const gb_plan *p, const gb_step *s, char *bufs[3], int esz[3
           if (s->dst_off % 2) ok = 0;
           P.real_pairs = ok;
      }
+     if (P.variant == GB_VAR_TMA && ((uintptr_t)(bufs[si] + s->src_off * esz[si]) % 16)) {
+          /* input not 16-byte aligned for bulk copies: same tile, register path */
+          P.variant = GB_VAR_REG;
+          P.smem = P.tb * gb_reg_sms(P.nfft) * 2 * P.prec;
+     }
      for (i = 0; i < s->nloop; ++i) idx[i] = 0;
      while (!done) {
           long long oi = s->src_off, oo = s->dst_off;
           for (i = 0; i < s->nloop; ++i) { oi += idx[i] * s->loop[i].is; oo += idx[i] * s->loop[i].os; }
+          if (P.variant == GB_VAR_TMA && ((uintptr_t)(bufs[si] + oi * esz[si]) % 16)) {
+               P.variant = GB_VAR_REG;
+               P.smem = P.tb * gb_reg_sms(P.nfft) * 2 * P.prec;
+          }
           if (gb_launch_pass(&P, bufs[si] + oi * esz[si], bufs[di] + oo * esz[di], p->stream)) {
                gb_set_error("pass launch failed: %s", gb_last_cuda_error());
                return -1;

@@ -110,8 +110,23 @@ const void *gb_table_chirp(int prec, long long n, int sign);
 const void *gb_table_chirp_spec(int prec, long long n, long long nb, int sign);
 void gb_tables_free(void);
 
+/* helpers shared with the plan-set compiler */
+int gb_factor_radices(long long n, int *rad);
+int gb_pass_tables(gb_pass *P);
+
+/* plan sets (gb_set.c) */
+typedef struct gb_set gb_set;
+gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags);
+int gb_execute_set(gb_set *S);
+void gb_set_stream_of_set(gb_set *S, void *stream, int async);
+void gb_set_info(const gb_set *S, int *nitems, int *ntransforms, int *nlong, int *grid, int *smem);
+void gb_destroy_set(gb_set *S);
+
 /* launch layer (fft_launch.cu) */
 int gb_chirp_pad(void *dst, const void *w, int prec, long long n, long long nb, void *stream);
+int gb_rader_omega(void *dst, const int *gpow, int prec, long long p, int sign, void *stream);
+const int *gb_table_rader_perm(long long p);
+const void *gb_table_rader_spec(int prec, long long p, int sign);
 int gb_pass_kernel_attrs(const gb_pass *p, int *regs, int *max_threads);
 
 #endif

@@ -156,6 +156,85 @@ const void *gb_table_chirp_spec(int prec, long long n, long long nb, int sign)
      return p;
 }
 
+/* Rader tables (dft/rader.c:45-74, kernel/primes.c:105-122): generator
+ * powers and discrete logs as int32, and the spectrum of omega/(p-1)
+ * computed on the device with this library's own forward FFT. */
+static long long powmod_ll(long long b, long long e, long long m)
+{
+     long long r = 1;
+     b %= m;
+     while (e > 0) {
+          if (e & 1) r = (long long)((__int128)r * b % m);
+          b = (long long)((__int128)b * b % m);
+          e >>= 1;
+     }
+     return r;
+}
+
+static long long find_generator(long long p)
+{
+     long long f[64], nf = 0, q = p - 1, d, g;
+     int i;
+     if (p == 2) return 1;
+     for (d = 2; d * d <= q; ++d)
+          if (q % d == 0) { f[nf++] = d; while (q % d == 0) q /= d; }
+     if (q > 1) f[nf++] = q;
+     for (g = 2;; ++g) {
+          for (i = 0; i < nf; ++i)
+               if (powmod_ll(g, (p - 1) / f[i], p) == 1) break;
+          if (i == nf) return g;
+     }
+}
+
+const int *gb_table_rader_perm(long long p)
+{
+     void *dp = tab_find(4, 3, p, 0, 0);
+     int *h;
+     long long g, ginv, k, v;
+     if (dp) return (const int *)dp;
+     dp = tab_add(4, 3, p, 0, 0, (size_t)(2 * (p - 1)) * sizeof(int));
+     if (!dp || gb_dry) return (const int *)dp;
+     h = (int *)malloc((size_t)(2 * (p - 1)) * sizeof(int));
+     g = find_generator(p);
+     ginv = powmod_ll(g, p - 2, p);
+     for (k = 0, v = 1; k < p - 1; ++k, v = v * g % p) h[k] = (int)v;
+     for (k = 0, v = 1; k < p - 1; ++k, v = v * ginv % p) h[(p - 1) + (v - 1)] = (int)k;
+     if (cudaMemcpy(dp, h, (size_t)(2 * (p - 1)) * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+          free(h);
+          gb_set_error("Rader table upload failed");
+          return 0;
+     }
+     free(h);
+     return (const int *)dp;
+}
+
+const void *gb_table_rader_spec(int prec, long long p, int sign)
+{
+     void *dp = tab_find(prec, 4, p, sign, 0);
+     const int *perm;
+     gb_pass P;
+     gb_dim d;
+     if (dp) return dp;
+     perm = gb_table_rader_perm(p);
+     if (!perm) return 0;
+     dp = tab_add(prec, 4, p, sign, 0, (size_t)(p - 1) * 2 * prec);
+     if (!dp || gb_dry) return dp;
+     if (gb_rader_omega(dp, perm, prec, p, sign, 0)) {
+          gb_set_error("Rader omega failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     d.n = 1; d.is = 0; d.os = 0;
+     if (config_pass(&P, prec, GB_KIND_C2C, p - 1, -1, 1, 1, 1, &d, 0, 0) != 0 || pass_tables(&P) != 0) {
+          gb_set_error("Rader: no forward FFT of length %lld", p - 1);
+          return 0;
+     }
+     if (gb_launch_pass(&P, dp, dp, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("Rader omega spectrum failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     return dp;
+}
+
 void gb_tables_free(void)
 {
      while (tabs) {
@@ -187,10 +266,13 @@ static int gb_factor(long long n, int *rad)
 }
 
 static int csize(int prec) { return 2 * prec; }
+
+int gb_factor_radices(long long n, int *rad) { return gb_factor(n, rad); }
 static int reg_max_log(int prec) { return prec == 4 ? 14 : 13; }
 static int reg_e(int nfft) { return nfft < 16 ? nfft : 16; }
-static int reg_sms(int nfft) { return nfft + (nfft >> 4) + 2; }
+static int reg_sms(int nfft) { return gb_reg_sms(nfft); }
 static int reg_maxthreads(int nfft) { int t = nfft / reg_e(nfft); return t > 512 ? t : 512; }
+static int tma_sms(int nfft) { return gb_reg_sms(nfft); }
 
 /* FFTW's canonical vector tensor: drop n = 1, merge dims that are
  * contiguous in both input and output (kernel/tensor7.c:99-167). */
@@ -255,6 +337,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
           return 0;
      }
 
+     if (kind == GB_KIND_RADER) { nfft = n - 1; P->nfft = (int)nfft; }
      if (kind == GB_KIND_BLUESTEIN) {   /* convolution length: power of two >= 2n-1 */
           long long nb = 1;
           while (nb < 2 * n - 1) nb <<= 1;
@@ -262,7 +345,8 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
           P->nfft = (int)nb;
      }
      if (is_pow2(nfft) && ilog2(nfft) <= reg_max_log(prec) &&
-         (kind == GB_KIND_C2C || kind == GB_KIND_BLUESTEIN || half) && !(kind == GB_KIND_BLUESTEIN && nfft < 32)) {
+         (kind == GB_KIND_C2C || kind == GB_KIND_BLUESTEIN || half) && !(kind == GB_KIND_BLUESTEIN && nfft < 32) &&
+         kind != GB_KIND_RADER) {
           int E = reg_e((int)nfft), T = (int)nfft / E, tb, maxt = reg_maxthreads((int)nfft);
           int cols_in, cols_out;
           long long sm1 = (long long)reg_sms((int)nfft) * csize(prec);
@@ -290,6 +374,30 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
           else P->store_mode = GB_MOVE_DIRECT;
           if (kind == GB_KIND_R2C && P->store_mode == GB_MOVE_DIRECT && llabs_(os) == 1 && T < 32)
                P->store_mode = GB_MOVE_ROWS;
+          /* unit-stride c2c with 16-byte aligned transform starts: persistent
+           * CTAs fed by bulk async copies (k_reg_tma) */
+          if (kind == GB_KIND_C2C && is == 1 && nfft >= 64 && nfft <= 4096 && tb_hint == 0 &&
+              !getenv("FFTW_GB300_NO_TMA")) {
+               int ok = 1, tbt = 256 / T;
+               long long sm2;
+               for (i = 0; i < nv; ++i)
+                    if ((P->vis[i] * csize(prec)) % 16) ok = 0;
+               if (tbt < 1) tbt = 1;
+               while (tbt > 1 && (tbt >> 1) >= v[0].n) tbt >>= 1;
+               sm2 = 2LL * tbt * tma_sms((int)nfft) * csize(prec);
+               while (tbt > 1 && sm2 > 76 * 1024) {   /* keep >= 3 CTAs per SM */
+                    tbt >>= 1;
+                    sm2 = 2LL * tbt * tma_sms((int)nfft) * csize(prec);
+               }
+               if (ok && sm2 <= smax) {
+                    P->variant = GB_VAR_TMA;
+                    P->tb = tbt;
+                    P->threads = tbt * T;
+                    P->smem = (int)sm2;
+                    P->load_mode = GB_MOVE_DIRECT;
+                    P->store_mode = GB_MOVE_DIRECT;
+               }
+          }
      } else {
           int k, tb;
           long long sm1, L = nfft;
@@ -332,6 +440,11 @@ static int pass_tables(gb_pass *P)
           P->tw_half = gb_table_twiddle(prec, P->n, P->n / 2 + 1, 1);
           if (!P->tw_half) return -1;
      }
+     if (P->kind == GB_KIND_RADER) {
+          P->perm = gb_table_rader_perm(P->n);
+          P->chirp_spec = gb_table_rader_spec(prec, P->n, P->sign);
+          if (!P->perm || !P->chirp_spec) return -1;
+     }
      if (P->kind == GB_KIND_BLUESTEIN) {
           P->chirp = gb_table_chirp(prec, P->n, P->sign);
           P->chirp_spec = gb_table_chirp_spec(prec, P->n, P->nfft, P->sign);
@@ -347,6 +460,8 @@ static int pass_tables(gb_pass *P)
      }
      return 0;
 }
+
+int gb_pass_tables(gb_pass *P) { return pass_tables(P); }
 
 /* ------------------------------------------------------------ plan building */
 typedef struct {
@@ -370,6 +485,23 @@ static void count_ops(gb_plan *p, const gb_pass *P, long long howmany)
      if (P->kind == GB_KIND_BLUESTEIN) per = 2 * per + 12.0 * n;
      p->add += 0.6 * per * howmany;
      p->mul += 0.4 * per * howmany;
+}
+
+/* Prime lengths: Rader (dft/rader.c) when n-1 factors into radices <= 13
+ * and the wisdom or FFTW_GB300_PRIME=rader asks for it; Bluestein
+ * otherwise (one CTA, power-of-two convolution, register stages). */
+static int use_rader(int prec, long long n, const gb_wisdom_entry *w)
+{
+     int rad[GB_MAXRAD];
+     const char *e = getenv("FFTW_GB300_PRIME");
+     if (n < 3 || gb_factor(n - 1, rad) < 0) return 0;
+     {
+          long long d;
+          for (d = 2; d * d <= n; ++d) if (n % d == 0) return 0;
+     }
+     if (2LL * n * csize(prec) > smem_max()) return 0;
+     if (w) return w->variant == GB_KIND_RADER;
+     return e && !strcmp(e, "rader");
 }
 
 /* Adds the steps of one batched 1D transform: length n along (is, os), batch
@@ -431,6 +563,19 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
      }
      --p->nstep;   /* the single-pass attempt is replaced below */
 
+     if (rc < 0 && kind == GB_KIND_C2C && use_rader(prec, n, w)) {
+          /* prime with a smooth n-1: Rader in one CTA */
+          s = new_step(b);
+          s->src = src; s->dst = dst;
+          if (nvk > GB_MAXV) { s->nloop = nvk - GB_MAXV; for (i = 0; i < s->nloop; ++i) s->loop[i] = v[i]; }
+          rc = config_pass(&s->pass, prec, GB_KIND_RADER, n, sign, is, os, nvk - s->nloop, v + s->nloop, 0, 0);
+          if (rc == 0) {
+               if (pass_tables(&s->pass)) { b->err = 1; return; }
+               count_ops(p, &s->pass, howmany);
+               return;
+          }
+          --p->nstep;
+     }
      if (rc < 0 && kind == GB_KIND_C2C) {
           /* length with a prime factor > 13: Bluestein in one CTA */
           s = new_step(b);
@@ -522,11 +667,11 @@ static void describe(gb_plan *p)
                      kn[p->prb.kind], p->prb.prec == 4 ? "f32" : "f64");
      for (i = 0; i < p->nstep && off < (int)sizeof p->desc - 64; ++i) {
           const gb_pass *P = &p->step[i].pass;
-          static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy"};
+          static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy", "rader"};
           static const char *mv[] = {"direct", "rows", "cols"};
           off += snprintf(p->desc + off, sizeof p->desc - off,
                           "\n  (pass %s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
-                          kk[P->kind], P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : "gen", P->tb,
+                          kk[P->kind], P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" : "gen", P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
                           P->vn[0], P->post_N ? " +twiddle" : "");
      }

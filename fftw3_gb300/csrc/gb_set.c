@@ -1,0 +1,385 @@
+/*
+ * Plan sets: many independent c2c plans of uneven lengths executed by one
+ * persistent kernel with a device work queue, captured once as a CUDA graph.
+ *
+ * The reference executes a set of transforms as a loop of fftw_execute calls,
+ * one plan after another (each a tree of solver applies, api/execute.c:23-27).
+ * Here the set compiles to queue items (gb_qitem):
+ *   - a transform that fits one CTA's shared memory (2 buffers of nfft+1
+ *     complex, nfft <= 8192 single / 4096 double) is a "single"; singles of
+ *     the same length, sign and strides are grouped into items of up to 32
+ *     transforms, each transform with its own array pointers;
+ *   - a prime length is a Bluestein single (power-of-two convolution) or, if
+ *     the tuner or FFTW_GB300_PRIME=rader asks and n-1 is smooth, a Rader single;
+ *   - a longer smooth transform is split n = n1*n2 into column tiles (pass A,
+ *     with the W_n^(n2 k1) twiddle, into set-owned scratch) and row tiles
+ *     (pass B, into the output); row tiles wait for their transform's column
+ *     tiles on a device counter.
+ * Items are queued column tiles first, then singles by decreasing cost, then
+ * row tiles, so no wait can block a claimed item.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <cuda_runtime_api.h>
+#include "gb_host.h"
+
+#define GB_Q_THREADS 512
+#define GB_Q_GROUP 32
+
+typedef struct { long long n; int sign; long long is, os; const void *in; void *out; } xform;
+
+struct gb_set {
+     int prec;
+     int nitems, nctr;
+     int grid, threads, smem;
+     gb_qitem *d_items;
+     int *d_head, *d_ctrs;
+     void **d_ptrs;
+     void *d_scratch;
+     size_t scratch_bytes;
+     void *stream;
+     int async;
+     cudaGraph_t graph;
+     cudaGraphExec_t gexec;
+     int nsingle_items, nlong, ntransforms;
+};
+typedef struct gb_set gb_set;
+
+static int is_prime_ll(long long n)
+{
+     long long d;
+     if (n < 2) return 0;
+     for (d = 2; d * d <= n; ++d)
+          if (n % d == 0) return 0;
+     return 1;
+}
+
+static long long pow2_at_least(long long v)
+{
+     long long p = 1;
+     while (p < v) p <<= 1;
+     return p;
+}
+
+/* Fill the pass fields a queue item needs (the shared-memory tile body). */
+static int item_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os,
+                     long long vn0, long long vis0, long long vos0, int tb, int cols_in, int cols_out)
+{
+     memset(P, 0, sizeof *P);
+     P->kind = kind; P->prec = prec; P->sign = sign; P->n = (int)n;
+     P->nfft = (int)(kind == GB_KIND_BLUESTEIN ? pow2_at_least(2 * n - 1) : kind == GB_KIND_RADER ? n - 1 : n);
+     P->variant = GB_VAR_GEN;
+     P->tb = tb;
+     P->threads = GB_Q_THREADS;
+     P->smem = 2 * tb * (P->nfft + 1) * 2 * prec;
+     P->load_mode = cols_in ? GB_MOVE_COLS : GB_MOVE_ROWS;
+     P->store_mode = cols_out ? GB_MOVE_COLS : GB_MOVE_ROWS;
+     P->is = is; P->os = os;
+     P->nv = 1;
+     P->vn[0] = vn0; P->vis[0] = vis0; P->vos[0] = vos0;
+     P->ntiles0 = 1; P->nblocks = 1;
+     P->nrad = gb_factor_radices(P->nfft, P->rad);
+     if (P->nrad < 0) return -1;
+     if (gb_pass_tables(P)) return -1;
+     return 0;
+}
+
+static double item_cost(const gb_qitem *q)
+{
+     double n = q->P.nfft;
+     return q->P.tb * n * (n > 1 ? log2(n) : 1) * (q->P.kind == GB_KIND_BLUESTEIN || q->P.kind == GB_KIND_RADER ? 2 : 1);
+}
+
+static int cmp_cost_desc(const void *a, const void *b)
+{
+     double ca = item_cost((const gb_qitem *)a), cb = item_cost((const gb_qitem *)b);
+     return ca < cb ? 1 : ca > cb ? -1 : 0;
+}
+
+static int cmp_key(const void *a, const void *b)
+{
+     const xform *x = (const xform *)a, *y = (const xform *)b;
+     if (x->n != y->n) return x->n < y->n ? -1 : 1;
+     if (x->sign != y->sign) return x->sign - y->sign;
+     if (x->is != y->is) return x->is < y->is ? -1 : 1;
+     if (x->os != y->os) return x->os < y->os ? -1 : 1;
+     return 0;
+}
+
+/* which way a prime (or non-smooth) length runs as a single */
+static int prime_kind(int prec, long long n, int cap)
+{
+     int rad[GB_MAXRAD];
+     const char *e = getenv("FFTW_GB300_PRIME");
+     char key[128];
+     const gb_wisdom_entry *w;
+     int rader_ok = is_prime_ll(n) && gb_factor_radices(n - 1, rad) >= 0 && n - 1 <= cap;
+     snprintf(key, sizeof key, "c2c p%d n%lld", prec, n);
+     w = gb_wisdom_lookup(key);
+     if (rader_ok && ((w && w->variant == GB_KIND_RADER) || (!w && e && !strcmp(e, "rader")))) return GB_KIND_RADER;
+     if (pow2_at_least(2 * n - 1) <= cap) return GB_KIND_BLUESTEIN;
+     if (rader_ok) return GB_KIND_RADER;
+     return -1;
+}
+
+gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
+{
+     gb_set *S;
+     xform *xs;
+     int nx = 0, cap = prec == 4 ? 8192 : 4096, i, j;
+     int cs = 2 * prec;
+     size_t maxitems;
+     gb_qitem *A = 0, *M = 0, *B = 0;
+     int na = 0, nm = 0, nb = 0, cap_a, cap_m, cap_b;
+     void **hptr = 0;
+     int nptr = 0, cap_ptr;
+     long long scratch_elems = 0;
+     int nctr = 0, smem = 0;
+     (void)flags;
+     if (gb_dry_run() || !gb_cuda_ready()) {
+          gb_set_error("plan sets need a GPU");
+          return 0;
+     }
+     for (i = 0; i < nplans; ++i) {
+          const gb_problem *pr;
+          if (!plans[i]) { gb_set_error("plan set: plan %d is NULL", i); return 0; }
+          pr = &plans[i]->prb;
+          if (pr->kind != GB_PROB_DFT || pr->rank != 1 || pr->vrank > 1 || pr->prec != prec) {
+               gb_set_error("plan set: plan %d is not a rank-1 c2c plan of this precision", i);
+               return 0;
+          }
+          nx += pr->vrank ? (int)pr->vec[0].n : 1;
+     }
+     xs = (xform *)malloc(sizeof(xform) * (size_t)(nx ? nx : 1));
+     nx = 0;
+     for (i = 0; i < nplans; ++i) {
+          const gb_problem *pr = &plans[i]->prb;
+          long long h = pr->vrank ? pr->vec[0].n : 1, t;
+          for (t = 0; t < h; ++t) {
+               xform *x = &xs[nx++];
+               x->n = pr->sz[0].n; x->sign = pr->sign; x->is = pr->sz[0].is; x->os = pr->sz[0].os;
+               x->in = (const char *)pr->in + (pr->vrank ? t * pr->vec[0].is : 0) * cs;
+               x->out = (char *)pr->out + (pr->vrank ? t * pr->vec[0].os : 0) * cs;
+          }
+     }
+     qsort(xs, (size_t)nx, sizeof(xform), cmp_key);
+     maxitems = (size_t)nx * 4 + 64;
+     cap_a = cap_m = cap_b = (int)maxitems;
+     A = (gb_qitem *)calloc((size_t)cap_a, sizeof(gb_qitem));
+     M = (gb_qitem *)calloc((size_t)cap_m, sizeof(gb_qitem));
+     B = (gb_qitem *)calloc((size_t)cap_b, sizeof(gb_qitem));
+     cap_ptr = 2 * nx + 2;
+     hptr = (void **)calloc((size_t)cap_ptr, sizeof(void *));
+
+     for (i = 0; i < nx;) {
+          xform *x = &xs[i];
+          long long n = x->n;
+          int rad[GB_MAXRAD], kind = GB_KIND_C2C, g;
+          int smooth = gb_factor_radices(n, rad) >= 0;
+          if (n <= cap && smooth) kind = GB_KIND_C2C;
+          else if (!smooth && (kind = prime_kind(prec, n, cap)) > 0) { /* single */ }
+          else kind = -1;
+          if (kind >= 0) {
+               /* group transforms with the same key */
+               gb_pass tmp;
+               long long nfft = kind == GB_KIND_BLUESTEIN ? pow2_at_least(2 * n - 1) : kind == GB_KIND_RADER ? n - 1 : n;
+               int tbmax = (int)((2LL * (cap + 1) * cs) / (2LL * (nfft + 1) * cs));
+               if (tbmax > GB_Q_GROUP) tbmax = GB_Q_GROUP;
+               if (tbmax < 1) tbmax = 1;
+               for (g = 0; i + g < nx && g < tbmax && cmp_key(&xs[i], &xs[i + g]) == 0; ++g) {}
+               if (item_pass(&tmp, prec, kind, n, x->sign, x->is, x->os, g, 0, 0, g, 0, 0)) goto fail;
+               {
+                    gb_qitem *q = &M[nm++];
+                    q->P = tmp;
+                    q->pin = (const void *const *)(size_t)nptr;     /* index now, device address later */
+                    q->pout = (void *const *)(size_t)(nptr + g);
+                    for (j = 0; j < g; ++j) { hptr[nptr + j] = (void *)xs[i + j].in; hptr[nptr + g + j] = xs[i + j].out; }
+                    nptr += 2 * g;
+                    q->wait_ctr = -1; q->signal_ctr = -1;
+                    if (tmp.smem > smem) smem = tmp.smem;
+               }
+               i += g;
+               continue;
+          }
+          if (!smooth) {
+               gb_set_error("plan set: length %lld is not supported in a set", n);
+               goto fail;
+          }
+          {
+               /* long transform: n = n1 * n2 with both factors in one CTA */
+               long long n1 = 0, n2, d, k0;
+               int tbc = prec == 4 ? 16 : 8, ctr = nctr++;
+               gb_pass pa, pb;
+               int nta = 0;
+               for (d = 2; d * d <= n; ++d)
+                    if (n % d == 0 && d <= cap && n / d <= cap && gb_factor_radices(d, rad) >= 0 &&
+                        gb_factor_radices(n / d, rad) >= 0)
+                         n1 = d;
+               if (!n1) { gb_set_error("plan set: length %lld has no two-pass split", n); goto fail; }
+               n2 = n / n1;
+               while (tbc > 1 && 2LL * tbc * ((n1 > n2 ? n1 : n2) + 1) * cs > 2LL * (cap + 1) * cs) tbc >>= 1;
+               /* pass A: columns n2 (stride is), n1-point transforms with
+                * element stride n2*is into scratch [n2][k1] */
+               if (item_pass(&pa, prec, GB_KIND_C2C, n1, x->sign, n2 * x->is, 1, n2, x->is, n1, tbc, 1, 0)) goto fail;
+               pa.post_N = n;
+               if (gb_pass_tables(&pa)) goto fail;
+               for (k0 = 0; k0 < n2; k0 += tbc) {
+                    gb_qitem *q = &A[na++];
+                    q->P = pa;
+                    q->v0 = k0;
+                    q->in = x->in;
+                    q->out = (void *)(size_t)scratch_elems;      /* offset now, address later */
+                    q->wait_ctr = -1; q->signal_ctr = ctr;
+                    ++nta;
+               }
+               if (pa.smem > smem) smem = pa.smem;
+               /* pass B: k1 columns of scratch (stride 1), n2-point transforms
+                * with element stride n1, into out[k1 + n1*k2] */
+               if (item_pass(&pb, prec, GB_KIND_C2C, n2, x->sign, n1, n1 * x->os, n1, 1, x->os, tbc, 1, 1)) goto fail;
+               for (k0 = 0; k0 < n1; k0 += tbc) {
+                    gb_qitem *q = &B[nb++];
+                    q->P = pb;
+                    q->v0 = k0;
+                    q->in = (const void *)(size_t)scratch_elems;
+                    q->out = x->out;
+                    q->wait_ctr = ctr; q->wait_target = nta; q->signal_ctr = -1;
+               }
+               if (pb.smem > smem) smem = pb.smem;
+               scratch_elems += n;
+               if (na + 4 > cap_a || nb + 4 > cap_b) { gb_set_error("plan set: too many tiles"); goto fail; }
+          }
+          ++i;
+     }
+     qsort(M, (size_t)nm, sizeof(gb_qitem), cmp_cost_desc);
+
+     S = (gb_set *)calloc(1, sizeof *S);
+     S->prec = prec;
+     S->nitems = na + nm + nb;
+     S->nctr = nctr;
+     S->threads = GB_Q_THREADS;
+     S->smem = smem;
+     S->nsingle_items = nm;
+     S->nlong = nctr;
+     S->ntransforms = nx;
+     S->scratch_bytes = (size_t)scratch_elems * cs;
+     S->grid = gb_queue_grid(prec, S->threads, S->smem);
+     if (S->grid <= 0) { gb_set_error("plan set: queue kernel does not fit (smem %d)", smem); free(S); goto fail; }
+     if (cudaMalloc((void **)&S->d_items, sizeof(gb_qitem) * (size_t)(S->nitems ? S->nitems : 1)) != cudaSuccess ||
+         cudaMalloc((void **)&S->d_head, sizeof(int)) != cudaSuccess ||
+         cudaMalloc((void **)&S->d_ctrs, sizeof(int) * (size_t)(nctr ? nctr : 1)) != cudaSuccess ||
+         cudaMalloc((void **)&S->d_ptrs, sizeof(void *) * (size_t)(nptr ? nptr : 1)) != cudaSuccess ||
+         (S->scratch_bytes && cudaMalloc(&S->d_scratch, S->scratch_bytes) != cudaSuccess)) {
+          cudaGetLastError();
+          gb_set_error("plan set: device allocation failed");
+          gb_destroy_set(S);
+          goto fail;
+     }
+     {
+          /* resolve indices/offsets into device addresses, then upload */
+          gb_qitem *all = (gb_qitem *)malloc(sizeof(gb_qitem) * (size_t)(S->nitems ? S->nitems : 1));
+          int k = 0;
+          for (i = 0; i < na; ++i) {
+               all[k] = A[i];
+               all[k].out = (char *)S->d_scratch + (size_t)A[i].out * cs;
+               ++k;
+          }
+          for (i = 0; i < nm; ++i) {
+               all[k] = M[i];
+               all[k].pin = (const void *const *)(S->d_ptrs + (size_t)M[i].pin);
+               all[k].pout = (void *const *)(S->d_ptrs + (size_t)M[i].pout);
+               ++k;
+          }
+          for (i = 0; i < nb; ++i) {
+               all[k] = B[i];
+               all[k].in = (const char *)S->d_scratch + (size_t)B[i].in * cs;
+               ++k;
+          }
+          if (cudaMemcpy(S->d_items, all, sizeof(gb_qitem) * (size_t)S->nitems, cudaMemcpyHostToDevice) != cudaSuccess ||
+              (nptr && cudaMemcpy(S->d_ptrs, hptr, sizeof(void *) * (size_t)nptr, cudaMemcpyHostToDevice) != cudaSuccess)) {
+               free(all);
+               gb_set_error("plan set: upload failed");
+               gb_destroy_set(S);
+               goto fail;
+          }
+          free(all);
+     }
+     free(A); free(M); free(B); free(hptr); free(xs);
+     return S;
+fail:
+     free(A); free(M); free(B); free(hptr); free(xs);
+     return 0;
+}
+
+/* Capture reset + queue launch into a CUDA graph on the set's stream. */
+static int build_graph(gb_set *S)
+{
+     cudaStream_t st = 0;
+     int own = 0, rc = 0;
+     if (S->gexec) return 0;
+     if (!S->stream) {
+          if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return -1;
+          own = 1;
+     } else st = (cudaStream_t)S->stream;
+     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = -1;
+     if (!rc) {
+          cudaMemsetAsync(S->d_head, 0, sizeof(int), st);
+          if (S->nctr) cudaMemsetAsync(S->d_ctrs, 0, sizeof(int) * (size_t)S->nctr, st);
+          if (gb_launch_queue(S->d_items, S->nitems, S->d_head, S->d_ctrs, S->prec, S->threads, S->smem, S->grid, st))
+               rc = -1;
+          if (cudaStreamEndCapture(st, &S->graph) != cudaSuccess) rc = -1;
+     }
+     if (!rc && cudaGraphInstantiate(&S->gexec, S->graph, 0) != cudaSuccess) rc = -1;
+     if (own) cudaStreamDestroy(st);
+     if (rc) {
+          cudaGetLastError();
+          gb_set_error("plan set: graph capture failed");
+     }
+     return rc;
+}
+
+int gb_execute_set(gb_set *S)
+{
+     cudaStream_t st = (cudaStream_t)S->stream;
+     if (build_graph(S)) return -1;
+     if (cudaGraphLaunch(S->gexec, st) != cudaSuccess) {
+          gb_set_error("plan set: graph launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+          return -1;
+     }
+     if (!S->async && cudaStreamSynchronize(st) != cudaSuccess) {
+          gb_set_error("plan set: %s", cudaGetErrorString(cudaGetLastError()));
+          return -1;
+     }
+     return 0;
+}
+
+void gb_set_stream_of_set(gb_set *S, void *stream, int async)
+{
+     if (S->stream != stream && S->gexec) {
+          cudaGraphExecDestroy(S->gexec);
+          cudaGraphDestroy(S->graph);
+          S->gexec = 0;
+          S->graph = 0;
+     }
+     S->stream = stream;
+     S->async = async;
+}
+
+void gb_set_info(const gb_set *S, int *nitems, int *ntransforms, int *nlong, int *grid, int *smem)
+{
+     *nitems = S->nitems; *ntransforms = S->ntransforms; *nlong = S->nlong; *grid = S->grid; *smem = S->smem;
+}
+
+void gb_destroy_set(gb_set *S)
+{
+     if (!S) return;
+     if (S->gexec) cudaGraphExecDestroy(S->gexec);
+     if (S->graph) cudaGraphDestroy(S->graph);
+     cudaFree(S->d_items);
+     cudaFree(S->d_head);
+     cudaFree(S->d_ctrs);
+     cudaFree(S->d_ptrs);
+     if (S->d_scratch) cudaFree(S->d_scratch);
+     free(S);
+}

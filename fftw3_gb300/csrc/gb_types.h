@@ -26,13 +26,15 @@ enum gb_kind {
      GB_KIND_R2C = 1,       /* real n -> complex n/2+1 */
      GB_KIND_C2R = 2,       /* complex n/2+1 -> real n */
      GB_KIND_BLUESTEIN = 3, /* complex n -> complex n through a chirp convolution of length nfft */
-     GB_KIND_COPY = 4       /* rank-0 problem: element copy */
+     GB_KIND_COPY = 4,      /* rank-0 problem: element copy */
+     GB_KIND_RADER = 5      /* prime n: cyclic convolution of length n-1 through the generator permutation */
 };
 
 /* How the transform is computed inside one CTA. */
 enum gb_variant {
      GB_VAR_REG = 0,   /* power-of-two length, register-resident Stockham stages of radix <= 16 */
-     GB_VAR_GEN = 1    /* any smooth length, shared-memory Stockham stages, runtime radix list */
+     GB_VAR_GEN = 1,   /* any smooth length, shared-memory Stockham stages, runtime radix list */
+     GB_VAR_TMA = 2    /* as GB_VAR_REG, persistent CTAs fed by bulk async copies (unit-stride c2c) */
 };
 
 /* How a tile of transforms moves between HBM and the CTA. */
@@ -74,24 +76,60 @@ typedef struct gb_pass {
      const void *post_hi;
      /* Bluestein: chirp w[k] (k < n) and the spectrum of the padded chirp / nfft */
      const void *chirp;
-     const void *chirp_spec;
+     const void *chirp_spec;   /* Bluestein: chirp spectrum; Rader: spectrum of omega / (n-1) */
+     const int *perm;          /* Rader: g^k mod n (k < n-1), then log_{g^-1} j (j = 1..n-1) */
      /* status word for bounded-wait and bounds reporting (device, owned by the library) */
      int *status;
 } gb_pass;
+
+/* One entry of a plan set's device work queue: a tile of transforms of one
+ * length, described by a pass, where the tile starts (v0 along vector
+ * dimension 0, bi/bo from the outer dimensions), its arrays, and optional
+ * dependencies.  Grouped transforms of different arrays use one pointer per
+ * transform (pin/pout, vn[0] of them); otherwise in/out + strides apply.
+ * An item with wait_ctr >= 0 starts only after counter wait_ctr reached
+ * wait_target; one with signal_ctr >= 0 increments it when done (the two
+ * passes of a long transform: column tiles signal, row tiles wait). */
+typedef struct gb_qitem {
+     gb_pass P;
+     long long bi, bo, v0;
+     const void *in;
+     void *out;
+     const void *const *pin;
+     void *const *pout;
+     int wait_ctr, wait_target, signal_ctr, pad_;
+} gb_qitem;
 
 /* Device status codes written to gb_pass.status. */
 #define GB_STATUS_OK 0
 #define GB_STATUS_BAD_DESCRIPTOR 1
 #define GB_STATUS_QUEUE_TIMEOUT 2
+#define GB_STATUS_COPY_TIMEOUT 3
+
+/* k_reg shared-memory layout, shared by the host planner and the kernels:
+ * transform element p lives at p + m*(p/16), m = 2 when the first radix-16
+ * stage writes 16 consecutive elements (nfft = 16^k >= 256), else 1; the
+ * per-transform stride is rounded up to an even count (16-byte alignment). */
+static inline int gb_pad_mult(int nfft)
+{
+     int r = nfft;
+     while (r > 16) r /= 16;
+     return (r == 16 && nfft >= 256) ? 2 : 1;
+}
+static inline int gb_reg_sms(int nfft) { return (nfft + gb_pad_mult(nfft) * (nfft >> 4) + 3) & ~1; }
 
 /* Launchers implemented in the .cu files (plain C ABI). */
 int gb_launch_pass(const gb_pass *p, const void *in, void *out, void *stream);
+int gb_launch_queue(const gb_qitem *items, int nitems, int *head, int *ctrs, int prec, int threads, int smem,
+                    int grid, void *stream);
+int gb_queue_grid(int prec, int threads, int smem);
 int gb_pass_configure(gb_pass *p, int max_smem_optin);
 int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream);
 int gb_chirp(void *dst, int prec, long long n, int sign, void *stream);
 int gb_device_max_smem(void);
 const char *gb_last_cuda_error(void);
 long long gb_launch_count(void);
+int gb_device_status(void);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,10 @@ extern int fftw_gb300_failures(void);
 extern void fftw_gb300_set_dry_run(int on);
 /* Number of kernels this library has launched since it was loaded. */
 extern long long fftw_gb300_launch_count(void);
+/* Read and clear the device status word: 0 when no kernel reported a
+ * problem, else a code (2: a work-queue dependency wait gave up, 3: a bulk
+ * copy never completed); kernels bound every wait instead of hanging. */
+extern int fftw_gb300_device_status(void);
 
 #define GB_FFTW_EXT_DECLARE(PFX)                                                       \
 extern int PFX##gb300_set_stream(PFX##plan p, void *cuda_stream);                     \
@@ -32,7 +36,18 @@ extern int PFX##gb300_set_async(PFX##plan p, int async);                        
 extern int PFX##gb300_npasses(PFX##plan p);                                           \
 extern int PFX##gb300_pass_info(PFX##plan p, int i, int *kind, int *nfft, int *variant,\
                                 int *tb, int *threads, int *smem, long long *blocks); \
-extern size_t PFX##gb300_scratch_bytes(PFX##plan p);
+extern size_t PFX##gb300_scratch_bytes(PFX##plan p);                                  \
+/* Plan sets: many rank-1 c2c plans (uneven lengths, device arrays) run by  \
+ * one persistent work-queue kernel, captured once as a CUDA graph; each     \
+ * execute is one graph launch equivalent to executing every plan.          */\
+typedef struct PFX##gb300_set_s *PFX##gb300_set;                                      \
+extern PFX##gb300_set PFX##gb300_plan_set(int nplans, const PFX##plan *plans,         \
+                                          unsigned flags);                            \
+extern int PFX##gb300_execute_set(PFX##gb300_set s);                                  \
+extern int PFX##gb300_set_stream_set(PFX##gb300_set s, void *cuda_stream, int async); \
+extern int PFX##gb300_set_info(PFX##gb300_set s, int *nitems, int *ntransforms,       \
+                               int *nlong, int *grid, int *smem);                     \
+extern void PFX##gb300_destroy_set(PFX##gb300_set s);
 
 GB_FFTW_EXT_DECLARE(fftw_)
 GB_FFTW_EXT_DECLARE(fftwf_)

@@ -309,3 +309,25 @@ def test_new_array_execute_and_roundtrip(lib, torch_cuda):
     before = g.launch_count()
     pf.execute()
     assert g.launch_count() == before + 1
+
+
+RADER_PRIMES = [17, 31, 61, 97, 101, 257, 401, 673, 1201, 3001]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("n", RADER_PRIMES)
+def test_c2c_rader(lib, torch_cuda, restatement, n, prec, monkeypatch):
+    """Primes through Rader's algorithm (dft/rader.c): generator permutation
+    and a cyclic convolution of length n-1, against the oracle's Rader."""
+    if prec == "d" and 2 * n * 16 > 227 * 1024:
+        pytest.skip("double Rader buffers exceed one CTA's shared memory")
+    monkeypatch.setenv("FFTW_GB300_PRIME", "rader")
+    rng = np.random.default_rng(n + 5)
+    hm = 3
+    x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
+    for sign in (-1, 1):
+        y, p = run_c2c(torch_cuda, x, [n], sign, prec, hm)
+        assert "rader" in p.describe()
+        ref = np.concatenate([restatement.dft_method(x[i * n:(i + 1) * n].astype(np.clongdouble), sign, 3, "l")
+                              for i in range(hm)])
+        assert rel_l2(y, ref) <= TOL[prec]

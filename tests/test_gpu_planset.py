@@ -1,0 +1,117 @@
+"""Plan sets: many c2c plans of uneven lengths run as one work-queue kernel
+launch (captured in a CUDA graph), checked transform by transform against
+the oracle and against executing the same plans one by one."""
+import ctypes
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def _make_set(torch, lengths, prec="f", sign=-1, seed=0):
+    import fftw3_gb300 as g
+    ct = torch.complex64 if prec == "f" else torch.complex128
+    offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    xin = torch.randn(int(offs[-1]), dtype=ct, device="cuda", generator=gen)
+    yout = torch.zeros_like(xin)
+    es = xin.element_size()
+    plans = []
+    for i, n in enumerate(lengths):
+        p = g.plan_many_dft([int(n)], 1, xin.data_ptr() + int(offs[i]) * es, yout.data_ptr() + int(offs[i]) * es,
+                            sign, g.FFTW_ESTIMATE, prec)
+        plans.append(p)
+    return xin, yout, offs, plans
+
+
+def _check(restatement, xin, yout, offs, lengths, prec, sign, sample=None):
+    x = xin.cpu().numpy()
+    y = yout.cpu().numpy()
+    tol = 1e-6 if prec == "f" else 1e-14
+    idx = range(len(lengths)) if sample is None else sample
+    worst = 0.0
+    for i in idx:
+        a, b = int(offs[i]), int(offs[i + 1])
+        xo = x[a:b].astype(np.clongdouble if prec == "d" else np.complex128)
+        ref = restatement.c2c(xo, [b - a], sign, "l" if prec == "d" else "d")
+        e = rel_l2(y[a:b], ref)
+        worst = max(worst, e)
+        assert e <= tol, f"transform {i} (n={b - a}): rel L2 {e:.3e}"
+    return worst
+
+
+def _set_of(plans, prec):
+    import fftw3_gb300 as g
+    lib = g.load()
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    arr = (ctypes.c_void_p * len(plans))(*[p.ptr for p in plans])
+    f = getattr(lib, pfx + "gb300_plan_set")
+    f.restype = ctypes.c_void_p
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint]
+    s = f(len(plans), arr, g.FFTW_ESTIMATE)
+    assert s, g.last_error()
+    getattr(lib, pfx + "gb300_execute_set").argtypes = [ctypes.c_void_p]
+    getattr(lib, pfx + "gb300_destroy_set").argtypes = [ctypes.c_void_p]
+    return lib, pfx, s
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_planset_mixed_lengths(lib, torch_cuda_set, restatement, prec):
+    torch = torch_cuda_set
+    import bench
+    rng = np.random.default_rng(42)
+    if prec == "f":
+        lengths = bench.uneven_lengths(rng, 240)
+        lengths += [64, 128, 4096, 8192, 16384, 65536, 60000, 17, 4093, 2039, 97, 1]
+    else:
+        lengths = bench.uneven_lengths(rng, 160, max_pow2=14, max_smooth=20000, max_prime=2047)
+        lengths += [64, 4096, 8192, 16384, 17, 2039, 1]
+    xin, yout, offs, plans = _make_set(torch, lengths, prec)
+    lib_, pfx, s = _set_of(plans, prec)
+    import fftw3_gb300 as g
+    before = g.launch_count()
+    assert getattr(lib_, pfx + "gb300_execute_set")(s) == 0, g.last_error()
+    torch.cuda.synchronize()
+    _check(restatement, xin, yout, offs, lengths, prec, -1)
+    # executing again gives the same result (counters and queue head reset by the graph)
+    y1 = yout.clone()
+    yout.zero_()
+    assert getattr(lib_, pfx + "gb300_execute_set")(s) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(y1, yout)
+    assert lib_.fftw_gb300_device_status() == 0
+    # the same plans one by one give the same transforms (within tolerance)
+    y2 = torch.zeros_like(yout)
+    es = yout.element_size()
+    for i, p in enumerate(plans):
+        p.execute_dft(xin.data_ptr() + int(offs[i]) * es, y2.data_ptr() + int(offs[i]) * es)
+    torch.cuda.synchronize()
+    assert rel_l2(y2.cpu().numpy(), y1.cpu().numpy()) < (2e-6 if prec == "f" else 1e-13)
+    getattr(lib_, pfx + "gb300_destroy_set")(s)
+
+
+def test_planset_backward_and_rader(lib, torch_cuda_set, restatement, monkeypatch):
+    monkeypatch.setenv("FFTW_GB300_PRIME", "rader")
+    torch = torch_cuda_set
+    lengths = [17, 31, 61, 97, 401, 673, 1201, 3001, 64, 60, 210, 5000, 32768]
+    xin, yout, offs, plans = _make_set(torch, lengths, "f", sign=1, seed=3)
+    lib_, pfx, s = _set_of(plans, "f")
+    assert getattr(lib_, pfx + "gb300_execute_set")(s) == 0
+    torch.cuda.synchronize()
+    _check(restatement, xin, yout, offs, lengths, "f", 1)
+    getattr(lib_, pfx + "gb300_destroy_set")(s)
+
+
+@pytest.fixture(scope="module")
+def torch_cuda_set():
+    import torch
+    assert torch.cuda.is_available()
+    return torch

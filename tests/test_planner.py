@@ -23,13 +23,13 @@ def passes(p):
 def test_batched_1d_is_one_pass():
     p = g.plan_many_dft([4096], 65536, 1 << 20, 1 << 30, prec="f")
     (ps,) = passes(p)
-    assert ps["nfft"] == 4096 and ps["variant"] == 0 and ps["blocks"] * ps["tb"] >= 65536
+    assert ps["nfft"] == 4096 and ps["variant"] in (0, 2) and ps["blocks"] * ps["tb"] >= 65536
 
 
 def test_double_precision_pass():
     p = g.plan_many_dft([1024], 4096, 1 << 20, 1 << 30, prec="d")
     (ps,) = passes(p)
-    assert ps["nfft"] == 1024 and ps["variant"] == 0
+    assert ps["nfft"] == 1024 and ps["variant"] in (0, 2)
 
 
 def test_long_transform_is_two_passes_with_scratch(lib):
@@ -125,3 +125,13 @@ def test_print_plan_names_passes():
     p = g.plan_many_dft([4096], 16, 1 << 20, 1 << 30, prec="f")
     s = p.describe()
     assert s.startswith("(gb300-dft-f32") and "nfft=4096" in s
+
+
+def test_prime_rader_when_asked(monkeypatch):
+    monkeypatch.setenv("FFTW_GB300_PRIME", "rader")
+    p = g.plan_many_dft([401], 10, 1 << 20, 1 << 30, prec="f")
+    (ps,) = passes(p)
+    assert ps["kind"] == 5 and ps["nfft"] == 400
+    # p-1 with a prime factor > 13 falls back to Bluestein
+    p = g.plan_many_dft([1021], 10, 1 << 20, 1 << 30, prec="f")
+    assert passes(p)[0]["kind"] == 3
