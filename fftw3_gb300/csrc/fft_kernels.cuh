@@ -207,6 +207,22 @@ __device__ __forceinline__ void apply_twiddles(C *v, const C *__restrict__ tw, i
      }
 }
 
+/* x[e] = element tid + T*e of the swizzled transform in shared memory */
+template <typename C, int N>
+__device__ __forceinline__ void reg_gather(C (&x)[reg_e(N)], int tid, const C *smt)
+{
+     constexpr int E = reg_e(N);
+     constexpr int T = N / E;
+     if constexpr (T % 16 == 0) {
+          const C *s = smt + pad_for(N, tid);
+#pragma unroll
+          for (int e = 0; e < E; ++e) x[e] = s[e * (T + pad_mult(N) * (T >> 4))];
+     } else {
+#pragma unroll
+          for (int e = 0; e < E; ++e) x[e] = smt[pad_for(N, tid + T * e)];
+     }
+}
+
 template <typename C, int N, int DIR, int NS>
 __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, const C *__restrict__ tw)
 {
@@ -235,6 +251,11 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
 #pragma unroll
                for (int q = 0; q < 8; ++q)
                     d[q] = make_float4(v[2 * q].x, v[2 * q].y, v[2 * q + 1].x, v[2 * q + 1].y);
+          } else if constexpr (NS % 16 == 0) {
+               /* the swizzle is linear across multiples of 16: one base, constant steps */
+               C *d = smt + pad_for(N, (j / NS) * NS * RAD + k);
+#pragma unroll
+               for (int q = 0; q < RAD; ++q) d[q * (NS + pad_mult(N) * (NS >> 4))] = v[q];
           } else {
                const int base = (j / NS) * NS * RAD + k;
 #pragma unroll
@@ -243,8 +264,7 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
      }
      if constexpr (!LAST) {
           __syncthreads();
-#pragma unroll
-          for (int e = 0; e < E; ++e) x[e] = smt[pad_for(N, tid + T * e)];
+          reg_gather<C, N>(x, tid, smt);
           __syncthreads();
           reg_stages<C, N, DIR, NS * RAD>(x, tid, smt, tw);
      }
@@ -524,8 +544,10 @@ __global__ void __launch_bounds__(256, 3) k_reg_tma(const gb_pass P, const void 
                for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
           }
           if (valid) {
+               /* unit output stride (checked at launch): constant offsets */
+               C *o = (C *)out + bo + tid;
 #pragma unroll
-               for (int e = 0; e < E; ++e) io<C>::stc(out, bo, tid + T * e, P.os, x[e]);
+               for (int e = 0; e < E; ++e) o[T * e] = x[e];
           }
      }
 }

@@ -17,6 +17,8 @@ extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir);
 extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
 extern "C" const void *gb_tma_kernel_f(int logn, int dir);
 extern "C" const void *gb_tma_kernel_d(int logn, int dir);
+extern "C" const void *gb_tc_kernel(int nfft, int dir);
+extern "C" int gb_tc_smem(int nfft);
 
 namespace gb {
 
@@ -148,6 +150,7 @@ static const void *pick_kernel(const gb_pass *p)
 {
      if (p->kind == GB_KIND_COPY)
           return p->prec == 4 ? (const void *)k_copy<float2> : (const void *)k_copy<double2>;
+     if (p->variant == GB_VAR_TC) return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_tc_kernel(p->nfft, p->sign) : 0;
      if (p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA) {
           int logn = 0;
           while ((1 << logn) < p->nfft) ++logn;
@@ -164,7 +167,7 @@ static const void *pick_kernel(const gb_pass *p)
 static unsigned grid_of(const gb_pass *p, const void *fn)
 {
      long long g = p->nblocks;
-     if (p->variant == GB_VAR_TMA) {
+     if (p->variant == GB_VAR_TMA || p->variant == GB_VAR_TC) {
           int dev = 0, sms = 0, per = 0;
           cudaGetDevice(&dev);
           cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -228,10 +231,14 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->variant == GB_VAR_REG && p->threads > reg_maxthreads(p->nfft)) bad = "tile exceeds the kernel's launch bounds";
           else if (reg_sms(p->nfft) != gb_reg_sms(p->nfft)) bad = "host and device shared-memory layouts disagree";
           else if (p->variant == GB_VAR_REG && p->smem < p->tb * reg_sms(p->nfft) * 2 * p->prec) bad = "shared memory too small for the tile";
-          else if (p->variant == GB_VAR_TMA && (p->threads > 256 || p->kind != GB_KIND_C2C || p->is != 1 ||
+          else if (p->variant == GB_VAR_TMA && (p->threads > 256 || p->kind != GB_KIND_C2C || p->is != 1 || p->os != 1 ||
                                                 p->smem < 2 * p->tb * tma_sms(p->nfft) * 2 * p->prec))
-               bad = "persistent bulk-copy pass needs unit-stride c2c, <= 256 threads and two smem slots";
+               bad = "persistent bulk-copy pass needs unit-stride c2c in and out, <= 256 threads and two smem slots";
           else if (p->variant == GB_VAR_TMA && ((uintptr_t)in % 16 != 0)) bad = "bulk copies need a 16-byte aligned input";
+          else if (p->variant == GB_VAR_TC && (p->prec != 4 || (p->nfft != 256 && p->nfft != 4096) || p->is != 1 ||
+                                               p->os != 1 || p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||
+                                               p->smem < gb_tc_smem(p->nfft)))
+               bad = "tensor-core pass needs f32 unit-stride c2c of 256 or 4096 points, 256 threads";
           if (bad) {
                snprintf(gb_errbuf, sizeof gb_errbuf, "refused pass (kind %d nfft %d): %s", p->kind, p->nfft, bad);
                return -1;

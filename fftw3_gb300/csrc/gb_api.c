@@ -164,3 +164,4 @@ GB_SET_EXT(fftw_, fftw_plan, fftw_gb300_set, 8)
 GB_SET_EXT(fftwf_, fftwf_plan, fftwf_gb300_set, 4)
 
 int fftw_gb300_device_status(void) { return gb_device_status(); }
+int fftw_gb300_tc_selftest(const void *A, const void *B, float *D, int ks) { return gb_tc_selftest(A, B, D, ks); }

@@ -376,7 +376,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                P->store_mode = GB_MOVE_ROWS;
           /* unit-stride c2c with 16-byte aligned transform starts: persistent
            * CTAs fed by bulk async copies (k_reg_tma) */
-          if (kind == GB_KIND_C2C && is == 1 && nfft >= 64 && nfft <= 4096 && tb_hint == 0 &&
+          if (kind == GB_KIND_C2C && is == 1 && os == 1 && nfft >= 64 && nfft <= 4096 && tb_hint == 0 &&
               !getenv("FFTW_GB300_NO_TMA")) {
                int ok = 1, tbt = 256 / T;
                long long sm2;
@@ -487,6 +487,28 @@ static void count_ops(gb_plan *p, const gb_pass *P, long long howmany)
      p->mul += 0.4 * per * howmany;
 }
 
+/* The split-FP16 tensor-core form (FFTW_GB300_TENSOR_CORE): f32 unit-stride
+ * c2c of 256 or 4096 points, 256 threads (one radix-16 butterfly each). */
+static void use_tensor_cores(gb_pass *P)
+{
+     int i;
+     if (P->kind != GB_KIND_C2C || P->prec != 4 || (P->nfft != 256 && P->nfft != 4096) || P->is != 1 ||
+         P->os != 1 || P->post_N)
+          return;
+     for (i = 0; i < P->nv; ++i)
+          if (P->vis[i] % 2 || P->vos[i] % 2) return;
+     if (gb_tc_smem(P->nfft) > smem_max()) return;
+     P->variant = GB_VAR_TC;
+     P->tb = 256 / (P->nfft / 16);
+     P->threads = 256;
+     P->smem = gb_tc_smem(P->nfft);
+     P->load_mode = GB_MOVE_ROWS;
+     P->store_mode = GB_MOVE_DIRECT;
+     P->ntiles0 = (P->vn[0] + P->tb - 1) / P->tb;
+     P->nblocks = P->ntiles0;
+     for (i = 1; i < P->nv; ++i) P->nblocks *= P->vn[i];
+}
+
 /* Prime lengths: Rader (dft/rader.c) when n-1 factors into radices <= 13
  * and the wisdom or FFTW_GB300_PRIME=rader asks for it; Bluestein
  * otherwise (one CTA, power-of-two convolution, register stages). */
@@ -556,6 +578,7 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
      }
      rc = config_pass(&s->pass, prec, kind, n, sign, is, os, nvk - s->nloop, v + s->nloop,
                       w ? w->tb : 0, 0);
+     if (rc == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
      if (rc == 0) {
           if (pass_tables(&s->pass)) { b->err = 1; return; }
           count_ops(p, &s->pass, howmany);
@@ -671,7 +694,8 @@ static void describe(gb_plan *p)
           static const char *mv[] = {"direct", "rows", "cols"};
           off += snprintf(p->desc + off, sizeof p->desc - off,
                           "\n  (pass %s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
-                          kk[P->kind], P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" : "gen", P->tb,
+                          kk[P->kind], P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" :
+                          P->variant == GB_VAR_TC ? "tc-split-fp16" : "gen", P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
                           P->vn[0], P->post_N ? " +twiddle" : "");
      }

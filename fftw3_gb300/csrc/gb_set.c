@@ -86,6 +86,22 @@ static int item_pass(gb_pass *P, int prec, int kind, long long n, int sign, long
      return 0;
 }
 
+/* growable item array */
+typedef struct { gb_qitem *v; int n, cap; } qvec;
+
+static gb_qitem *qpush(qvec *q)
+{
+     if (q->n == q->cap) {
+          int nc = q->cap ? 2 * q->cap : 256;
+          gb_qitem *nv = (gb_qitem *)realloc(q->v, sizeof(gb_qitem) * (size_t)nc);
+          if (!nv) return 0;
+          q->v = nv;
+          q->cap = nc;
+     }
+     memset(&q->v[q->n], 0, sizeof(gb_qitem));
+     return &q->v[q->n++];
+}
+
 static double item_cost(const gb_qitem *q)
 {
      double n = q->P.nfft;
@@ -130,9 +146,9 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
      xform *xs;
      int nx = 0, cap = prec == 4 ? 8192 : 4096, i, j;
      int cs = 2 * prec;
-     size_t maxitems;
-     gb_qitem *A = 0, *M = 0, *B = 0;
-     int na = 0, nm = 0, nb = 0, cap_a, cap_m, cap_b;
+     qvec QA = {0, 0, 0}, QM = {0, 0, 0}, QB = {0, 0, 0};
+     gb_qitem *A, *M, *B;
+     int na, nm, nb;
      void **hptr = 0;
      int nptr = 0, cap_ptr;
      long long scratch_elems = 0;
@@ -165,11 +181,6 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           }
      }
      qsort(xs, (size_t)nx, sizeof(xform), cmp_key);
-     maxitems = (size_t)nx * 4 + 64;
-     cap_a = cap_m = cap_b = (int)maxitems;
-     A = (gb_qitem *)calloc((size_t)cap_a, sizeof(gb_qitem));
-     M = (gb_qitem *)calloc((size_t)cap_m, sizeof(gb_qitem));
-     B = (gb_qitem *)calloc((size_t)cap_b, sizeof(gb_qitem));
      cap_ptr = 2 * nx + 2;
      hptr = (void **)calloc((size_t)cap_ptr, sizeof(void *));
 
@@ -191,7 +202,8 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                for (g = 0; i + g < nx && g < tbmax && cmp_key(&xs[i], &xs[i + g]) == 0; ++g) {}
                if (item_pass(&tmp, prec, kind, n, x->sign, x->is, x->os, g, 0, 0, g, 0, 0)) goto fail;
                {
-                    gb_qitem *q = &M[nm++];
+                    gb_qitem *q = qpush(&QM);
+                    if (!q) goto fail;
                     q->P = tmp;
                     q->pin = (const void *const *)(size_t)nptr;     /* index now, device address later */
                     q->pout = (void *const *)(size_t)(nptr + g);
@@ -226,7 +238,8 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                pa.post_N = n;
                if (gb_pass_tables(&pa)) goto fail;
                for (k0 = 0; k0 < n2; k0 += tbc) {
-                    gb_qitem *q = &A[na++];
+                    gb_qitem *q = qpush(&QA);
+                    if (!q) goto fail;
                     q->P = pa;
                     q->v0 = k0;
                     q->in = x->in;
@@ -239,7 +252,8 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                 * with element stride n1, into out[k1 + n1*k2] */
                if (item_pass(&pb, prec, GB_KIND_C2C, n2, x->sign, n1, n1 * x->os, n1, 1, x->os, tbc, 1, 1)) goto fail;
                for (k0 = 0; k0 < n1; k0 += tbc) {
-                    gb_qitem *q = &B[nb++];
+                    gb_qitem *q = qpush(&QB);
+                    if (!q) goto fail;
                     q->P = pb;
                     q->v0 = k0;
                     q->in = (const void *)(size_t)scratch_elems;
@@ -248,11 +262,12 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                }
                if (pb.smem > smem) smem = pb.smem;
                scratch_elems += n;
-               if (na + 4 > cap_a || nb + 4 > cap_b) { gb_set_error("plan set: too many tiles"); goto fail; }
           }
           ++i;
      }
-     qsort(M, (size_t)nm, sizeof(gb_qitem), cmp_cost_desc);
+     A = QA.v; M = QM.v; B = QB.v;
+     na = QA.n; nm = QM.n; nb = QB.n;
+     if (nm) qsort(M, (size_t)nm, sizeof(gb_qitem), cmp_cost_desc);
 
      S = (gb_set *)calloc(1, sizeof *S);
      S->prec = prec;
@@ -305,10 +320,10 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           }
           free(all);
      }
-     free(A); free(M); free(B); free(hptr); free(xs);
+     free(QA.v); free(QM.v); free(QB.v); free(hptr); free(xs);
      return S;
 fail:
-     free(A); free(M); free(B); free(hptr); free(xs);
+     free(QA.v); free(QM.v); free(QB.v); free(hptr); free(xs);
      return 0;
 }
 

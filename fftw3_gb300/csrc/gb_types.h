@@ -34,7 +34,8 @@ enum gb_kind {
 enum gb_variant {
      GB_VAR_REG = 0,   /* power-of-two length, register-resident Stockham stages of radix <= 16 */
      GB_VAR_GEN = 1,   /* any smooth length, shared-memory Stockham stages, runtime radix list */
-     GB_VAR_TMA = 2    /* as GB_VAR_REG, persistent CTAs fed by bulk async copies (unit-stride c2c) */
+     GB_VAR_TMA = 2,   /* as GB_VAR_REG, persistent CTAs fed by bulk async copies (unit-stride c2c) */
+     GB_VAR_TC = 3     /* radix-16 stages as split-FP16 tcgen05 GEMMs (nfft 256 or 4096, f32, unit stride) */
 };
 
 /* How a tile of transforms moves between HBM and the CTA. */

@@ -16,6 +16,11 @@
 extern "C" {
 #endif
 
+/* Planner flag (a bit the reference leaves unused): run the radix-16 stages
+ * of f32 unit-stride c2c plans of 256 or 4096 points on the tensor cores,
+ * as split-FP16 (hi + lo) DFT-matrix GEMMs with FP32 accumulation. */
+#define FFTW_GB300_TENSOR_CORE (1U << 28)
+
 /* Message of the last planner or execute failure in this thread. */
 extern const char *fftw_gb300_last_error(void);
 /* Number of execute calls that failed since the library was loaded. */
@@ -29,6 +34,10 @@ extern long long fftw_gb300_launch_count(void);
  * problem, else a code (2: a work-queue dependency wait gave up, 3: a bulk
  * copy never completed); kernels bound every wait instead of hanging. */
 extern int fftw_gb300_device_status(void);
+/* Tensor-core path self-test: D = A . B^T with A 128 x 16ks and B 32 x 16ks
+ * (IEEE half, row-major, device memory) and D 128 x 32 (float, device);
+ * ks in 1..6.  Returns 0 on success. */
+extern int fftw_gb300_tc_selftest(const void *A, const void *B, float *D, int ks);
 
 #define GB_FFTW_EXT_DECLARE(PFX)                                                       \
 extern int PFX##gb300_set_stream(PFX##plan p, void *cuda_stream);                     \
