@@ -61,6 +61,18 @@ static int device_accessible(const void *ptr)
      return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+/* Page-locked host memory mapped into the device address space (what
+ * fftw_malloc returns): its device address, else NULL. */
+static void *mapped_host(const void *ptr)
+{
+     struct cudaPointerAttributes a;
+     if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+          cudaGetLastError();
+          return 0;
+     }
+     return (a.type == cudaMemoryTypeHost) ? a.devicePointer : 0;
+}
+
 static int ensure(void **buf, size_t *have, size_t need)
 {
      if (*have >= need) return 0;
@@ -76,7 +88,8 @@ static int ensure(void **buf, size_t *have, size_t need)
      return 0;
 }
 
-static int run_step(const gb_plan *p, const gb_step *s, char *bufs[3], int esz[3], int real_pairs_ok[3])
+static int run_step(const gb_plan *p, const gb_step *s, char *bufs[3], int esz[3], int real_pairs_ok[3],
+                    int direct_host)
 {
      gb_pass P = s->pass;
      long long idx[GB_MAXLOOP];
@@ -95,8 +108,9 @@ static int run_step(const gb_plan *p, const gb_step *s, char *bufs[3], int esz[3
           if (s->dst_off % 2) ok = 0;
           P.real_pairs = ok;
      }
-     if (P.variant == GB_VAR_TMA && ((uintptr_t)(bufs[si] + s->src_off * esz[si]) % 16)) {
-          /* input not 16-byte aligned for bulk copies: same tile, register path */
+     if (P.variant == GB_VAR_TMA && (direct_host || ((uintptr_t)(bufs[si] + s->src_off * esz[si]) % 16))) {
+          /* host memory or an input not 16-byte aligned: same tile, plain loads
+           * (register kernel) instead of bulk copies */
           P.variant = GB_VAR_REG;
           P.smem = P.tb * gb_reg_sms(P.nfft) * 2 * P.prec;
      }
@@ -129,7 +143,7 @@ int gb_execute(gb_plan *p, void *in, void *out)
      int esin = elsize(prb, 0), esout = elsize(prb, 1);
      int cs = 2 * prb->prec;
      int inplace = (in == out);
-     int stage_i, stage_o;
+     int stage_i, stage_o, direct_host = 0;
      char *din, *dout;
      char *bufs[3];
      int esz[3], rp[3];
@@ -150,6 +164,19 @@ int gb_execute(gb_plan *p, void *in, void *out)
 
      din = (char *)in;
      dout = (char *)out;
+     /* single-pass plans on page-locked host arrays: the kernel reads and
+      * writes host memory directly over the CPU-GPU link (both directions at
+      * once, no staging copies) */
+     if ((stage_i || stage_o) && p->nstep == 1 && !getenv("FFTW_GB300_STAGE_HOST")) {
+          void *mi = stage_i ? mapped_host(in) : (void *)in, *mo = stage_o ? mapped_host(out) : out;
+          if (mi && mo && ((uintptr_t)mi % (esin == cs ? cs : prb->prec)) == 0 &&
+              ((uintptr_t)mo % (esout == cs ? cs : prb->prec)) == 0) {
+               din = (char *)mi;
+               dout = (char *)mo;
+               stage_i = stage_o = 0;
+               direct_host = 1;
+          }
+     }
      if (inplace && stage_i) {
           long long lo = ein.lo * esin < eout.lo * esout ? ein.lo * esin : eout.lo * esout;
           long long hi = (ein.hi + 1) * esin > (eout.hi + 1) * esout ? (ein.hi + 1) * esin : (eout.hi + 1) * esout;
@@ -189,7 +216,7 @@ int gb_execute(gb_plan *p, void *in, void *out)
       * c2r reads complex (its c2c passes work in place there) and writes
       * reals; scratch is complex */
      for (k = 0; k < p->nstep; ++k)
-          if (run_step(p, &p->step[k], bufs, esz, rp)) return -1;
+          if (run_step(p, &p->step[k], bufs, esz, rp, direct_host)) return -1;
 
      if (inplace && stage_i) {
           long long lo = ein.lo * esin < eout.lo * esout ? ein.lo * esin : eout.lo * esout;
@@ -201,7 +228,7 @@ int gb_execute(gb_plan *p, void *in, void *out)
                               device_accessible(out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st) != cudaSuccess)
                goto cuerr;
      }
-     if (stage_i || stage_o || !p->async) {
+     if (stage_i || stage_o || direct_host || !p->async) {
           if (cudaStreamSynchronize(st) != cudaSuccess) goto cuerr;
      }
      return 0;

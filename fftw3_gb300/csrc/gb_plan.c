@@ -58,6 +58,10 @@ int gb_cuda_ready(void)
      return state;
 }
 
+/* planner-wide choice set by add_1d from wisdom (the planner runs under the
+ * library lock): 1 = do not use the bulk-copy fed persistent variant */
+static int cfg_no_tma = 0;
+
 static int smem_max(void)
 {
      static int v = 0;
@@ -376,7 +380,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                P->store_mode = GB_MOVE_ROWS;
           /* unit-stride c2c with 16-byte aligned transform starts: persistent
            * CTAs fed by bulk async copies (k_reg_tma) */
-          if (kind == GB_KIND_C2C && is == 1 && os == 1 && nfft >= 64 && nfft <= 4096 && tb_hint == 0 &&
+          if (kind == GB_KIND_C2C && is == 1 && os == 1 && nfft >= 64 && nfft <= 4096 && tb_hint == 0 && !cfg_no_tma &&
               !getenv("FFTW_GB300_NO_TMA")) {
                int ok = 1, tbt = 256 / T;
                long long sm2;
@@ -576,8 +580,10 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
           s->nloop = nvk - GB_MAXV;
           for (i = 0; i < s->nloop; ++i) s->loop[i] = v[i];
      }
+     cfg_no_tma = (w && w->variant == GB_VAR_REG);
      rc = config_pass(&s->pass, prec, kind, n, sign, is, os, nvk - s->nloop, v + s->nloop,
-                      w ? w->tb : 0, 0);
+                      (w && w->tb > 0) ? w->tb : 0, 0);
+     cfg_no_tma = 0;
      if (rc == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
      if (rc == 0) {
           if (pass_tables(&s->pass)) { b->err = 1; return; }
