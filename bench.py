@@ -40,6 +40,8 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # name: (kind, shape, howmany, prec, inplace)
     "c2c4096": ("c2c", [4096], 65536, "f", False),
+    "c2c256": ("c2c", [256], 1 << 20, "f", False),
+    "c2c65536": ("c2c", [65536], 4096, "f", False),
     "c2c1024d": ("c2c", [1024], 4096, "d", False),
     "r2c16384": ("r2c", [16384], 16384, "f", False),
     "c2c1m": ("c2c", [1 << 20], 64, "f", False),
@@ -321,6 +323,11 @@ def run_ours(args):
                                 "d" if prec == "f" else "l", os.cpu_count() or 1)
         err = rel_l2(yout[: k * nc].cpu().numpy(), ref)
 
+    # the split-FP16 tensor-core form on the same batch, beside the FP32 form
+    tc = None
+    if kind == "c2c" and prec == "f" and n in (256, 4096, 65536) and not args.no_tc:
+        tc = run_tc_form(g, shape, howmany, xin, yout, stream, args, fl, ws)
+
     # dominant kernel: per-launch time from the events (one pass per step for
     # single-pass plans; per-pass share otherwise is taken from the ncu list)
     npass = len(p.passes())
@@ -358,6 +365,7 @@ def run_ours(args):
             "clocks": clk.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "tc_form": tc,
         }
         print(json.dumps(out))
     if ws > 1:
@@ -465,6 +473,40 @@ def run_uneven(args):
     print(json.dumps(out))
 
 
+def run_tc_form(g, shape, howmany, xin, yout, stream, args, fl, ws):
+    """Time the FFTW_GB300_TENSOR_CORE plan (radix-16 stages as split-FP16
+    tcgen05 GEMMs) on the same input and report it beside the FP32 form,
+    with its error against the FP64 oracle on a sample of transforms."""
+    import numpy as np
+    import torch
+    from oracle.oracle import Restatement, rel_l2
+    n = math.prod(shape)
+    p = g.plan_many_dft(shape, howmany, xin.data_ptr(), yout.data_ptr(), -1, g.FFTW_ESTIMATE | (1 << 28), "f")
+    if "tc-split-fp16" not in p.describe():
+        return None
+    p.set_stream(stream.cuda_stream)
+    p.set_async(True)
+    for _ in range(args.warmup):
+        p.execute()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        p.execute()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    k = min(howmany, 16)
+    ref = Restatement().c2c(xin[: k * n].cpu().numpy().astype(np.complex128), shape, -1, "d", os.cpu_count() or 1)
+    err = rel_l2(yout[: k * n].cpu().numpy(), ref)
+    hbm, _ = peaks()
+    alg = 2 * n * 8 * howmany
+    return {"value": round(fl * ws / (ms * 1e-3) / 1e9, 2), "unit": "Gflop/s", "ms_per_step": round(ms, 4),
+            "hbm_frac": round(alg / (ms * 1e-3) / 1e9 / hbm, 4), "rel_l2_vs_fp64_oracle": err,
+            "passes": len(p.passes()),
+            "form": "radix-16 stages as tcgen05 kind::f16 GEMMs, operands split FP16 hi+lo (3 products), FP32 accumulate"}
+
+
 def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
     """fftwf_execute_dft on page-locked host arrays: H2D + passes + D2H timed."""
     import ctypes
@@ -508,6 +550,7 @@ def main():
     ap.add_argument("--howmany", type=int, default=0, help="override the batch (profiling runs only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tc", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

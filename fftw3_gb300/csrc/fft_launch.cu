@@ -235,10 +235,10 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
                                                 p->smem < 2 * p->tb * tma_sms(p->nfft) * 2 * p->prec))
                bad = "persistent bulk-copy pass needs unit-stride c2c in and out, <= 256 threads and two smem slots";
           else if (p->variant == GB_VAR_TMA && ((uintptr_t)in % 16 != 0)) bad = "bulk copies need a 16-byte aligned input";
-          else if (p->variant == GB_VAR_TC && (p->prec != 4 || (p->nfft != 256 && p->nfft != 4096) || p->is != 1 ||
-                                               p->os != 1 || p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||
-                                               p->smem < gb_tc_smem(p->nfft)))
-               bad = "tensor-core pass needs f32 unit-stride c2c of 256 or 4096 points, 256 threads";
+          else if (p->variant == GB_VAR_TC && (p->prec != 4 || (p->nfft != 256 && p->nfft != 4096) ||
+                                               p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||
+                                               p->smem < gb_tc_smem(p->nfft) || (p->store_mode == GB_MOVE_DIRECT && p->os != 1)))
+               bad = "tensor-core pass needs f32 c2c of 256 or 4096 points, 256 threads";
           if (bad) {
                snprintf(gb_errbuf, sizeof gb_errbuf, "refused pass (kind %d nfft %d): %s", p->kind, p->nfft, bad);
                return -1;

@@ -1,6 +1,8 @@
 /*
  * Tensor-core form of the radix-16 stages (tcgen05, split FP16, FP32
- * accumulation), for batched unit-stride c2c of N = 256 and 4096 (16^2, 16^3).
+ * accumulation), for batched c2c of N = 256 and 4096 (16^2, 16^3) in any
+ * layout (rows, adjacent columns, or the two passes of a 65536 = 256 x 256
+ * four-step with its W_N^(n2 k1) twiddle).
  *
  * Per stage, each of the CTA's 256 threads owns one radix-16 butterfly: it
  * gathers its 16 inputs from the shared-memory copy of the transform(s),
@@ -131,11 +133,15 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
 
      for (long long blk = blockIdx.x; blk < P.nblocks && ok; blk += gridDim.x) {
           const tile_t tile = tile_of(P, blk);
-          /* load TB transforms (unit stride) */
+          /* load TB transforms: element-fast for unit-stride rows, transform-
+           * fast for adjacent columns (four-step tiles, strided axes) */
           for (int i = threadIdx.x; i < TB * N; i += blockDim.x) {
-               const int t = i / N, e = i - t * N;
+               int t, e;
+               if (P.load_mode == GB_MOVE_COLS) { t = i % TB; e = i / TB; }
+               else { t = i / N; e = i - t * N; }
                const long long v = tile.v0 + t;
-               dat[i] = (v < P.vn[0]) ? ((const float2 *)in)[tile.bi + v * P.vis[0] + e] : make_float2(0.f, 0.f);
+               dat[t * N + e] = (v < P.vn[0]) ? ((const float2 *)in)[tile.bi + v * P.vis[0] + e * P.is]
+                                              : make_float2(0.f, 0.f);
           }
           __syncthreads();
           int NS = 1;
@@ -207,17 +213,41 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
 #pragma unroll
                     for (int q = 0; q < 16; ++q) dt[base + q * NS] = make_float2(v[q] * inv, v[16 + q] * inv);
                } else {
+                    /* outputs j + q*T in natural order; four-step passes also
+                     * apply W_postN^(v*k) */
                     const long long vv = tile.v0 + tl;
-                    if (vv < P.vn[0]) {
-                         float2 *o = (float2 *)out + tile.bo + vv * P.vos[0] + j;
+                    float2 y[16];
 #pragma unroll
-                         for (int q = 0; q < 16; ++q) o[q * T] = make_float2(v[q] * inv, v[16 + q] * inv);
+                    for (int q = 0; q < 16; ++q) y[q] = make_float2(v[q] * inv, v[16 + q] * inv);
+                    if (P.post_N) {
+#pragma unroll
+                         for (int q = 0; q < 16; ++q) y[q] = cmul(y[q], post_twiddle<float2>(P, vv * (long long)(j + q * T)));
+                    }
+                    if (P.store_mode == GB_MOVE_DIRECT) {
+                         if (vv < P.vn[0]) {
+                              float2 *o = (float2 *)out + tile.bo + vv * P.vos[0] + j;
+#pragma unroll
+                              for (int q = 0; q < 16; ++q) o[q * T] = y[q];
+                         }
+                    } else {
+#pragma unroll
+                         for (int q = 0; q < 16; ++q) dt[j + q * T] = y[q];
                     }
                }
                tc::fence_before_sync();
                __syncthreads();
                tc::fence_after_sync();
                NS *= 16;
+          }
+          if (ok && P.store_mode != GB_MOVE_DIRECT) {
+               for (int i = threadIdx.x; i < TB * N; i += blockDim.x) {
+                    int t, e;
+                    if (P.store_mode == GB_MOVE_COLS) { t = i % TB; e = i / TB; }
+                    else { t = i / N; e = i - t * N; }
+                    const long long v = tile.v0 + t;
+                    if (v < P.vn[0]) ((float2 *)out)[tile.bo + v * P.vos[0] + e * P.os] = dat[t * N + e];
+               }
+               __syncthreads();
           }
      }
      if (!ok && threadIdx.x == 0 && P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);

@@ -496,18 +496,14 @@ static void count_ops(gb_plan *p, const gb_pass *P, long long howmany)
 static void use_tensor_cores(gb_pass *P)
 {
      int i;
-     if (P->kind != GB_KIND_C2C || P->prec != 4 || (P->nfft != 256 && P->nfft != 4096) || P->is != 1 ||
-         P->os != 1 || P->post_N)
-          return;
-     for (i = 0; i < P->nv; ++i)
-          if (P->vis[i] % 2 || P->vos[i] % 2) return;
+     if (P->kind != GB_KIND_C2C || P->prec != 4 || (P->nfft != 256 && P->nfft != 4096)) return;
      if (gb_tc_smem(P->nfft) > smem_max()) return;
      P->variant = GB_VAR_TC;
      P->tb = 256 / (P->nfft / 16);
      P->threads = 256;
      P->smem = gb_tc_smem(P->nfft);
-     P->load_mode = GB_MOVE_ROWS;
-     P->store_mode = GB_MOVE_DIRECT;
+     P->load_mode = (P->is == 1 || llabs_(P->vis[0]) != 1) ? GB_MOVE_ROWS : GB_MOVE_COLS;
+     P->store_mode = (P->os == 1) ? GB_MOVE_DIRECT : (llabs_(P->vos[0]) == 1) ? GB_MOVE_COLS : GB_MOVE_ROWS;
      P->ntiles0 = (P->vn[0] + P->tb - 1) / P->tb;
      P->nblocks = P->ntiles0;
      for (i = 1; i < P->nv; ++i) P->nblocks *= P->vn[i];
@@ -663,6 +659,7 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
           if (na > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
           /* dim 0 stays n2: the twiddle W_n^(n2 k1) indexes it */
           r1 = config_pass(&s->pass, prec, GB_KIND_C2C, n1, sign, n2 * is, 1, na, va, 0, 1);
+          if (r1 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
           s->pass.post_N = n;
           if (r1 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass A config failed"); b->err = 1; return; }
           count_ops(p, &s->pass, howmany * n2);
@@ -680,6 +677,7 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
           s->src = GB_BUF_SCRATCH; s->dst = dst;
           if (nb > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
           r2 = config_pass(&s->pass, prec, GB_KIND_C2C, n2, sign, n1, n1 * os, nb, vb, 0, 1);
+          if (r2 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
           if (r2 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass B config failed"); b->err = 1; return; }
           count_ops(p, &s->pass, howmany * n1);
           return;

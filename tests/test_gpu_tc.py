@@ -41,13 +41,14 @@ def test_tc_gemm_selftest(lib, torch_tc, ks):
     assert lib_.fftw_gb300_device_status() == 0
 
 
-@pytest.mark.parametrize("n", [256, 4096])
+@pytest.mark.parametrize("n", [256, 4096, 65536])
 @pytest.mark.parametrize("dist", ["normal", "loguniform"])
 @pytest.mark.parametrize("sign", [-1, 1])
 def test_tc_fft_parity(lib, torch_tc, restatement, n, dist, sign):
+    """1D batches; 65536 runs as two tensor-core passes of 256 (four-step)."""
     import fftw3_gb300 as g
     torch = torch_tc
-    hm = 64 if n == 4096 else 1024
+    hm = {256: 1024, 4096: 64, 65536: 4}[n]
     rng = np.random.default_rng(n + (sign > 0))
     if dist == "normal":
         x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
@@ -65,3 +66,20 @@ def test_tc_fft_parity(lib, torch_tc, restatement, n, dist, sign):
     err = rel_l2(y, ref)
     assert err <= 1e-6, f"rel L2 {err:.3e}"
     assert g.load().fftw_gb300_device_status() == 0
+
+
+def test_tc_multid_columns(lib, torch_tc, restatement):
+    """2D 256 x 256: the column axis runs through the tensor-core kernel with
+    column tiles (strided loads and stores)."""
+    import fftw3_gb300 as g
+    torch = torch_tc
+    shape = [256, 256]
+    rng = np.random.default_rng(77)
+    x = (rng.standard_normal(2 * 65536) + 1j * rng.standard_normal(2 * 65536)).astype(np.complex64)
+    xi = torch.from_numpy(x).cuda()
+    yo = torch.empty_like(xi)
+    p = g.plan_many_dft(shape, 2, xi.data_ptr(), yo.data_ptr(), -1, g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE, "f")
+    assert p.describe().count("tc-split-fp16") == 2
+    p.execute()
+    ref = restatement.c2c(x.astype(np.complex128), shape, -1, "d", nthreads=4)
+    assert rel_l2(yo.cpu().numpy(), ref) <= 1e-6
