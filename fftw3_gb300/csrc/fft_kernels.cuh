@@ -113,11 +113,11 @@ template <typename C> struct io {
      }
 };
 
-/* exp(sign 2 pi i m / N) from the two-level table (four-step twiddle) */
+/* exp(sign 2 pi i m / N) from the two-level table (four-step twiddle);
+ * callers pass m = v * k with v < n2 and k < n1, so m < N. */
 template <typename C> __device__ __forceinline__ C post_twiddle(const gb_pass &P, long long m)
 {
-     m %= P.post_N;
-     long long hi = m / P.post_S, lo = m - hi * P.post_S;
+     const long long hi = m >> P.post_lS, lo = m & (P.post_S - 1);
      C a = __ldg((const C *)P.post_lo + lo), b = __ldg((const C *)P.post_hi + hi);
      C w = cmul(a, b);
      if (P.sign > 0) w.y = -w.y;
@@ -137,8 +137,10 @@ __device__ __forceinline__ void coop_load(const gb_pass &P, const void *in, C *s
      const int total = tb * L;
      for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
           int t, j;
-          if (mode == GB_MOVE_COLS) { t = idx % tb; j = idx / tb; }
-          else { t = idx / L; j = idx - t * L; }
+          if (mode == GB_MOVE_COLS) {
+               if (P.ltb >= 0) { t = idx & (tb - 1); j = idx >> P.ltb; }
+               else { t = idx % tb; j = idx / tb; }
+          } else { t = idx / L; j = idx - t * L; }
           long long v = tl.v0 + t;
           if (v < P.vn[0]) {
                long long base = tl.bi + v * P.vis[0];
@@ -156,8 +158,10 @@ __device__ __forceinline__ void coop_store(const gb_pass &P, void *out, const C 
      const int total = tb * L;
      for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
           int t, j;
-          if (mode == GB_MOVE_COLS) { t = idx % tb; j = idx / tb; }
-          else { t = idx / L; j = idx - t * L; }
+          if (mode == GB_MOVE_COLS) {
+               if (P.ltb >= 0) { t = idx & (tb - 1); j = idx >> P.ltb; }
+               else { t = idx % tb; j = idx / tb; }
+          } else { t = idx / L; j = idx - t * L; }
           long long v = tl.v0 + t;
           if (v < P.vn[0]) {
                long long base = tl.bo + v * P.vos[0];
@@ -631,10 +635,12 @@ template <typename C> __device__ __forceinline__ C *dst_of(const gb_pass &P, con
      if (A.pout) return (C *)A.pout[v];
      return (C *)A.out + tl.bo + v * P.vos[0];
 }
-__device__ __forceinline__ void tile_index(int idx, int tb, int L, int mode, int &t, int &j)
+__device__ __forceinline__ void tile_index(int idx, int tb, int L, int mode, int &t, int &j, int ltb = -1)
 {
-     if (mode == GB_MOVE_COLS) { t = idx % tb; j = idx / tb; }
-     else { t = idx / L; j = idx - t * L; }
+     if (mode == GB_MOVE_COLS) {
+          if (ltb >= 0) { t = idx & (tb - 1); j = idx >> ltb; }
+          else { t = idx % tb; j = idx / tb; }
+     } else { t = idx / L; j = idx - t * L; }
 }
 
 /* One tile of k_gen: load, stages (direction from P.sign), store.  Also the
@@ -660,7 +666,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           const int L = (kind == GB_KIND_RADER) ? n : (kind == GB_KIND_C2R) ? n / 2 + 1 : N;
           for (int idx = threadIdx.x; idx < tb * L; idx += blockDim.x) {
                int t, j;
-               tile_index(idx, tb, L, P.load_mode, t, j);
+               tile_index(idx, tb, L, P.load_mode, t, j, P.ltb);
                if (tile.v0 + t < vn0) {
                     C x;
                     if (kind == GB_KIND_R2C) {
@@ -674,7 +680,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           /* odd n: real sequence as complex with zero imaginary part */
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
                int t, j;
-               tile_index(idx, tb, N, P.load_mode, t, j);
+               tile_index(idx, tb, N, P.load_mode, t, j, P.ltb);
                if (tile.v0 + t < vn0) b0[t * sms + j] = mk<C>(src_of<R>(P, tile, A, t)[j * P.is], 0);
           }
      } else if (kind == GB_KIND_BLUESTEIN) {
@@ -682,7 +688,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           const C *__restrict__ w = (const C *)P.chirp;
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
                int t, j;
-               tile_index(idx, tb, N, P.load_mode, t, j);
+               tile_index(idx, tb, N, P.load_mode, t, j, P.ltb);
                C x = mk<C>(0, 0);
                if (j < n && tile.v0 + t < vn0) x = cmul(src_of<C>(P, tile, A, t)[j * P.is], cconj(__ldg(w + j)));
                b0[t * sms + j] = x;
@@ -750,7 +756,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
      if (kind == GB_KIND_C2C) {
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
                int t, k;
-               tile_index(idx, tb, N, P.store_mode, t, k);
+               tile_index(idx, tb, N, P.store_mode, t, k, P.ltb);
                const long long v = tile.v0 + t;
                if (v < vn0) {
                     C y = res[t * sms + k];
@@ -763,7 +769,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           const C *__restrict__ w = (const C *)P.chirp;
           for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x) {
                int t, k;
-               tile_index(idx, tb, n, P.store_mode, t, k);
+               tile_index(idx, tb, n, P.store_mode, t, k, P.ltb);
                if (tile.v0 + t < vn0)
                     dst_of<C>(P, tile, A, t)[k * P.os] = cmul(res[t * sms + k], cconj(__ldg(w + k)));
           }
@@ -772,7 +778,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           const int *__restrict__ lg = P.perm + N;
           for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x) {
                int t, j;
-               tile_index(idx, tb, n, P.store_mode, t, j);
+               tile_index(idx, tb, n, P.store_mode, t, j, P.ltb);
                if (tile.v0 + t < vn0) {
                     const C y = (j == 0) ? b1[t * sms + N] : cadd(b0[t * sms + N], res[t * sms + __ldg(lg + j - 1)]);
                     dst_of<C>(P, tile, A, t)[j * P.os] = y;
@@ -799,13 +805,13 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           }
           for (int idx = threadIdx.x; idx < tb * nc; idx += blockDim.x) {
                int t, k;
-               tile_index(idx, tb, nc, P.store_mode, t, k);
+               tile_index(idx, tb, nc, P.store_mode, t, k, P.ltb);
                if (tile.v0 + t < vn0) dst_of<C>(P, tile, A, t)[k * P.os] = src[t * sms + k];
           }
      } else if (kind == GB_KIND_C2R) {
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
                int t, j;
-               tile_index(idx, tb, N, P.store_mode, t, j);
+               tile_index(idx, tb, N, P.store_mode, t, j, P.ltb);
                if (tile.v0 + t < vn0) {
                     R *r = dst_of<R>(P, tile, A, t);
                     const C y = res[t * sms + j];

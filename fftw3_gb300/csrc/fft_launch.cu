@@ -81,6 +81,49 @@ __global__ void k_rader_omega(C *dst, const int *gpow, long long p, int sign)
      }
 }
 
+/* Element-wise passes between the FFT passes of multi-pass plans: each CTA
+ * takes a chunk of 4096 elements of one transform.  Tables: tw_half
+ * (exp(-2 pi i k/n), k <= n/2) for the hc2c passes (rdft/ct-hc2c.c), chirp
+ * and chirp_spec for Bluestein (dft/bluestein.c:82-128). */
+template <typename C>
+__global__ void __launch_bounds__(256) k_pointwise(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+{
+     typedef typename real_of<C>::T R;
+     const int M = P.nfft;
+     const int L = (P.pw == GB_PW_HC2C_POST) ? M + 1 : (P.pw == GB_PW_CHIRP_OUT) ? P.n : M;
+     for (long long blk = blockIdx.x; blk < P.nblocks; blk += gridDim.x) {
+          const long long tr = blk / P.pw_chunks;
+          const int k0 = (int)(blk - tr * P.pw_chunks) * 4096;
+          const tile_t tile = tile_of(P, tr);
+          const C *src = (const C *)in + tile.bi + tile.v0 * P.vis[0];
+          C *dst = (C *)out + tile.bo + tile.v0 * P.vos[0];
+          for (int k = k0 + threadIdx.x; k < L && k < k0 + 4096; k += blockDim.x) {
+               C y;
+               if (P.pw == GB_PW_HC2C_POST) {
+                    C a = src[(long long)(k % M) * P.is], b = src[(long long)((M - k) % M) * P.is];
+                    b.y = -b.y;
+                    C ev = cscale(cadd(a, b), (R)0.5), dd = csub(a, b);
+                    C od = mk<C>(dd.y * (R)0.5, -dd.x * (R)0.5);
+                    y = cadd(ev, cmul(__ldg((const C *)P.tw_half + k), od));
+               } else if (P.pw == GB_PW_HC2C_PRE) {
+                    C a = src[(long long)k * P.is], b = src[(long long)(M - k) * P.is];
+                    if (k == 0) { a.y = 0; b.y = 0; }
+                    b.y = -b.y;
+                    C sm = cadd(a, b), d = csub(a, b), w = __ldg((const C *)P.tw_half + k);
+                    C cd = mk<C>(w.x * d.x + w.y * d.y, w.x * d.y - w.y * d.x);
+                    y = mk<C>(sm.x - cd.y, sm.y + cd.x);
+               } else if (P.pw == GB_PW_CHIRP_IN) {
+                    y = (k < P.n) ? cmul(src[(long long)k * P.is], cconj(__ldg((const C *)P.chirp + k))) : mk<C>(0, 0);
+               } else if (P.pw == GB_PW_SPEC_MUL) {
+                    y = cmul(src[(long long)k * P.is], __ldg((const C *)P.chirp_spec + k));
+               } else {
+                    y = cmul(src[(long long)k * P.is], cconj(__ldg((const C *)P.chirp + k)));
+               }
+               dst[(long long)k * P.os] = y;
+          }
+     }
+}
+
 } /* namespace gb */
 
 using namespace gb;
@@ -148,6 +191,8 @@ extern "C" int gb_rader_omega(void *dst, const int *gpow, int prec, long long p,
 
 static const void *pick_kernel(const gb_pass *p)
 {
+     if (p->kind == GB_KIND_POINTWISE)
+          return p->prec == 4 ? (const void *)k_pointwise<float2> : (const void *)k_pointwise<double2>;
      if (p->kind == GB_KIND_COPY)
           return p->prec == 4 ? (const void *)k_copy<float2> : (const void *)k_copy<double2>;
      if (p->variant == GB_VAR_TC) return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_tc_kernel(p->nfft, p->sign) : 0;
@@ -218,7 +263,12 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
       * the launch limits is refused on the host instead of run */
      {
           const char *bad = 0;
-          if (p->kind != GB_KIND_COPY && !p->tw) bad = "twiddle table missing";
+          if (p->kind == GB_KIND_POINTWISE) {
+               if ((p->pw == GB_PW_HC2C_POST || p->pw == GB_PW_HC2C_PRE) && !p->tw_half) bad = "hc2c table missing";
+               else if ((p->pw == GB_PW_CHIRP_IN || p->pw == GB_PW_CHIRP_OUT) && !p->chirp) bad = "chirp missing";
+               else if (p->pw == GB_PW_SPEC_MUL && !p->chirp_spec) bad = "chirp spectrum missing";
+               else if (p->pw_chunks < 1 || p->threads != 256 || p->tb != 1) bad = "bad pointwise launch shape";
+          } else if (p->kind != GB_KIND_COPY && !p->tw) bad = "twiddle table missing";
           else if ((p->kind == GB_KIND_R2C || p->kind == GB_KIND_C2R) && p->n % 2 == 0 && !p->tw_half)
                bad = "half-length twiddle table missing";
           else if (p->kind == GB_KIND_BLUESTEIN && (!p->chirp || !p->chirp_spec)) bad = "chirp tables missing";
@@ -230,6 +280,9 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
                    p->threads != p->tb * (p->nfft / reg_e(p->nfft))) bad = "thread count does not match the tile";
           else if (p->variant == GB_VAR_REG && p->threads > reg_maxthreads(p->nfft)) bad = "tile exceeds the kernel's launch bounds";
           else if (reg_sms(p->nfft) != gb_reg_sms(p->nfft)) bad = "host and device shared-memory layouts disagree";
+          else if (p->ltb >= 0 && (p->ltb > 10 || (1 << p->ltb) != p->tb)) bad = "tile shift does not match the tile";
+          else if (p->post_N && (p->post_lS < 0 || (1LL << p->post_lS) != p->post_S || p->post_S * p->post_S < p->post_N))
+               bad = "four-step twiddle table split is inconsistent";
           else if (p->variant == GB_VAR_REG && p->smem < p->tb * reg_sms(p->nfft) * 2 * p->prec) bad = "shared memory too small for the tile";
           else if (p->variant == GB_VAR_TMA && (p->threads > 256 || p->kind != GB_KIND_C2C || p->is != 1 || p->os != 1 ||
                                                 p->smem < 2 * p->tb * tma_sms(p->nfft) * 2 * p->prec))

@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
            * fast for adjacent columns (four-step tiles, strided axes) */
           for (int i = threadIdx.x; i < TB * N; i += blockDim.x) {
                int t, e;
-               if (P.load_mode == GB_MOVE_COLS) { t = i % TB; e = i / TB; }
+               if (P.load_mode == GB_MOVE_COLS) { t = i & (TB - 1); e = i / TB; }
                else { t = i / N; e = i - t * N; }
                const long long v = tile.v0 + t;
                dat[t * N + e] = (v < P.vn[0]) ? ((const float2 *)in)[tile.bi + v * P.vis[0] + e * P.is]
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
           if (ok && P.store_mode != GB_MOVE_DIRECT) {
                for (int i = threadIdx.x; i < TB * N; i += blockDim.x) {
                     int t, e;
-                    if (P.store_mode == GB_MOVE_COLS) { t = i % TB; e = i / TB; }
+                    if (P.store_mode == GB_MOVE_COLS) { t = i & (TB - 1); e = i / TB; }
                     else { t = i / N; e = i - t * N; }
                     const long long v = tile.v0 + t;
                     if (v < P.vn[0]) ((float2 *)out)[tile.bo + v * P.vos[0] + e * P.os] = dat[t * N + e];

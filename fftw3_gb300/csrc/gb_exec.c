@@ -88,7 +88,7 @@ static int ensure(void **buf, size_t *have, size_t need)
      return 0;
 }
 
-static int run_step(const gb_plan *p, const gb_step *s, char *bufs[3], int esz[3], int real_pairs_ok[3],
+static int run_step(const gb_plan *p, const gb_step *s, char *bufs[4], int esz[4], int real_pairs_ok[4],
                     int direct_host)
 {
      gb_pass P = s->pass;
@@ -145,8 +145,8 @@ int gb_execute(gb_plan *p, void *in, void *out)
      int inplace = (in == out);
      int stage_i, stage_o, direct_host = 0;
      char *din, *dout;
-     char *bufs[3];
-     int esz[3], rp[3];
+     char *bufs[4];
+     int esz[4], rp[4];
      int k;
      cudaStream_t st = (cudaStream_t)p->stream;
 
@@ -207,11 +207,12 @@ int gb_execute(gb_plan *p, void *in, void *out)
           }
      }
 
-     bufs[GB_BUF_IN] = din; bufs[GB_BUF_OUT] = dout; bufs[GB_BUF_SCRATCH] = (char *)p->scratch;
-     esz[GB_BUF_IN] = esin; esz[GB_BUF_OUT] = esout; esz[GB_BUF_SCRATCH] = cs;
+     bufs[GB_BUF_IN] = din; bufs[GB_BUF_OUT] = dout;
+     bufs[GB_BUF_SCRATCH] = (char *)p->scratch; bufs[GB_BUF_SCRATCH2] = (char *)p->scratch2;
+     esz[GB_BUF_IN] = esin; esz[GB_BUF_OUT] = esout; esz[GB_BUF_SCRATCH] = cs; esz[GB_BUF_SCRATCH2] = cs;
      rp[GB_BUF_IN] = ((uintptr_t)din % cs) == 0;
      rp[GB_BUF_OUT] = ((uintptr_t)dout % cs) == 0;
-     rp[GB_BUF_SCRATCH] = 1;
+     rp[GB_BUF_SCRATCH] = rp[GB_BUF_SCRATCH2] = 1;
      /* element size of each buffer: r2c reads reals and writes complex;
       * c2r reads complex (its c2c passes work in place there) and writes
       * reals; scratch is complex */

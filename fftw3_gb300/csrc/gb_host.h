@@ -36,7 +36,7 @@ typedef struct gb_problem {
 } gb_problem;
 
 /* buffer ids a pass reads or writes */
-enum { GB_BUF_IN = 0, GB_BUF_OUT = 1, GB_BUF_SCRATCH = 2 };
+enum { GB_BUF_IN = 0, GB_BUF_OUT = 1, GB_BUF_SCRATCH = 2, GB_BUF_SCRATCH2 = 3 };
 
 typedef struct gb_step {
      gb_pass pass;
@@ -52,8 +52,8 @@ struct gb_plan {
      unsigned flags;
      int nstep;
      gb_step step[GB_MAXPASS];
-     size_t scratch_bytes;
-     void *scratch;             /* device scratch (four-step intermediates) */
+     size_t scratch_bytes, scratch2_bytes;
+     void *scratch, *scratch2;  /* device scratch (intermediates of multi-pass lengths) */
      /* staging buffers for host arrays */
      void *stage_in, *stage_out;
      size_t stage_in_bytes, stage_out_bytes;

@@ -26,6 +26,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <cuda_runtime_api.h>
+#include "fftw3.h"
 #include "gb_host.h"
 
 /* ------------------------------------------------------------ errors */
@@ -149,13 +150,29 @@ const void *gb_table_chirp_spec(int prec, long long n, long long nb, int sign)
           return 0;
      }
      d.n = 1; d.is = 0; d.os = 0;
-     if (config_pass(&P, prec, GB_KIND_C2C, nb, -1, 1, 1, 1, &d, 0, 0) != 0 || pass_tables(&P) != 0) {
-          gb_set_error("chirp spectrum: no forward FFT of length %lld", nb);
-          return 0;
+     if (config_pass(&P, prec, GB_KIND_C2C, nb, -1, 1, 1, 1, &d, 0, 0) == 0 && pass_tables(&P) == 0) {
+          if (gb_launch_pass(&P, p, p, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+               gb_set_error("chirp spectrum failed: %s", gb_last_cuda_error());
+               return 0;
+          }
+          return p;
      }
-     if (gb_launch_pass(&P, p, p, 0) || cudaDeviceSynchronize() != cudaSuccess) {
-          gb_set_error("chirp spectrum failed: %s", gb_last_cuda_error());
-          return 0;
+     {
+          /* convolution longer than one CTA: a forward plan of length nb,
+           * in place on the table */
+          gb_problem prb;
+          gb_plan *q;
+          int rc;
+          memset(&prb, 0, sizeof prb);
+          prb.kind = GB_PROB_DFT; prb.prec = prec; prb.sign = -1; prb.rank = 1;
+          prb.sz[0].n = nb; prb.sz[0].is = 1; prb.sz[0].os = 1;
+          prb.vrank = 1; prb.vec[0].n = 1; prb.vec[0].is = nb; prb.vec[0].os = nb;
+          prb.in = p; prb.out = p;
+          q = gb_mkplan(&prb, FFTW_ESTIMATE);
+          if (!q) return 0;
+          rc = gb_execute(q, p, p);
+          gb_destroy(q);
+          if (rc) return 0;
      }
      return p;
 }
@@ -433,10 +450,16 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
      return 0;
 }
 
-/* Fill the device tables a configured pass needs. */
+/* Fill the device tables a configured pass needs (and the derived shift
+ * fields the kernels use instead of divisions). */
 static int pass_tables(gb_pass *P)
 {
      int prec = P->prec;
+     {
+          int l = 0;
+          while ((1 << l) < P->tb) ++l;
+          P->ltb = ((1 << l) == P->tb) ? l : -1;
+     }
      if (P->kind == GB_KIND_COPY) return 0;
      P->tw = gb_table_twiddle(prec, P->nfft, P->nfft, 1);
      if (!P->tw) return -1;
@@ -456,8 +479,10 @@ static int pass_tables(gb_pass *P)
      }
      if (P->post_N) {
           long long S = 1;
-          while (S * S < P->post_N) S <<= 1;
+          int l = 0;
+          while (S * S < P->post_N) { S <<= 1; ++l; }
           P->post_S = S;
+          P->post_lS = l;
           P->post_lo = gb_table_twiddle(prec, P->post_N, S, 1);
           P->post_hi = gb_table_twiddle(prec, P->post_N, (P->post_N + S - 1) / S, S);
           if (!P->post_lo || !P->post_hi) return -1;
@@ -529,8 +554,74 @@ static int use_rader(int prec, long long n, const gb_wisdom_entry *w)
 /* Adds the steps of one batched 1D transform: length n along (is, os), batch
  * dims v (count nv), from buffer src to dst.  Chooses single-CTA kernels,
  * the in-CTA Bluestein, or the two-pass four-step decomposition. */
+static void need_scratch(gb_plan *p, int buf, size_t bytes)
+{
+     if (buf == GB_BUF_SCRATCH && bytes > p->scratch_bytes) p->scratch_bytes = bytes;
+     if (buf == GB_BUF_SCRATCH2 && bytes > p->scratch2_bytes) p->scratch2_bytes = bytes;
+}
+
+/* An element-wise pass over nv vector dims (in/out strides), length L per
+ * transform as the mode defines it. */
+static gb_step *add_pointwise(builder *b, int pw, long long n, long long nfft, int sign, long long is, long long os,
+                              int nv, const gb_dim *v, int src, int dst)
+{
+     gb_plan *p = b->p;
+     int prec = p->prb.prec, i;
+     long long L = (pw == GB_PW_HC2C_POST) ? nfft + 1 : (pw == GB_PW_CHIRP_OUT) ? n : nfft;
+     gb_step *s = new_step(b);
+     gb_pass *P;
+     if (!s) return 0;
+     if (nv > GB_MAXV) { gb_set_error("element-wise pass with too many vector dims"); b->err = 1; return 0; }
+     s->src = src; s->dst = dst;
+     P = &s->pass;
+     memset(P, 0, sizeof *P);
+     P->kind = GB_KIND_POINTWISE; P->pw = pw; P->prec = prec; P->sign = sign;
+     P->n = (int)n; P->nfft = (int)nfft; P->variant = GB_VAR_GEN;
+     P->tb = 1; P->threads = 256; P->smem = 0;
+     P->is = is; P->os = os;
+     P->nv = nv > 0 ? nv : 1;
+     if (nv == 0) { P->vn[0] = 1; P->vis[0] = 0; P->vos[0] = 0; }
+     for (i = 0; i < nv; ++i) { P->vn[i] = v[i].n; P->vis[i] = v[i].is; P->vos[i] = v[i].os; }
+     P->ntiles0 = P->vn[0];
+     P->pw_chunks = (L + 4095) / 4096;
+     P->nblocks = P->pw_chunks;
+     for (i = 0; i < P->nv; ++i) P->nblocks *= P->vn[i];
+     if (pw == GB_PW_HC2C_POST || pw == GB_PW_HC2C_PRE) {
+          P->tw_half = gb_table_twiddle(prec, 2 * nfft, nfft + 1, 1);
+          if (!P->tw_half) { b->err = 1; return 0; }
+     } else {
+          P->chirp = gb_table_chirp(prec, n, sign);
+          if (pw == GB_PW_SPEC_MUL) P->chirp_spec = gb_table_chirp_spec(prec, n, nfft, sign);
+          if (!P->chirp || (pw == GB_PW_SPEC_MUL && !P->chirp_spec)) { b->err = 1; return 0; }
+     }
+     return s;
+}
+
+static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is, long long os,
+                       int nv, const gb_dim *v_in, int src, int dst, int mid);
+
 static void add_1d(builder *b, int kind, long long n, int sign, long long is, long long os,
                    int nv, const gb_dim *v_in, int src, int dst)
+{
+     add_1d_mid(b, kind, n, sign, is, os, nv, v_in, src, dst, GB_BUF_SCRATCH);
+}
+
+/* dense layout of a batch: transform length L, vector dims v (outermost
+ * first) re-strided contiguously, keeping the caller's strides on one side */
+static void dense_dims(const gb_dim *v, int nv, long long L, gb_dim *out, int keep_in)
+{
+     long long d = L;
+     int i;
+     for (i = nv - 1; i >= 0; --i) {
+          out[i].n = v[i].n;
+          out[i].is = keep_in ? v[i].is : d;
+          out[i].os = keep_in ? d : v[i].os;
+          d *= v[i].n;
+     }
+}
+
+static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is, long long os,
+                       int nv, const gb_dim *v_in, int src, int dst, int mid)
 {
      gb_plan *p = b->p;
      int prec = p->prb.prec, rc, i;
@@ -613,9 +704,30 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
                return;
           }
           --p->nstep;
-          gb_set_error("length %lld: prime factor too large for a one-CTA Bluestein convolution", n);
-          b->err = 1;
-          return;
+          {
+               /* multi-pass Bluestein: chirp multiply into scratch (zero-
+                * padded to nb), FFT(nb), spectrum multiply, inverse FFT(nb),
+                * chirp multiply into dst (dft/bluestein.c:82-128) */
+               long long nb = 1, hm = howmany;
+               gb_dim vin[GB_MAXRANK + 2], vmid[GB_MAXRANK + 2], vout[GB_MAXRANK + 2];
+               while (nb < 2 * n - 1) nb <<= 1;
+               if (src == GB_BUF_SCRATCH || dst == GB_BUF_SCRATCH) {
+                    gb_set_error("length %lld: nested multi-pass convolution", n);
+                    b->err = 1;
+                    return;
+               }
+               dense_dims(v, nvk, nb, vin, 1);     /* caller's input strides -> dense nb */
+               dense_dims(v, nvk, nb, vmid, 0);
+               for (i = 0; i < nvk; ++i) vmid[i].is = vmid[i].os = vin[i].os;
+               dense_dims(v, nvk, nb, vout, 0);    /* dense nb -> caller's output strides */
+               need_scratch(p, GB_BUF_SCRATCH, (size_t)(nb * hm) * csize(prec));
+               add_pointwise(b, GB_PW_CHIRP_IN, n, nb, sign, is, 1, nvk, vin, src, GB_BUF_SCRATCH);
+               add_1d_mid(b, GB_KIND_C2C, nb, -1, 1, 1, nvk, vmid, GB_BUF_SCRATCH, GB_BUF_SCRATCH, GB_BUF_SCRATCH2);
+               add_pointwise(b, GB_PW_SPEC_MUL, n, nb, sign, 1, 1, nvk, vmid, GB_BUF_SCRATCH, GB_BUF_SCRATCH);
+               add_1d_mid(b, GB_KIND_C2C, nb, 1, 1, 1, nvk, vmid, GB_BUF_SCRATCH, GB_BUF_SCRATCH, GB_BUF_SCRATCH2);
+               add_pointwise(b, GB_PW_CHIRP_OUT, n, nb, sign, 1, os, nvk, vout, GB_BUF_SCRATCH, dst);
+               return;
+          }
      }
 
      if (kind == GB_KIND_C2C && rc == 1) {
@@ -643,7 +755,7 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
           n1 = best; n2 = n / n1;
           if (w && w->n1 > 0 && n % w->n1 == 0) { n1 = w->n1; n2 = n / n1; }
           sz = n * howmany;
-          if ((size_t)sz * csize(prec) > p->scratch_bytes) p->scratch_bytes = (size_t)sz * csize(prec);
+          need_scratch(p, mid, (size_t)sz * csize(prec));
           /* pass A: transform over n1 with element stride n2*is; dim0 = n2 */
           va[na].n = n2; va[na].is = is; va[na].os = n1; ++na;
           {
@@ -655,7 +767,7 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
           }
           s = new_step(b);
           if (!s) return;
-          s->src = src; s->dst = GB_BUF_SCRATCH;
+          s->src = src; s->dst = mid;
           if (na > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
           /* dim 0 stays n2: the twiddle W_n^(n2 k1) indexes it */
           r1 = config_pass(&s->pass, prec, GB_KIND_C2C, n1, sign, n2 * is, 1, na, va, 0, 1);
@@ -674,12 +786,48 @@ static void add_1d(builder *b, int kind, long long n, int sign, long long is, lo
           }
           s = new_step(b);
           if (!s) return;
-          s->src = GB_BUF_SCRATCH; s->dst = dst;
+          s->src = mid; s->dst = dst;
           if (nb > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
           r2 = config_pass(&s->pass, prec, GB_KIND_C2C, n2, sign, n1, n1 * os, nb, vb, 0, 1);
           if (r2 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
           if (r2 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass B config failed"); b->err = 1; return; }
           count_ops(p, &s->pass, howmany * n1);
+          return;
+     }
+     if ((kind == GB_KIND_R2C || kind == GB_KIND_C2R) && rc == 1 && n % 2 == 0) {
+          /* even length beyond one CTA: the half-length complex FFT runs as
+           * its own (multi-pass) c2c on the real array viewed as pairs, and
+           * the hc2c post-pass (r2c) or pre-pass (c2r) as an element-wise
+           * pass through scratch (rdft/ct-hc2c.c:31-83) */
+          long long M = n / 2;
+          gb_dim vp[GB_MAXRANK + 2], vd[GB_MAXRANK + 2];
+          int ok = 1;
+          if (kind == GB_KIND_R2C) {
+               if (is != 1) ok = 0;
+               for (i = 0; i < nvk; ++i) if (v[i].is % 2) ok = 0;
+          } else {
+               if (os != 1) ok = 0;
+               for (i = 0; i < nvk; ++i) if (v[i].os % 2) ok = 0;
+          }
+          if (!ok || src == GB_BUF_SCRATCH || dst == GB_BUF_SCRATCH) {
+               gb_set_error("real length %lld beyond one CTA needs unit real stride", n);
+               b->err = 1;
+               return;
+          }
+          need_scratch(p, GB_BUF_SCRATCH, (size_t)(M * howmany) * csize(prec));
+          if (kind == GB_KIND_R2C) {
+               for (i = 0; i < nvk; ++i) { vp[i].n = v[i].n; vp[i].is = v[i].is / 2; }
+               dense_dims(v, nvk, M, vd, 0);
+               for (i = 0; i < nvk; ++i) vp[i].os = vd[i].is;      /* dense M in scratch */
+               add_1d_mid(b, GB_KIND_C2C, M, -1, 1, 1, nvk, vp, src, GB_BUF_SCRATCH, GB_BUF_SCRATCH2);
+               for (i = 0; i < nvk; ++i) { vd[i].is = vp[i].os; vd[i].os = v[i].os; }
+               add_pointwise(b, GB_PW_HC2C_POST, n, M, -1, 1, os, nvk, vd, GB_BUF_SCRATCH, dst);
+          } else {
+               dense_dims(v, nvk, M, vd, 1);                      /* caller's input -> dense M */
+               add_pointwise(b, GB_PW_HC2C_PRE, n, M, 1, is, 1, nvk, vd, src, GB_BUF_SCRATCH);
+               for (i = 0; i < nvk; ++i) { vp[i].n = v[i].n; vp[i].is = vd[i].os; vp[i].os = v[i].os / 2; }
+               add_1d_mid(b, GB_KIND_C2C, M, 1, 1, 1, nvk, vp, GB_BUF_SCRATCH, dst, GB_BUF_SCRATCH2);
+          }
           return;
      }
      gb_set_error("length %lld is not supported for this transform kind", n);
@@ -694,7 +842,7 @@ static void describe(gb_plan *p)
                      kn[p->prb.kind], p->prb.prec == 4 ? "f32" : "f64");
      for (i = 0; i < p->nstep && off < (int)sizeof p->desc - 64; ++i) {
           const gb_pass *P = &p->step[i].pass;
-          static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy", "rader"};
+          static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy", "rader", "pointwise"};
           static const char *mv[] = {"direct", "rows", "cols"};
           off += snprintf(p->desc + off, sizeof p->desc - off,
                           "\n  (pass %s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
@@ -763,6 +911,13 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
                add_1d(&b, GB_KIND_C2C, prb->sz[a].n, -1, prb->sz[a].os, prb->sz[a].os, nv, v, GB_BUF_OUT, GB_BUF_OUT);
           }
      } else {
+          /* multi-dimensional c2r works in place on its input; like the
+           * reference, no input-preserving algorithm exists for it */
+          if (r > 1 && (flags & FFTW_PRESERVE_INPUT)) {
+               gb_set_error("multi-dimensional c2r cannot preserve its input");
+               free(p);
+               return 0;
+          }
           /* c2r: c2c backward over the leading axes in place on the input
            * (the reference destroys the input here, api/plan-many-dft-c2r.c:41-42),
            * then the last axis c2r from in to out */
@@ -788,6 +943,14 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
           free(p);
           return 0;
      }
+     if (p->scratch2_bytes && !gb_dry) {
+          if (cudaMalloc(&p->scratch2, p->scratch2_bytes) != cudaSuccess) {
+               cudaGetLastError();
+               gb_set_error("cudaMalloc(%zu) for plan scratch failed", p->scratch2_bytes);
+               free(p);
+               return 0;
+          }
+     }
      if (p->scratch_bytes && !gb_dry) {
           if (cudaMalloc(&p->scratch, p->scratch_bytes) != cudaSuccess) {
                cudaGetLastError();
@@ -806,6 +969,7 @@ void gb_destroy(gb_plan *p)
      if (!p) return;
      if (!gb_dry) {
           if (p->scratch) cudaFree(p->scratch);
+          if (p->scratch2) cudaFree(p->scratch2);
           if (p->stage_in) cudaFree(p->stage_in);
           if (p->stage_out) cudaFree(p->stage_out);
      }

@@ -83,6 +83,7 @@ static int item_pass(gb_pass *P, int prec, int kind, long long n, int sign, long
      P->nrad = gb_factor_radices(P->nfft, P->rad);
      if (P->nrad < 0) return -1;
      if (gb_pass_tables(P)) return -1;
+     if (P->ltb >= 0 && (1 << P->ltb) != P->tb) return -1;
      return 0;
 }
 

@@ -27,7 +27,17 @@ enum gb_kind {
      GB_KIND_C2R = 2,       /* complex n/2+1 -> real n */
      GB_KIND_BLUESTEIN = 3, /* complex n -> complex n through a chirp convolution of length nfft */
      GB_KIND_COPY = 4,      /* rank-0 problem: element copy */
-     GB_KIND_RADER = 5      /* prime n: cyclic convolution of length n-1 through the generator permutation */
+     GB_KIND_RADER = 5,     /* prime n: cyclic convolution of length n-1 through the generator permutation */
+     GB_KIND_POINTWISE = 6  /* element-wise pass between multi-pass stages (field pw) */
+};
+
+/* Element-wise passes of multi-pass plans (lengths beyond one CTA). */
+enum gb_pw {
+     GB_PW_HC2C_POST = 0,   /* r2c: Z (n/2 complex) -> X (n/2+1): hc2c post-pass */
+     GB_PW_HC2C_PRE = 1,    /* c2r: X (n/2+1) -> Z' (n/2): hc2c pre-pass */
+     GB_PW_CHIRP_IN = 2,    /* Bluestein: x conj(w), zero-padded to nfft */
+     GB_PW_SPEC_MUL = 3,    /* Bluestein: multiply by the chirp spectrum, in place */
+     GB_PW_CHIRP_OUT = 4    /* Bluestein: conv conj(w), first n */
 };
 
 /* How the transform is computed inside one CTA. */
@@ -58,6 +68,8 @@ typedef struct gb_pass {
      int load_mode;     /* enum gb_move */
      int store_mode;    /* enum gb_move */
      int real_pairs;    /* r2c input / c2r output: stride 1 and 8-/16-byte aligned pairs */
+     int pw;            /* GB_KIND_POINTWISE: enum gb_pw */
+     long long pw_chunks; /* GB_KIND_POINTWISE: CTAs per transform */
      long long is, os;  /* element stride along the transform (complex or real elements) */
      int nv;            /* number of vector dimensions */
      long long vn[GB_MAXV], vis[GB_MAXV], vos[GB_MAXV];
@@ -72,7 +84,9 @@ typedef struct gb_pass {
       * vector dimension 0 is v by exp(sign 2 pi i v k / post_N).  The
       * factor is read from two tables: post_lo[m % post_S] * post_hi[m / post_S]. */
      long long post_N;
-     long long post_S;
+     long long post_S;    /* power of two; post_lS = log2(post_S) */
+     int post_lS;
+     int ltb;             /* log2(tb) when tb is a power of two, else -1 */
      const void *post_lo;
      const void *post_hi;
      /* Bluestein: chirp w[k] (k < n) and the spectrum of the padded chirp / nfft */

@@ -7,6 +7,8 @@ reference algorithms run in long double (double results) / double (float
 results).  Bounds: relative L2 error <= 1e-6 for float, <= 1e-14 for double,
 as the accuracy target of this path states.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -331,3 +333,62 @@ def test_c2c_rader(lib, torch_cuda, restatement, n, prec, monkeypatch):
         ref = np.concatenate([restatement.dft_method(x[i * n:(i + 1) * n].astype(np.clongdouble), sign, 3, "l")
                               for i in range(hm)])
         assert rel_l2(y, ref) <= TOL[prec]
+
+
+LARGE_BLUESTEIN = [(10007, "f"), (20011, "f"), (2 * 10007, "f"), (5003, "d"), (8191, "d")]
+
+
+@pytest.mark.parametrize("n,prec", LARGE_BLUESTEIN)
+def test_c2c_bluestein_multipass(lib, torch_cuda, restatement, n, prec):
+    """Lengths whose convolution exceeds one CTA: chirp multiply, FFT(nb) in
+    two passes, spectrum multiply, inverse FFT(nb), chirp multiply."""
+    rng = np.random.default_rng(n + 6)
+    hm = 2
+    x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
+    for sign in (-1, 1):
+        y, p = run_c2c(torch_cuda, x, [n], sign, prec, hm)
+        assert "pointwise" in p.describe()
+        assert rel_l2(y, oracle_c2c(restatement, x, [n], sign, prec)) <= TOL[prec]
+
+
+LARGE_REAL = [(1 << 16, "f"), (40000, "f"), (1 << 20, "f"), (1 << 15, "d"), (60000, "d")]
+
+
+@pytest.mark.parametrize("n,prec", LARGE_REAL)
+def test_r2c_c2r_multipass(lib, torch_cuda, restatement, n, prec):
+    """Even real lengths beyond one CTA: half-length c2c over the real array
+    as pairs plus an element-wise hc2c pass."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    rng = np.random.default_rng(n + 7)
+    hm = 2
+    nc = n // 2 + 1
+    x = rng.standard_normal(n * hm)
+    xi = _dev(torch, x.astype(RT[prec]))
+    yo = torch.empty(hm * nc, dtype=torch.complex64 if prec == "f" else torch.complex128, device="cuda")
+    p = g.plan_many_dft_r2c([n], hm, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE, prec)
+    p.execute()
+    op = "l" if prec == "d" else "d"
+    ref = restatement.r2c(x.astype(np.longdouble if prec == "d" else np.float64), [n], op, nthreads=4)
+    assert rel_l2(_host(yo), ref) <= TOL[prec]
+    z = rng.standard_normal(nc * hm) + 1j * rng.standard_normal(nc * hm)
+    zi = _dev(torch, z.astype(CT[prec]))
+    ro = torch.empty(hm * n, dtype=torch.float32 if prec == "f" else torch.float64, device="cuda")
+    q = g.plan_many_dft_c2r([n], hm, zi.data_ptr(), ro.data_ptr(), g.FFTW_ESTIMATE, prec)
+    q.execute()
+    ref = restatement.c2r(z.astype(np.clongdouble if prec == "d" else np.complex128), [n], op, nthreads=4)
+    assert rel_l2(_host(ro), ref) <= TOL[prec]
+
+
+def test_c2r_multid_preserve_input_is_null(lib):
+    """Like the reference, a multi-dimensional c2r cannot preserve its input."""
+    import fftw3_gb300 as g
+    lib_ = g.load()
+    n = (ctypes.c_int * 2)(16, 16)
+    p = lib_.fftwf_plan_many_dft_c2r(2, n, 1, 1 << 20, None, 1, 16 * 9, 1 << 21, None, 1, 256,
+                                     g.FFTW_ESTIMATE | g.FFTW_PRESERVE_INPUT)
+    assert not p
+    q = lib_.fftwf_plan_many_dft_c2r(1, n, 1, 1 << 20, None, 1, 9, 1 << 21, None, 1, 16,
+                                     g.FFTW_ESTIMATE | g.FFTW_PRESERVE_INPUT)
+    assert q
+    lib_.fftwf_destroy_plan(q)
