@@ -462,8 +462,8 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
 }
 
 /* ======================================================================
- * k_reg_tma: persistent variant of k_reg for unit-stride c2c batches whose
- * transforms start on 16-byte boundaries.  Each CTA walks its tiles with a
+ * k_reg_tma: persistent variant of k_reg for unit-stride c2c and r2c
+ * batches whose transforms start on 16-byte boundaries.  Each CTA walks its tiles with a
  * two-slot pipeline: while the tile in one shared-memory slot is being
  * transformed, the TMA engine copies the next tile into the other slot
  * (cp.async.bulk, completion tracked by an mbarrier), so HBM reads overlap
@@ -472,24 +472,35 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
 
 __host__ __device__ constexpr int tma_sms(int nfft) { return reg_sms(nfft); }
 
-template <typename C, int N>
+/* Element offsets of r2c inputs count reals; the slot receives the real
+ * pairs, i.e. the same N * sizeof(C) bytes as a complex transform. */
+template <typename C, int N, int KIND>
 __device__ __forceinline__ void tma_issue(const gb_pass &P, const void *in, long long blk, C *dst,
                                           unsigned long long *bar)
 {
+     typedef typename real_of<C>::T R;
      const tile_t tl = tile_of(P, blk);
      const long long rem = P.vn[0] - tl.v0;
      const int ntr = rem < P.tb ? (int)rem : P.tb;
      const unsigned bytes = (unsigned)(N * sizeof(C));
      mbar_expect_tx(bar, bytes * (unsigned)ntr);
-     for (int t = 0; t < ntr; ++t)
-          bulk_g2s(dst + t * tma_sms(N), (const C *)in + tl.bi + (tl.v0 + t) * P.vis[0], bytes, bar);
+     for (int t = 0; t < ntr; ++t) {
+          const long long off = tl.bi + (tl.v0 + t) * P.vis[0];
+          const void *src = (KIND == GB_KIND_R2C) ? (const void *)((const R *)in + off) : (const void *)((const C *)in + off);
+          bulk_g2s(dst + t * tma_sms(N), src, bytes, bar);
+     }
 }
+
+/* threads per CTA of k_reg_tma: 256, or one transform's T when larger */
+__host__ __device__ constexpr int tma_threads(int nfft) { return (nfft / reg_e(nfft)) > 256 ? (nfft / reg_e(nfft)) : 256; }
 
 #define GB_WAIT_NS 2000000000ull   /* bound on any wait for a copy: 2 s */
 
-template <typename C, int LOGN, int DIR>
-__global__ void __launch_bounds__(256, 3) k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+template <typename C, int LOGN, int DIR, int KIND>
+__global__ void __launch_bounds__(tma_threads(1 << LOGN), tma_threads(1 << LOGN) > 256 ? 1 : 3)
+k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
 {
+     typedef typename real_of<C>::T R;
      constexpr int N = 1 << LOGN;
      constexpr int E = reg_e(N);
      constexpr int T = N / E;
@@ -510,7 +521,7 @@ __global__ void __launch_bounds__(256, 3) k_reg_tma(const gb_pass P, const void 
      __syncthreads();
      const long long stride = gridDim.x;
      long long blk = blockIdx.x;
-     if (threadIdx.x == 0 && blk < P.nblocks) tma_issue<C, N>(P, in, blk, buf0, &bar[0]);
+     if (threadIdx.x == 0 && blk < P.nblocks) tma_issue<C, N, KIND>(P, in, blk, buf0, &bar[0]);
      unsigned parity = 0;   /* bit b: parity of the next phase of bar[b] */
 
      for (int it = 0; blk < P.nblocks; blk += stride, ++it) {
@@ -520,7 +531,7 @@ __global__ void __launch_bounds__(256, 3) k_reg_tma(const gb_pass P, const void 
           const bool issued = nxt < P.nblocks;
           if (threadIdx.x == 0 && issued) {
                fence_proxy_async_smem();
-               tma_issue<C, N>(P, in, nxt, b ? buf0 : buf1, &bar[b ^ 1]);
+               tma_issue<C, N, KIND>(P, in, nxt, b ? buf0 : buf1, &bar[b ^ 1]);
           }
           const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u, GB_WAIT_NS);
           if (!__syncthreads_and(ok)) {
@@ -543,15 +554,41 @@ __global__ void __launch_bounds__(256, 3) k_reg_tma(const gb_pass P, const void 
           for (int e = 0; e < E; ++e) x[e] = smt[tid + T * e];
           __syncthreads();
           reg_stages<C, N, DIR, 1>(x, tid, smt, tw);
-          if (P.post_N) {
+          if constexpr (KIND == GB_KIND_R2C) {
+               /* hc2c post-pass (rdft/ct-hc2c.c:197-210):
+                * X[k] = (Z[k] + conj Z[N-k])/2 + W_2N^k (Z[k] - conj Z[N-k])/(2i) */
 #pragma unroll
-               for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
-          }
-          if (valid) {
-               /* unit output stride (checked at launch): constant offsets */
-               C *o = (C *)out + bo + tid;
+               for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
+               __syncthreads();
+               const C *__restrict__ th = (const C *)P.tw_half;
 #pragma unroll
-               for (int e = 0; e < E; ++e) o[T * e] = x[e];
+               for (int e = 0; e < E; ++e) {
+                    const int k = tid + T * e;
+                    C a = smt[pad_for(N, k)], bq = smt[pad_for(N, (N - k) & (N - 1))];
+                    bq.y = -bq.y;
+                    const C ev = cscale(cadd(a, bq), (R)0.5), dd = csub(a, bq);
+                    const C od = mk<C>(dd.y * (R)0.5, -dd.x * (R)0.5);
+                    x[e] = cadd(ev, cmul(__ldg(th + k), od));
+               }
+               const C z0 = smt[pad_for(N, 0)];
+               if (valid) {
+                    C *o = (C *)out + bo + tid;
+#pragma unroll
+                    for (int e = 0; e < E; ++e) o[T * e] = x[e];
+                    if (tid == 0) o[N] = mk<C>(z0.x - z0.y, 0);
+               }
+               __syncthreads();   /* the slot is the next bulk copy's target */
+          } else {
+               if (P.post_N) {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
+               }
+               if (valid) {
+                    /* unit output stride (checked at launch): constant offsets */
+                    C *o = (C *)out + bo + tid;
+#pragma unroll
+                    for (int e = 0; e < E; ++e) o[T * e] = x[e];
+               }
           }
      }
 }

@@ -15,8 +15,8 @@
 
 extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir);
 extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
-extern "C" const void *gb_tma_kernel_f(int logn, int dir);
-extern "C" const void *gb_tma_kernel_d(int logn, int dir);
+extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir);
+extern "C" const void *gb_tma_kernel_d(int logn, int kind, int dir);
 extern "C" const void *gb_tc_kernel(int nfft, int dir);
 extern "C" int gb_tc_smem(int nfft);
 
@@ -200,7 +200,9 @@ static const void *pick_kernel(const gb_pass *p)
           int logn = 0;
           while ((1 << logn) < p->nfft) ++logn;
           if (p->variant == GB_VAR_TMA)
-               return (p->kind == GB_KIND_C2C) ? (p->prec == 4 ? gb_tma_kernel_f(logn, p->sign) : gb_tma_kernel_d(logn, p->sign)) : 0;
+               return (p->kind == GB_KIND_C2C || p->kind == GB_KIND_R2C)
+                           ? (p->prec == 4 ? gb_tma_kernel_f(logn, p->kind, p->sign) : gb_tma_kernel_d(logn, p->kind, p->sign))
+                           : 0;
           return p->prec == 4 ? gb_reg_kernel_f(logn, p->kind, p->sign) : gb_reg_kernel_d(logn, p->kind, p->sign);
      }
      return p->prec == 4 ? (const void *)k_gen<float2> : (const void *)k_gen<double2>;
@@ -284,9 +286,11 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->post_N && (p->post_lS < 0 || (1LL << p->post_lS) != p->post_S || p->post_S * p->post_S < p->post_N))
                bad = "four-step twiddle table split is inconsistent";
           else if (p->variant == GB_VAR_REG && p->smem < p->tb * reg_sms(p->nfft) * 2 * p->prec) bad = "shared memory too small for the tile";
-          else if (p->variant == GB_VAR_TMA && (p->threads > 256 || p->kind != GB_KIND_C2C || p->is != 1 || p->os != 1 ||
+          else if (p->variant == GB_VAR_TMA && (p->threads > tma_threads(p->nfft) || p->is != 1 || p->os != 1 ||
+                                                (p->kind != GB_KIND_C2C && p->kind != GB_KIND_R2C) ||
+                                                (p->kind == GB_KIND_R2C && p->n != 2 * p->nfft) ||
                                                 p->smem < 2 * p->tb * tma_sms(p->nfft) * 2 * p->prec))
-               bad = "persistent bulk-copy pass needs unit-stride c2c in and out, <= 256 threads and two smem slots";
+               bad = "persistent bulk-copy pass needs unit-stride c2c/r2c in and out and two smem slots";
           else if (p->variant == GB_VAR_TMA && ((uintptr_t)in % 16 != 0)) bad = "bulk copies need a 16-byte aligned input";
           else if (p->variant == GB_VAR_TC && (p->prec != 4 || (p->nfft != 256 && p->nfft != 4096) ||
                                                p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||

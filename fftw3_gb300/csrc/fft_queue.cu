@@ -29,8 +29,8 @@ __device__ __forceinline__ void red_release_add(int *p, int v)
      asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-template <typename C>
-__global__ void __launch_bounds__(512) k_queue(const gb_qitem *__restrict__ items, int nitems, int *head,
+template <typename C, int THREADS>
+__global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_queue(const gb_qitem *__restrict__ items, int nitems, int *head,
                                                 int *ctrs, int *status)
 {
      extern __shared__ __align__(16) unsigned char gb_smem[];
@@ -85,15 +85,18 @@ using namespace gb;
 
 extern "C" int *gb_device_status_ptr(void);
 
-static const void *queue_kernel(int prec)
+/* two instantiations: 256 threads for the small-tile queue (three CTAs per
+ * SM), 512 threads for the queue of items that need the largest tiles */
+static const void *queue_kernel(int prec, int threads)
 {
-     return prec == 4 ? (const void *)k_queue<float2> : (const void *)k_queue<double2>;
+     if (threads <= 256) return prec == 4 ? (const void *)k_queue<float2, 256> : (const void *)k_queue<double2, 256>;
+     return prec == 4 ? (const void *)k_queue<float2, 512> : (const void *)k_queue<double2, 512>;
 }
 
 /* CTAs of the queue kernel that fit on the device at once. */
 extern "C" int gb_queue_grid(int prec, int threads, int smem)
 {
-     const void *fn = queue_kernel(prec);
+     const void *fn = queue_kernel(prec, threads);
      int dev = 0, sms = 0, per = 0;
      if (smem > 48 * 1024 && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
           return -1;
@@ -107,7 +110,7 @@ extern "C" int gb_queue_grid(int prec, int threads, int smem)
 extern "C" int gb_launch_queue(const gb_qitem *items, int nitems, int *head, int *ctrs, int prec, int threads,
                                int smem, int grid, void *stream)
 {
-     const void *fn = queue_kernel(prec);
+     const void *fn = queue_kernel(prec, threads);
      int *status = gb_device_status_ptr();
      void *args[5] = {(void *)&items, (void *)&nitems, (void *)&head, (void *)&ctrs, (void *)&status};
      if (smem > 48 * 1024 && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)

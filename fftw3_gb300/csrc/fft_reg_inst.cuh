@@ -17,19 +17,22 @@ static const void *reg_pick(int kind, int dir)
 }
 
 template <int L>
-static const void *tma_pick(int dir)
+static const void *tma_pick(int kind, int dir)
 {
-     if constexpr (L < 6 || L > 12) return 0;
-     else return dir < 0 ? (const void *)k_reg_tma<GB_CT, L, -1> : (const void *)k_reg_tma<GB_CT, L, 1>;
+     if constexpr (L < 6 || L > 13) return 0;
+     else {
+          if (kind == GB_KIND_R2C) return (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_R2C>;
+          return dir < 0 ? (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_C2C> : (const void *)k_reg_tma<GB_CT, L, 1, GB_KIND_C2C>;
+     }
 }
 
 template <int L>
-static const void *tma_lookup(int logn, int dir)
+static const void *tma_lookup(int logn, int kind, int dir)
 {
-     if constexpr (L > 12) return 0;
+     if constexpr (L > 13) return 0;
      else {
-          if (logn == L) return tma_pick<L>(dir);
-          return tma_lookup<L + 1>(logn, dir);
+          if (logn == L) return tma_pick<L>(kind, dir);
+          return tma_lookup<L + 1>(logn, kind, dir);
      }
 }
 

@@ -331,6 +331,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
      long long nfft;
      int half = (kind == GB_KIND_R2C || kind == GB_KIND_C2R) && (n % 2 == 0);
      memset(P, 0, sizeof *P);
+     P->ltb = -1;
      if (nv > GB_MAXV) nv = GB_MAXV;
      for (i = 0; i < nv; ++i) v[i] = v_in[i];
      if (nv == 0) { v[0].n = 1; v[0].is = 0; v[0].os = 0; nv = 1; }
@@ -397,12 +398,13 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                P->store_mode = GB_MOVE_ROWS;
           /* unit-stride c2c with 16-byte aligned transform starts: persistent
            * CTAs fed by bulk async copies (k_reg_tma) */
-          if (kind == GB_KIND_C2C && is == 1 && os == 1 && nfft >= 64 && nfft <= 4096 && tb_hint == 0 && !cfg_no_tma &&
-              !getenv("FFTW_GB300_NO_TMA")) {
+          if ((kind == GB_KIND_C2C || kind == GB_KIND_R2C) && is == 1 && os == 1 && nfft >= 64 && nfft <= 8192 &&
+              tb_hint == 0 && !cfg_no_tma && !getenv("FFTW_GB300_NO_TMA")) {
                int ok = 1, tbt = 256 / T;
                long long sm2;
+               const int ein = kind == GB_KIND_R2C ? prec : csize(prec);   /* bytes per input element */
                for (i = 0; i < nv; ++i)
-                    if ((P->vis[i] * csize(prec)) % 16) ok = 0;
+                    if ((P->vis[i] * ein) % 16) ok = 0;
                if (tbt < 1) tbt = 1;
                while (tbt > 1 && (tbt >> 1) >= v[0].n) tbt >>= 1;
                sm2 = 2LL * tbt * tma_sms((int)nfft) * csize(prec);
@@ -575,6 +577,7 @@ static gb_step *add_pointwise(builder *b, int pw, long long n, long long nfft, i
      s->src = src; s->dst = dst;
      P = &s->pass;
      memset(P, 0, sizeof *P);
+     P->ltb = -1;
      P->kind = GB_KIND_POINTWISE; P->pw = pw; P->prec = prec; P->sign = sign;
      P->n = (int)n; P->nfft = (int)nfft; P->variant = GB_VAR_GEN;
      P->tb = 1; P->threads = 256; P->smem = 0;

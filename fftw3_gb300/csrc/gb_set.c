@@ -6,7 +6,7 @@
  * one plan after another (each a tree of solver applies, api/execute.c:23-27).
  * Here the set compiles to queue items (gb_qitem):
  *   - a transform that fits one CTA's shared memory (2 buffers of nfft+1
- *     complex, nfft <= 8192 single / 4096 double) is a "single"; singles of
+ *     complex, nfft <= 4096 single / 2048 double) is a "single"; singles of
  *     the same length, sign and strides are grouped into items of up to 32
  *     transforms, each transform with its own array pointers;
  *   - a prime length is a Bluestein single (power-of-two convolution) or, if
@@ -16,7 +16,9 @@
  *     (pass B, into the output); row tiles wait for their transform's column
  *     tiles on a device counter.
  * Items are queued column tiles first, then singles by decreasing cost, then
- * row tiles, so no wait can block a claimed item.
+ * row tiles, so no wait can block a claimed item.  Prime singles whose
+ * convolution needs twice the tile (nb up to 8192 single / 4096 double) go to
+ * a second queue with larger tiles, launched first in the same graph.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -25,7 +27,6 @@
 #include <cuda_runtime_api.h>
 #include "gb_host.h"
 
-#define GB_Q_THREADS 512
 #define GB_Q_GROUP 32
 
 typedef struct { long long n; int sign; long long is, os; const void *in; void *out; } xform;
@@ -33,9 +34,11 @@ typedef struct { long long n; int sign; long long is, os; const void *in; void *
 struct gb_set {
      int prec;
      int nitems, nctr;
-     int grid, threads, smem;
+     int nsmall, nlarge;            /* items of the small-tile and large-tile queues */
+     int grid, threads, smem;       /* small-tile queue launch */
+     int grid_l, threads_l, smem_l; /* large-tile queue launch */
      gb_qitem *d_items;
-     int *d_head, *d_ctrs;
+     int *d_head, *d_ctrs;          /* two queue heads */
      void **d_ptrs;
      void *d_scratch;
      size_t scratch_bytes;
@@ -65,14 +68,15 @@ static long long pow2_at_least(long long v)
 
 /* Fill the pass fields a queue item needs (the shared-memory tile body). */
 static int item_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os,
-                     long long vn0, long long vis0, long long vos0, int tb, int cols_in, int cols_out)
+                     long long vn0, long long vis0, long long vos0, int tb, int cols_in, int cols_out, int threads)
 {
      memset(P, 0, sizeof *P);
+     P->ltb = -1;
      P->kind = kind; P->prec = prec; P->sign = sign; P->n = (int)n;
      P->nfft = (int)(kind == GB_KIND_BLUESTEIN ? pow2_at_least(2 * n - 1) : kind == GB_KIND_RADER ? n - 1 : n);
      P->variant = GB_VAR_GEN;
      P->tb = tb;
-     P->threads = GB_Q_THREADS;
+     P->threads = threads;
      P->smem = 2 * tb * (P->nfft + 1) * 2 * prec;
      P->load_mode = cols_in ? GB_MOVE_COLS : GB_MOVE_ROWS;
      P->store_mode = cols_out ? GB_MOVE_COLS : GB_MOVE_ROWS;
@@ -125,19 +129,30 @@ static int cmp_key(const void *a, const void *b)
      return 0;
 }
 
-/* which way a prime (or non-smooth) length runs as a single */
-static int prime_kind(int prec, long long n, int cap)
+/* How a prime (or non-smooth) length runs as a single: Rader (n-1 smooth)
+ * or Bluestein (power-of-two convolution), in the small-tile queue when its
+ * FFT fits cap_s, else in the large-tile queue (cap_l).  *large is set for
+ * the latter; -1 when neither fits. */
+static int prime_kind(int prec, long long n, int cap_s, int cap_l, int *large)
 {
      int rad[GB_MAXRAD];
      const char *e = getenv("FFTW_GB300_PRIME");
      char key[128];
      const gb_wisdom_entry *w;
-     int rader_ok = is_prime_ll(n) && gb_factor_radices(n - 1, rad) >= 0 && n - 1 <= cap;
+     int rader = is_prime_ll(n) && gb_factor_radices(n - 1, rad) >= 0;
+     long long nb = pow2_at_least(2 * n - 1);
+     int want_rader;
      snprintf(key, sizeof key, "c2c p%d n%lld", prec, n);
      w = gb_wisdom_lookup(key);
-     if (rader_ok && ((w && w->variant == GB_KIND_RADER) || (!w && e && !strcmp(e, "rader")))) return GB_KIND_RADER;
-     if (pow2_at_least(2 * n - 1) <= cap) return GB_KIND_BLUESTEIN;
-     if (rader_ok) return GB_KIND_RADER;
+     want_rader = rader && ((w && w->variant == GB_KIND_RADER) || (!w && e && !strcmp(e, "rader")));
+     *large = 0;
+     if (want_rader && n - 1 <= cap_s) return GB_KIND_RADER;
+     if (nb <= cap_s) return GB_KIND_BLUESTEIN;
+     if (rader && n - 1 <= cap_s) return GB_KIND_RADER;
+     *large = 1;
+     if (want_rader && n - 1 <= cap_l) return GB_KIND_RADER;
+     if (nb <= cap_l) return GB_KIND_BLUESTEIN;
+     if (rader && n - 1 <= cap_l) return GB_KIND_RADER;
      return -1;
 }
 
@@ -145,11 +160,16 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
 {
      gb_set *S;
      xform *xs;
-     int nx = 0, cap = prec == 4 ? 8192 : 4096, i, j;
+     int nx = 0, i, j;
+     /* small-tile queue: 2 x (4096+1) complex64 (2048 complex128) = 65.5 KB,
+      * three 256-thread CTAs per SM; large-tile queue: twice that, one
+      * 512-thread CTA per SM, only for what the small tiles cannot hold */
+     const int cap_s = prec == 4 ? 4096 : 2048, cap_l = 2 * cap_s, cap = cap_s;
      int cs = 2 * prec;
-     qvec QA = {0, 0, 0}, QM = {0, 0, 0}, QB = {0, 0, 0};
-     gb_qitem *A, *M, *B;
-     int na, nm, nb;
+     qvec QA = {0, 0, 0}, QM = {0, 0, 0}, QB = {0, 0, 0}, QL = {0, 0, 0};
+     gb_qitem *A, *M, *B, *Lg;
+     int na, nm, nb, nl;
+     int smem_l = 0;
      void **hptr = 0;
      int nptr = 0, cap_ptr;
      long long scratch_elems = 0;
@@ -188,22 +208,23 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
      for (i = 0; i < nx;) {
           xform *x = &xs[i];
           long long n = x->n;
-          int rad[GB_MAXRAD], kind = GB_KIND_C2C, g;
+          int rad[GB_MAXRAD], kind = GB_KIND_C2C, g, large = 0;
           int smooth = gb_factor_radices(n, rad) >= 0;
-          if (n <= cap && smooth) kind = GB_KIND_C2C;
-          else if (!smooth && (kind = prime_kind(prec, n, cap)) > 0) { /* single */ }
+          if (n <= cap_s && smooth) kind = GB_KIND_C2C;
+          else if (!smooth && (kind = prime_kind(prec, n, cap_s, cap_l, &large)) > 0) { /* single */ }
           else kind = -1;
           if (kind >= 0) {
                /* group transforms with the same key */
                gb_pass tmp;
+               int cq = large ? cap_l : cap_s, thr = large ? 512 : 256;
                long long nfft = kind == GB_KIND_BLUESTEIN ? pow2_at_least(2 * n - 1) : kind == GB_KIND_RADER ? n - 1 : n;
-               int tbmax = (int)((2LL * (cap + 1) * cs) / (2LL * (nfft + 1) * cs));
+               int tbmax = (int)((2LL * (cq + 1) * cs) / (2LL * (nfft + 1) * cs));
                if (tbmax > GB_Q_GROUP) tbmax = GB_Q_GROUP;
                if (tbmax < 1) tbmax = 1;
                for (g = 0; i + g < nx && g < tbmax && cmp_key(&xs[i], &xs[i + g]) == 0; ++g) {}
-               if (item_pass(&tmp, prec, kind, n, x->sign, x->is, x->os, g, 0, 0, g, 0, 0)) goto fail;
+               if (item_pass(&tmp, prec, kind, n, x->sign, x->is, x->os, g, 0, 0, g, 0, 0, thr)) goto fail;
                {
-                    gb_qitem *q = qpush(&QM);
+                    gb_qitem *q = qpush(large ? &QL : &QM);
                     if (!q) goto fail;
                     q->P = tmp;
                     q->pin = (const void *const *)(size_t)nptr;     /* index now, device address later */
@@ -211,7 +232,8 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                     for (j = 0; j < g; ++j) { hptr[nptr + j] = (void *)xs[i + j].in; hptr[nptr + g + j] = xs[i + j].out; }
                     nptr += 2 * g;
                     q->wait_ctr = -1; q->signal_ctr = -1;
-                    if (tmp.smem > smem) smem = tmp.smem;
+                    if (large) { if (tmp.smem > smem_l) smem_l = tmp.smem; }
+                    else if (tmp.smem > smem) smem = tmp.smem;
                }
                i += g;
                continue;
@@ -235,7 +257,7 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                while (tbc > 1 && 2LL * tbc * ((n1 > n2 ? n1 : n2) + 1) * cs > 2LL * (cap + 1) * cs) tbc >>= 1;
                /* pass A: columns n2 (stride is), n1-point transforms with
                 * element stride n2*is into scratch [n2][k1] */
-               if (item_pass(&pa, prec, GB_KIND_C2C, n1, x->sign, n2 * x->is, 1, n2, x->is, n1, tbc, 1, 0)) goto fail;
+               if (item_pass(&pa, prec, GB_KIND_C2C, n1, x->sign, n2 * x->is, 1, n2, x->is, n1, tbc, 1, 0, 256)) goto fail;
                pa.post_N = n;
                if (gb_pass_tables(&pa)) goto fail;
                for (k0 = 0; k0 < n2; k0 += tbc) {
@@ -251,7 +273,7 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                if (pa.smem > smem) smem = pa.smem;
                /* pass B: k1 columns of scratch (stride 1), n2-point transforms
                 * with element stride n1, into out[k1 + n1*k2] */
-               if (item_pass(&pb, prec, GB_KIND_C2C, n2, x->sign, n1, n1 * x->os, n1, 1, x->os, tbc, 1, 1)) goto fail;
+               if (item_pass(&pb, prec, GB_KIND_C2C, n2, x->sign, n1, n1 * x->os, n1, 1, x->os, tbc, 1, 1, 256)) goto fail;
                for (k0 = 0; k0 < n1; k0 += tbc) {
                     gb_qitem *q = qpush(&QB);
                     if (!q) goto fail;
@@ -266,24 +288,30 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           }
           ++i;
      }
-     A = QA.v; M = QM.v; B = QB.v;
-     na = QA.n; nm = QM.n; nb = QB.n;
+     A = QA.v; M = QM.v; B = QB.v; Lg = QL.v;
+     na = QA.n; nm = QM.n; nb = QB.n; nl = QL.n;
      if (nm) qsort(M, (size_t)nm, sizeof(gb_qitem), cmp_cost_desc);
+     if (nl) qsort(Lg, (size_t)nl, sizeof(gb_qitem), cmp_cost_desc);
 
      S = (gb_set *)calloc(1, sizeof *S);
      S->prec = prec;
-     S->nitems = na + nm + nb;
+     S->nitems = na + nm + nb + nl;
+     S->nsmall = na + nm + nb;
+     S->nlarge = nl;
      S->nctr = nctr;
-     S->threads = GB_Q_THREADS;
+     S->threads = 256;
      S->smem = smem;
+     S->threads_l = 512;
+     S->smem_l = smem_l;
      S->nsingle_items = nm;
      S->nlong = nctr;
      S->ntransforms = nx;
      S->scratch_bytes = (size_t)scratch_elems * cs;
-     S->grid = gb_queue_grid(prec, S->threads, S->smem);
-     if (S->grid <= 0) { gb_set_error("plan set: queue kernel does not fit (smem %d)", smem); free(S); goto fail; }
+     S->grid = S->nsmall ? gb_queue_grid(prec, S->threads, S->smem) : 1;
+     S->grid_l = S->nlarge ? gb_queue_grid(prec, S->threads_l, S->smem_l) : 1;
+     if (S->grid <= 0 || S->grid_l <= 0) { gb_set_error("plan set: queue kernel does not fit (smem %d/%d)", smem, smem_l); free(S); goto fail; }
      if (cudaMalloc((void **)&S->d_items, sizeof(gb_qitem) * (size_t)(S->nitems ? S->nitems : 1)) != cudaSuccess ||
-         cudaMalloc((void **)&S->d_head, sizeof(int)) != cudaSuccess ||
+         cudaMalloc((void **)&S->d_head, 2 * sizeof(int)) != cudaSuccess ||
          cudaMalloc((void **)&S->d_ctrs, sizeof(int) * (size_t)(nctr ? nctr : 1)) != cudaSuccess ||
          cudaMalloc((void **)&S->d_ptrs, sizeof(void *) * (size_t)(nptr ? nptr : 1)) != cudaSuccess ||
          (S->scratch_bytes && cudaMalloc(&S->d_scratch, S->scratch_bytes) != cudaSuccess)) {
@@ -312,6 +340,12 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                all[k].in = (const char *)S->d_scratch + (size_t)B[i].in * cs;
                ++k;
           }
+          for (i = 0; i < nl; ++i) {
+               all[k] = Lg[i];
+               all[k].pin = (const void *const *)(S->d_ptrs + (size_t)Lg[i].pin);
+               all[k].pout = (void *const *)(S->d_ptrs + (size_t)Lg[i].pout);
+               ++k;
+          }
           if (cudaMemcpy(S->d_items, all, sizeof(gb_qitem) * (size_t)S->nitems, cudaMemcpyHostToDevice) != cudaSuccess ||
               (nptr && cudaMemcpy(S->d_ptrs, hptr, sizeof(void *) * (size_t)nptr, cudaMemcpyHostToDevice) != cudaSuccess)) {
                free(all);
@@ -321,10 +355,10 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           }
           free(all);
      }
-     free(QA.v); free(QM.v); free(QB.v); free(hptr); free(xs);
+     free(QA.v); free(QM.v); free(QB.v); free(QL.v); free(hptr); free(xs);
      return S;
 fail:
-     free(QA.v); free(QM.v); free(QB.v); free(hptr); free(xs);
+     free(QA.v); free(QM.v); free(QB.v); free(QL.v); free(hptr); free(xs);
      return 0;
 }
 
@@ -340,9 +374,13 @@ static int build_graph(gb_set *S)
      } else st = (cudaStream_t)S->stream;
      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = -1;
      if (!rc) {
-          cudaMemsetAsync(S->d_head, 0, sizeof(int), st);
+          cudaMemsetAsync(S->d_head, 0, 2 * sizeof(int), st);
           if (S->nctr) cudaMemsetAsync(S->d_ctrs, 0, sizeof(int) * (size_t)S->nctr, st);
-          if (gb_launch_queue(S->d_items, S->nitems, S->d_head, S->d_ctrs, S->prec, S->threads, S->smem, S->grid, st))
+          if (S->nlarge && gb_launch_queue(S->d_items + S->nsmall, S->nlarge, S->d_head + 1, S->d_ctrs, S->prec,
+                                           S->threads_l, S->smem_l, S->grid_l, st))
+               rc = -1;
+          if (S->nsmall && gb_launch_queue(S->d_items, S->nsmall, S->d_head, S->d_ctrs, S->prec, S->threads,
+                                           S->smem, S->grid, st))
                rc = -1;
           if (cudaStreamEndCapture(st, &S->graph) != cudaSuccess) rc = -1;
      }
@@ -386,6 +424,8 @@ void gb_set_info(const gb_set *S, int *nitems, int *ntransforms, int *nlong, int
 {
      *nitems = S->nitems; *ntransforms = S->ntransforms; *nlong = S->nlong; *grid = S->grid; *smem = S->smem;
 }
+
+int gb_set_large_items(const gb_set *S) { return S->nlarge; }
 
 void gb_destroy_set(gb_set *S)
 {

@@ -84,8 +84,7 @@ int gb_tune(gb_plan *p, unsigned flags)
      const gb_problem *prb = &p->prb;
      char key[128];
      gb_wisdom_entry cand[64], best_e;
-     int nc = 0, i, have_prev = 0;
-     gb_wisdom_entry prev;
+     int nc = 0, i;
      const gb_wisdom_entry *w;
      double best = 1e30, t0 = now_s(), limit = gb_get_timelimit();
      void *din = 0, *dout = 0;
@@ -104,7 +103,7 @@ int gb_tune(gb_plan *p, unsigned flags)
           int tbs[] = {1, 2, 4, 8, 16, 32, 64};
           int ntb = (flags & (FFTW_PATIENT | FFTW_EXHAUSTIVE)) ? 7 : 4;
           cand[nc].variant = -1; cand[nc].tb = 0; cand[nc].n1 = 0; ++nc;    /* the heuristic choice */
-          if ((n & (n - 1)) == 0 && n >= 64 && n <= 4096) {
+          if ((n & (n - 1)) == 0 && n >= 64 && n <= 8192) {
                cand[nc].variant = GB_VAR_REG; cand[nc].tb = 0; ++nc;       /* no bulk-copy pipeline */
           }
           for (i = 0; i < ntb && nc < 40; ++i) {
@@ -145,7 +144,6 @@ int gb_tune(gb_plan *p, unsigned flags)
      }
      cudaFree(din);
      cudaFree(dout);
-     (void)have_prev; (void)prev;
      strcpy(best_e.key, key);
      gb_wisdom_store(&best_e);
      {
@@ -160,6 +158,7 @@ int gb_tune(gb_plan *p, unsigned flags)
                p->measured_ms = best;
                free(q);
                if (keep.scratch) cudaFree(keep.scratch);
+               if (keep.scratch2) cudaFree(keep.scratch2);
                if (keep.stage_in) cudaFree(keep.stage_in);
                if (keep.stage_out) cudaFree(keep.stage_out);
           }
