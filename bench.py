@@ -107,6 +107,20 @@ def bytes_per_step(kind, shape, howmany, prec):
     return (n * cs // 2 + nc * cs) * howmany
 
 
+def aggregate(ms_local, ws, flops_per_rank, device):
+    """Whole-job throughput: the slowest rank's time (max over ranks, the
+    only collective; the transforms themselves never cross ranks) and the
+    flops of all ranks over it.  Returns (ms_max, Gflop/s)."""
+    ms = float(ms_local)
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, flops_per_rank * ws / (ms * 1e-3) / 1e9
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -298,13 +312,9 @@ def run_ours(args):
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     launches = g.launch_count() - l0
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / args.steps
     fl = flops_per_step(kind, shape, howmany)
-    value = fl * ws / (ms_step * 1e-3) / 1e9
+    ms, value = aggregate(ms, ws, fl * args.steps, "cuda")
+    ms_step = ms / args.steps
 
     # accuracy of this run on a sample of transforms, against the oracle
     # (in-place or very long single transforms: forward/backward round trip)

@@ -133,20 +133,35 @@ template <typename C, bool PADDED, bool PAIRS_REAL>
 __device__ __forceinline__ void coop_load(const gb_pass &P, const void *in, C *sm, int sms, const tile_t &tl,
                                           int L, int mode, int nfft = 0)
 {
+     /* eight loads in flight per thread before their shared-memory stores, so
+      * the memory latency is paid once per batch instead of once per element */
+     constexpr int U = 8;
      const int tb = P.tb;
      const int total = tb * L;
-     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-          int t, j;
-          if (mode == GB_MOVE_COLS) {
-               if (P.ltb >= 0) { t = idx & (tb - 1); j = idx >> P.ltb; }
-               else { t = idx % tb; j = idx / tb; }
-          } else { t = idx / L; j = idx - t * L; }
-          long long v = tl.v0 + t;
-          if (v < P.vn[0]) {
-               long long base = tl.bi + v * P.vis[0];
-               C x = PAIRS_REAL ? io<C>::ldpair(in, base, j, P.is, P.real_pairs) : io<C>::ldc(in, base, j, P.is);
-               sm[t * sms + (PADDED ? pad_for(nfft, j) : j)] = x;
+     for (int base0 = threadIdx.x; base0 < total; base0 += U * blockDim.x) {
+          C x[U];
+          int slot[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+               const int idx = base0 + u * blockDim.x;
+               slot[u] = -1;
+               if (idx < total) {
+                    int t, j;
+                    if (mode == GB_MOVE_COLS) {
+                         if (P.ltb >= 0) { t = idx & (tb - 1); j = idx >> P.ltb; }
+                         else { t = idx % tb; j = idx / tb; }
+                    } else { t = idx / L; j = idx - t * L; }
+                    const long long v = tl.v0 + t;
+                    if (v < P.vn[0]) {
+                         const long long base = tl.bi + v * P.vis[0];
+                         x[u] = PAIRS_REAL ? io<C>::ldpair(in, base, j, P.is, P.real_pairs) : io<C>::ldc(in, base, j, P.is);
+                         slot[u] = t * sms + (PADDED ? pad_for(nfft, j) : j);
+                    }
+               }
           }
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+               if (slot[u] >= 0) sm[slot[u]] = x[u];
      }
 }
 
@@ -701,17 +716,29 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
            * for the kinds that rearrange them afterwards */
           C *dst = (kind == GB_KIND_C2C || kind == GB_KIND_R2C) ? b0 : b1;
           const int L = (kind == GB_KIND_RADER) ? n : (kind == GB_KIND_C2R) ? n / 2 + 1 : N;
-          for (int idx = threadIdx.x; idx < tb * L; idx += blockDim.x) {
-               int t, j;
-               tile_index(idx, tb, L, P.load_mode, t, j, P.ltb);
-               if (tile.v0 + t < vn0) {
-                    C x;
-                    if (kind == GB_KIND_R2C) {
-                         const R *r = (const R *)src_of<R>(P, tile, A, t);
-                         x = P.real_pairs ? ((const C *)r)[j] : mk<C>(r[2 * j * P.is], r[(2 * j + 1) * P.is]);
-                    } else x = src_of<C>(P, tile, A, t)[j * P.is];
-                    dst[t * sms + j] = x;
+          constexpr int U = 4;   /* loads in flight per thread */
+          for (int idx0 = threadIdx.x; idx0 < tb * L; idx0 += U * blockDim.x) {
+               C x[U];
+               int slot[U];
+#pragma unroll
+               for (int u = 0; u < U; ++u) {
+                    const int idx = idx0 + u * blockDim.x;
+                    slot[u] = -1;
+                    if (idx < tb * L) {
+                         int t, j;
+                         tile_index(idx, tb, L, P.load_mode, t, j, P.ltb);
+                         if (tile.v0 + t < vn0) {
+                              if (kind == GB_KIND_R2C) {
+                                   const R *r = (const R *)src_of<R>(P, tile, A, t);
+                                   x[u] = P.real_pairs ? ((const C *)r)[j] : mk<C>(r[2 * j * P.is], r[(2 * j + 1) * P.is]);
+                              } else x[u] = src_of<C>(P, tile, A, t)[j * P.is];
+                              slot[u] = t * sms + j;
+                         }
+                    }
                }
+#pragma unroll
+               for (int u = 0; u < U; ++u)
+                    if (slot[u] >= 0) dst[slot[u]] = x[u];
           }
      } else if (kind == GB_KIND_R2C) {
           /* odd n: real sequence as complex with zero imaginary part */

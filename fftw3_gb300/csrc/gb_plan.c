@@ -381,6 +381,10 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
           if (cols_in || cols_out) { int want = prec == 4 ? 16 : 8; if (tb < want) tb = want; }
           if (tb_hint > 0) tb = tb_hint;
           while (tb > 1 && (tb * T > maxt || tb * sm1 > smax)) tb >>= 1;
+          /* column tiles: at most 256 threads, so two or more CTAs share an SM
+           * and one's loads overlap another's stages */
+          if ((cols_in || cols_out) && tb_hint == 0)
+               while (tb > 1 && tb * T > 256) tb >>= 1;
           while (tb > 1 && (tb >> 1) >= v[0].n) tb >>= 1;
           if (sm1 > smax) return 1;
           P->tb = tb;
