@@ -63,6 +63,7 @@ __host__ __device__ constexpr int reg_r0(int nfft)
 struct tile_t {
      long long bi, bo;   /* offsets contributed by dims 1.. */
      long long v0;       /* first index along dim 0 */
+     long long vpost;    /* index along dim post_vdim (>= 1) of a four-step pass */
 };
 
 __device__ __forceinline__ tile_t tile_of(const gb_pass &P, long long blk)
@@ -70,7 +71,7 @@ __device__ __forceinline__ tile_t tile_of(const gb_pass &P, long long blk)
      tile_t t;
      long long rest = blk / P.ntiles0;
      t.v0 = (blk - rest * P.ntiles0) * P.tb;
-     t.bi = 0; t.bo = 0;
+     t.bi = 0; t.bo = 0; t.vpost = 0;
 #pragma unroll
      for (int d = 1; d < GB_MAXV; ++d) {
           if (d < P.nv) {
@@ -79,6 +80,7 @@ __device__ __forceinline__ tile_t tile_of(const gb_pass &P, long long blk)
                rest = q;
                t.bi += i * P.vis[d];
                t.bo += i * P.vos[d];
+               if (d == P.post_vdim) t.vpost = i;
           }
      }
      return t;
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass
                     if (P.post_N) {
 #pragma unroll
                          for (int e = 0; e < E; ++e)
-                              x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
+                              x[e] = cmul(x[e], post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)(tid + T * e)));
                     }
                }
                constexpr bool RP = (KIND == GB_KIND_C2R);
@@ -596,7 +598,7 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
           } else {
                if (P.post_N) {
 #pragma unroll
-                    for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
+                    for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)(tid + T * e)));
                }
                if (valid) {
                     /* unit output stride (checked at launch): constant offsets */
@@ -824,7 +826,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                const long long v = tile.v0 + t;
                if (v < vn0) {
                     C y = res[t * sms + k];
-                    if (P.post_N) y = cmul(y, post_twiddle<C>(P, v * (long long)k));
+                    if (P.post_N) y = cmul(y, post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)k));
                     dst_of<C>(P, tile, A, t)[k * P.os] = y;
                }
           }

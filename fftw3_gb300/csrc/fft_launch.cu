@@ -277,6 +277,8 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->kind == GB_KIND_RADER && (p->variant != GB_VAR_GEN || !p->perm || !p->chirp_spec || p->nfft != p->n - 1))
                bad = "Rader pass needs its permutation and omega tables";
           else if (p->post_N && (!p->post_lo || !p->post_hi || p->post_S <= 0)) bad = "four-step twiddle tables missing";
+          else if (p->post_vdim < 0 || p->post_vdim >= p->nv || (p->post_vdim && !p->post_N))
+               bad = "four-step twiddle dimension is not a vector dimension of the pass";
           else if (p->threads < 1 || p->threads > 1024 || p->tb < 1 || p->nv < 1 || p->nv > GB_MAXV) bad = "bad launch shape";
           else if ((p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA) && p->kind != GB_KIND_COPY &&
                    p->threads != p->tb * (p->nfft / reg_e(p->nfft))) bad = "thread count does not match the tile";

@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_queue(const
                C *b0 = (C *)gb_smem;
                C *b1 = b0 + it.P.tb * (it.P.nfft + 1);
                tile_t tile;
-               tile.bi = it.bi; tile.bo = it.bo; tile.v0 = it.v0;
+               tile.bi = it.bi; tile.bo = it.bo; tile.v0 = it.v0; tile.vpost = 0;
                gen_addr A;
                A.in = it.in; A.out = it.out; A.pin = it.pin; A.pout = it.pout;
                gen_tile<C>(it.P, tile, A, b0, b1);

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
                     for (int q = 0; q < 16; ++q) y[q] = make_float2(v[q] * inv, v[16 + q] * inv);
                     if (P.post_N) {
 #pragma unroll
-                         for (int q = 0; q < 16; ++q) y[q] = cmul(y[q], post_twiddle<float2>(P, vv * (long long)(j + q * T)));
+                         for (int q = 0; q < 16; ++q) y[q] = cmul(y[q], post_twiddle<float2>(P, (P.post_vdim ? tile.vpost : vv) * (long long)(j + q * T)));
                     }
                     if (P.store_mode == GB_MOVE_DIRECT) {
                          if (vv < P.vn[0]) {

@@ -627,6 +627,69 @@ static void dense_dims(const gb_dim *v, int nv, long long L, gb_dim *out, int ke
      }
 }
 
+/* Four-step for an axis whose batch has a unit-stride dimension u (columns
+ * of a multi-dimensional array): both passes tile along u, so every tile
+ * row is a contiguous run of columns.  Scratch holds [outer][n2][k1][u].
+ * Pass A: n1-point transforms at element stride n2*is, twiddle
+ * W_n^(n2*k1) indexed by vector dimension 1 (n2); pass B: n2-point
+ * transforms at scratch stride n1*nu, written to k1 + n1*k2.
+ * Returns 0 when added, -1 when the layout or lengths do not allow it. */
+static int add_fourstep_cols(builder *b, long long n, int sign, long long is, long long os,
+                             int nvk, const gb_dim *v, int src, int dst, int mid)
+{
+     gb_plan *p = b->p;
+     int prec = p->prb.prec, i, u = -1, no = 0;
+     long long n1 = 0, d, nu, dense, outer = 1;
+     gb_dim va[GB_MAXV], vb[GB_MAXV], vo[GB_MAXRANK];
+     gb_step *sa, *sb;
+     for (i = 0; i < nvk; ++i)
+          if (llabs_(v[i].is) == 1 && llabs_(v[i].os) == 1 && v[i].n >= 8) { u = i; break; }
+     if (u < 0 || nvk - 1 > GB_MAXV - 2) return -1;
+     for (d = 2; d * d <= n; ++d) {
+          gb_pass t1, t2;
+          gb_dim one = {1, 0, 0};
+          if (n % d) continue;
+          if (config_pass(&t1, prec, GB_KIND_C2C, d, sign, 1, 1, 1, &one, 0, 0) == 0 &&
+              config_pass(&t2, prec, GB_KIND_C2C, n / d, sign, 1, 1, 1, &one, 0, 0) == 0 &&
+              t1.variant != GB_VAR_GEN && t2.variant != GB_VAR_GEN)
+               n1 = d;
+     }
+     if (!n1) return -1;
+     nu = v[u].n;
+     for (i = 0; i < nvk; ++i) if (i != u) { vo[no++] = v[i]; outer *= v[i].n; }
+     need_scratch(p, mid, (size_t)(n * nu * outer) * csize(prec));
+     /* pass A */
+     va[0].n = nu; va[0].is = v[u].is; va[0].os = 1;
+     va[1].n = n / n1; va[1].is = is; va[1].os = n1 * nu;
+     dense = n * nu;
+     for (i = 0; i < no; ++i) { va[2 + i].n = vo[i].n; va[2 + i].is = vo[i].is; va[2 + i].os = dense; dense *= vo[i].n; }
+     sa = new_step(b);
+     if (!sa) return -1;
+     sa->src = src; sa->dst = mid;
+     if (config_pass(&sa->pass, prec, GB_KIND_C2C, n1, sign, (n / n1) * is, nu, 2 + no, va, 0, 1)) { --p->nstep; return -1; }
+     sa->pass.post_N = n;
+     sa->pass.post_vdim = 1;
+     if (p->flags & GB_FLAG_TENSOR_CORE) use_tensor_cores(&sa->pass);
+     if (pass_tables(&sa->pass)) { b->err = 1; return 0; }
+     /* pass B */
+     vb[0].n = nu; vb[0].is = 1; vb[0].os = v[u].os;
+     vb[1].n = n1; vb[1].is = nu; vb[1].os = os;
+     dense = n * nu;
+     for (i = 0; i < no; ++i) { vb[2 + i].n = vo[i].n; vb[2 + i].is = dense; vb[2 + i].os = vo[i].os; dense *= vo[i].n; }
+     sb = new_step(b);
+     if (!sb) return -1;
+     sb->src = mid; sb->dst = dst;
+     if (config_pass(&sb->pass, prec, GB_KIND_C2C, n / n1, sign, n1 * nu, n1 * os, 2 + no, vb, 0, 1)) {
+          p->nstep -= 2;
+          return -1;
+     }
+     if (p->flags & GB_FLAG_TENSOR_CORE) use_tensor_cores(&sb->pass);
+     if (pass_tables(&sb->pass)) { b->err = 1; return 0; }
+     count_ops(p, &sa->pass, outer * nu * (n / n1));
+     count_ops(p, &sb->pass, outer * nu * n1);
+     return 0;
+}
+
 static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is, long long os,
                        int nv, const gb_dim *v_in, int src, int dst, int mid)
 {
@@ -678,6 +741,18 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
      rc = config_pass(&s->pass, prec, kind, n, sign, is, os, nvk - s->nloop, v + s->nloop,
                       (w && w->tb > 0) ? w->tb : 0, 0);
      cfg_no_tma = 0;
+     if (rc == 0 && kind == GB_KIND_C2C && !(w && w->tb > 0) && src != mid && dst != mid &&
+         (s->pass.load_mode == GB_MOVE_COLS || s->pass.store_mode == GB_MOVE_COLS) &&
+         s->pass.tb * csize(prec) < 32 && s->nloop == 0) {
+          /* a column pass whose tile rows would be narrower than one 32-byte
+           * sector: two passes with wide column tiles move fewer wasted bytes */
+          gb_step keep = *s;
+          --p->nstep;
+          if (add_fourstep_cols(b, n, sign, is, os, nvk, v, src, dst, mid) == 0) return;
+          if (b->err) return;
+          p->step[p->nstep++] = keep;
+          s = &p->step[p->nstep - 1];
+     }
      if (rc == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
      if (rc == 0) {
           if (pass_tables(&s->pass)) { b->err = 1; return; }

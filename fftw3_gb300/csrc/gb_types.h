@@ -86,6 +86,7 @@ typedef struct gb_pass {
      long long post_N;
      long long post_S;    /* power of two; post_lS = log2(post_S) */
      int post_lS;
+     int post_vdim;       /* vector dimension whose index v multiplies k in the twiddle (0 = the tile dim) */
      int ltb;             /* log2(tb) when tb is a power of two, else -1 */
      const void *post_lo;
      const void *post_hi;

@@ -153,6 +153,30 @@ def test_c2c_multid(lib, torch_cuda, restatement, shape, prec):
         assert rel_l2(y, oracle_c2c(restatement, x, shape, sign, prec)) <= TOL[prec]
 
 
+COLS4 = [([4096, 16], "f"), ([16384, 8], "f"), ([8192, 64], "f"), ([4096, 1024], "f"),
+         ([8192, 128], "d"), ([4096, 64], "d")]
+
+
+@pytest.mark.parametrize("shape,prec", COLS4, ids=[f"{'x'.join(map(str, s))}-{p}" for s, p in COLS4])
+def test_c2c_column_fourstep(lib, torch_cuda, restatement, shape, prec):
+    """A long strided axis whose single column pass would move tiles narrower
+    than 32 bytes runs as two column passes (four-step, twiddle indexed by a
+    vector dimension of the first pass)."""
+    import fftw3_gb300 as g
+    g.set_dry_run(True)
+    try:
+        d = g.plan_many_dft(shape, 2, 1 << 20, 1 << 30, prec=prec).describe()
+    finally:
+        g.set_dry_run(False)
+    assert "ld=cols st=cols" in d and "+twiddle" in d
+    rng = np.random.default_rng(shape[0] + shape[1])
+    tot = int(np.prod(shape))
+    x = rng.standard_normal(tot * 2) + 1j * rng.standard_normal(tot * 2)
+    for sign in (-1, 1):
+        y, _ = run_c2c(torch_cuda, x, shape, sign, prec, 2)
+        assert rel_l2(y, oracle_c2c(restatement, x, shape, sign, prec)) <= TOL[prec]
+
+
 def test_c2c_inplace_3d(lib, torch_cuda, restatement):
     """plan_dft_3d in place, forward then backward (the 3D in-place workload's layout)."""
     import fftw3_gb300 as g
@@ -232,7 +256,8 @@ def test_r2c_c2r_1d(lib, torch_cuda, restatement, n, prec):
     assert rel_l2(_host(ro), ref) <= TOL[prec]
 
 
-@pytest.mark.parametrize("shape", [[8, 6], [64, 64], [5, 7, 9], [16, 32, 30], [256, 512]], ids=str)
+@pytest.mark.parametrize("shape", [[8, 6], [64, 64], [5, 7, 9], [16, 32, 30], [256, 512], [2048, 2048], [4096, 100]],
+                         ids=str)
 def test_r2c_c2r_multid(lib, torch_cuda, restatement, shape):
     import fftw3_gb300 as g
     torch = torch_cuda

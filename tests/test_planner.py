@@ -4,6 +4,8 @@ Bluestein for large primes, tile/move choices for strided axes), and the
 wisdom text format."""
 import ctypes
 
+import numpy as np
+
 import pytest
 
 import fftw3_gb300 as g
@@ -64,7 +66,12 @@ def test_r2c_2d_is_r2c_then_c2c():
     p = g.plan_many_dft_r2c([8192, 8192], 1, 1 << 20, 1 << 30, prec="f")
     ps = passes(p)
     assert ps[0]["kind"] == 1 and ps[0]["nfft"] == 4096
-    assert ps[1]["kind"] == 0 and ps[1]["nfft"] == 8192
+    # the 8192-point column axis: one column pass would move tiles one
+    # column (8 bytes) wide, so it runs as a four-step pair of column passes
+    # with wide tiles whose lengths multiply to 8192
+    assert all(x["kind"] == 0 for x in ps[1:])
+    assert int(np.prod([x["nfft"] for x in ps[1:]])) == 8192
+    assert p.describe().count("ld=cols") == len(ps) - 1
 
 
 def test_c2r_multid_does_c2c_first():
