@@ -118,6 +118,8 @@ def load(path: str | None = None):
     lib.fftw_gb300_failures.restype = ci
     lib.fftw_gb300_set_dry_run.argtypes = [ci]
     lib.fftw_gb300_launch_count.restype = ctypes.c_longlong
+    lib.fftwf_gb300_dft_1d_noalloc.restype = ci
+    lib.fftwf_gb300_dft_1d_noalloc.argtypes = [ci, ci, vp, vp, ci, vp]
     _lib = lib
     return lib
 
@@ -131,7 +133,7 @@ def declared_symbols() -> list[str]:
     for pfx in ("fftw_", "fftwf_"):
         names += [pfx + n for n in per]
     ext = open(HEADERS[1]).read()
-    names += re.findall(r"extern [^;(]*?\b(fftw_gb300_\w+)\s*\(", ext)
+    names += re.findall(r"extern [^;(]*?\b(fftwf?_gb300_\w+)\s*\(", ext)
     body = ext[ext.index("#define GB_FFTW_EXT_DECLARE"):ext.index("GB_FFTW_EXT_DECLARE(fftw_)")]
     per = sorted(set(re.findall(r"PFX##(\w+)\s*\(", body)))
     for pfx in ("fftw_", "fftwf_"):

@@ -39,6 +39,23 @@ extern int fftw_gb300_device_status(void);
  * ks in 1..6.  Returns 0 on success. */
 extern int fftw_gb300_tc_selftest(const void *A, const void *B, float *D, int ks);
 
+/* No counterpart in the reference: a batched f32 1D c2c DFT that allocates
+ * no device memory, for callers that cannot call cudaMalloc (device memory
+ * owned by their own arena or budget; loops that cannot take cudaMalloc's
+ * implicit synchronisation).  It runs the two-pass (four-step) kernels of
+ * a long 1D plan with their scratch and twiddle tables in one fixed device
+ * array of the library, which every GPU it runs on holds until exit
+ * (16 MiB + 33 KiB).  howmany contiguous transforms of length n at distance
+ * n; in and out are device arrays (they may be the same); n is a power of
+ * two from 2^12 to 2^21 and n * howmany <= FFTWF_GB300_NOALLOC_MAX_POINTS,
+ * else it returns -1 without launching.  Enqueues on cuda_stream and
+ * returns 0, or -1 with fftw_gb300_last_error() set.  The first call on a
+ * device looks up the array's address (set-up); make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+#define FFTWF_GB300_NOALLOC_MAX_POINTS (1 << 21)
+extern int fftwf_gb300_dft_1d_noalloc(int n, int howmany, const fftwf_complex *in, fftwf_complex *out,
+                                      int sign, void *cuda_stream);
+
 #define GB_FFTW_EXT_DECLARE(PFX)                                                       \
 extern int PFX##gb300_set_stream(PFX##plan p, void *cuda_stream);                     \
 extern int PFX##gb300_set_async(PFX##plan p, int async);                              \
