@@ -291,16 +291,26 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
      }
 }
 
-/* Threads per CTA for k_reg: T = nfft/E threads per transform, at most 512
+/* Threads per CTA for k_reg: T = nfft/E threads per transform, at most 256
  * per CTA unless one transform needs more (several transforms per CTA for
  * short lengths). */
 __host__ __device__ constexpr int reg_maxthreads(int nfft)
 {
-     return (nfft / reg_e(nfft)) > 512 ? (nfft / reg_e(nfft)) : 512;
+     return (nfft / reg_e(nfft)) > 256 ? (nfft / reg_e(nfft)) : 256;
+}
+
+/* CTAs of k_reg resident per SM that the register budget is sized for:
+ * three 256-thread CTAs (80 registers a thread) for f32 c2c, whose strided
+ * column passes need the extra warps in flight to cover HBM latency; two
+ * (128 registers) where three would spill: f64, and the kinds with pre- or
+ * post-processing. */
+__host__ __device__ constexpr int reg_minblocks(int nfft, int csize, int kind)
+{
+     return reg_maxthreads(nfft) > 256 ? 1 : ((csize == 8 && kind == 0) ? 3 : 2);
 }
 
 template <typename C, int LOGN, int DIR, int KIND>
-__global__ void __launch_bounds__(reg_maxthreads(1 << LOGN)) k_reg(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+__global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << LOGN, sizeof(C), KIND)) k_reg(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
 {
      typedef typename real_of<C>::T R;
      constexpr int N = 1 << LOGN;

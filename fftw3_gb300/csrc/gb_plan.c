@@ -292,7 +292,7 @@ int gb_factor_radices(long long n, int *rad) { return gb_factor(n, rad); }
 static int reg_max_log(int prec) { return prec == 4 ? 14 : 13; }
 static int reg_e(int nfft) { return nfft < 16 ? nfft : 16; }
 static int reg_sms(int nfft) { return gb_reg_sms(nfft); }
-static int reg_maxthreads(int nfft) { int t = nfft / reg_e(nfft); return t > 512 ? t : 512; }
+static int reg_maxthreads(int nfft) { int t = nfft / reg_e(nfft); return t > 256 ? t : 256; }
 static int tma_sms(int nfft) { return gb_reg_sms(nfft); }
 
 /* FFTW's canonical vector tensor: drop n = 1, merge dims that are
