@@ -14,6 +14,7 @@
 #include <string.h>
 #include <stdint.h>
 #include <cuda_runtime_api.h>
+#include "fftw3.h"
 #include "gb_host.h"
 
 typedef struct { long long lo, hi; } extent;   /* element offsets, [lo, hi] */
@@ -135,6 +136,135 @@ static int run_step(const gb_plan *p, const gb_step *s, char *bufs[4], int esz[4
      return 0;
 }
 
+/* ------------------------------------------------ pipelined host staging */
+
+/* Input bytes per chunk: large enough that each copy runs at full link
+ * speed, small enough that a long batch gives several chunks to overlap. */
+#define GB_CHUNK_BYTES (96LL << 20)
+
+/* Decide whether the batch can be cut into chunks along one vector
+ * dimension d (the one with the largest input stride): every transform's
+ * input and output must lie inside one stride of d (chunks are disjoint
+ * byte ranges), the output of a chunk must be dense (no gaps whose host
+ * values a copy-out would overwrite), and an in-place transform must use
+ * the same byte range for input and output.  On success allocates three
+ * device slots per side, two streams and the events, and compiles the
+ * chunk plans.  Returns 1 when ready, 0 when not applicable, -1 on error. */
+static int chunk_prepare(gb_plan *p, int inplace)
+{
+     gb_problem q = p->prb;
+     const gb_problem *prb = &p->prb;
+     extent ei, eo;
+     long long ci, co, nd, m, bi, bo;
+     int d = -1, i, j, esin = elsize(prb, 0), esout = elsize(prb, 1);
+     if (p->chunk_state) return p->chunk_state;
+     p->chunk_state = -1;
+     for (i = 0; i < prb->vrank; ++i)
+          if (prb->vec[i].n >= 2 && prb->vec[i].is > 0 && prb->vec[i].os > 0 &&
+              (d < 0 || prb->vec[i].is * esin > prb->vec[d].is * esin))
+               d = i;
+     if (d < 0) return 0;
+     nd = prb->vec[d].n;
+     q.vec[d].n = 1;
+     ei = tensor_extent(&q, 0, &ci);
+     eo = tensor_extent(&q, 1, &co);
+     if (ei.lo != 0 || eo.lo != 0) return 0;
+     if ((ei.hi + 1) > prb->vec[d].is || (eo.hi + 1) != prb->vec[d].os || co != eo.hi + 1) return 0;
+     if (inplace && prb->vec[d].is * esin != prb->vec[d].os * esout) return 0;
+     if (nd * prb->vec[d].is * esin < 2 * GB_CHUNK_BYTES || prb->vec[d].is * esin > GB_CHUNK_BYTES) return 0;
+     m = GB_CHUNK_BYTES / (prb->vec[d].is * esin);
+     if (m < 1) m = 1;
+     if (m > nd / 2) m = nd / 2;
+     bi = ((m - 1) * prb->vec[d].is + ei.hi + 1) * esin;
+     bo = m * prb->vec[d].os * esout;
+     if (inplace && bo > bi) bi = bo;
+     for (j = 0; j < GB_CHUNK_SLOTS; ++j) {
+          if (cudaMalloc(&p->chunk_buf[0][j], (size_t)bi + 256) != cudaSuccess) goto fail;
+          if (!inplace && cudaMalloc(&p->chunk_buf[1][j], (size_t)bo + 256) != cudaSuccess) goto fail;
+     }
+     p->chunk_bytes[0] = (size_t)bi;
+     p->chunk_bytes[1] = (size_t)bo;
+     for (i = 0; i < 2; ++i)
+          if (cudaStreamCreateWithFlags((cudaStream_t *)&p->chunk_stream[i], cudaStreamNonBlocking) != cudaSuccess) goto fail;
+     for (i = 0; i < 3; ++i)
+          for (j = 0; j < GB_CHUNK_SLOTS; ++j)
+               if (cudaEventCreateWithFlags((cudaEvent_t *)&p->chunk_ev[i][j], cudaEventDisableTiming) != cudaSuccess)
+                    goto fail;
+     q = p->prb;
+     q.in = p->chunk_buf[0][0];
+     q.out = inplace ? q.in : p->chunk_buf[1][0];
+     q.vec[d].n = m;
+     p->chunk_plan[0] = gb_mkplan(&q, FFTW_ESTIMATE);
+     if (!p->chunk_plan[0]) return -1;
+     if (nd % m) {
+          q.vec[d].n = nd % m;
+          p->chunk_plan[1] = gb_mkplan(&q, FFTW_ESTIMATE);
+          if (!p->chunk_plan[1]) return -1;
+     }
+     p->chunk_dim = d;
+     p->chunk_m = m;
+     p->chunk_state = 1;
+     return 1;
+fail:
+     cudaGetLastError();
+     gb_set_error("device slots for pipelined staging: %s", cudaGetErrorString(cudaGetLastError()));
+     return -1;
+}
+
+/* Host arrays, chunk by chunk on three streams: copy-in (H2D), the plan's
+ * stream (the chunk plan's passes) and copy-out (D2H).  Slot s = c mod 3 is
+ * reused by chunk c only after chunk c-3 has been transformed (input slot)
+ * and copied out (output slot), which the events order on the device. */
+static int chunk_execute(gb_plan *p, const char *in, char *out, int inplace)
+{
+     const gb_problem *prb = &p->prb;
+     const int d = p->chunk_dim, esin = elsize(prb, 0), esout = elsize(prb, 1);
+     const long long nd = prb->vec[d].n, m = p->chunk_m, nc = (nd + m - 1) / m;
+     cudaStream_t st = (cudaStream_t)p->stream, sin_ = (cudaStream_t)p->chunk_stream[0],
+                  sout = (cudaStream_t)p->chunk_stream[1];
+     gb_problem q = p->prb;
+     extent ei;
+     long long ci, c;
+     q.vec[d].n = 1;
+     ei = tensor_extent(&q, 0, &ci);
+     /* the caller's stream may still be writing the host input (or reading
+      * an earlier output): start the copies after what is queued there */
+     if (cudaEventRecord((cudaEvent_t)p->chunk_ev[2][0], st) != cudaSuccess ||
+         cudaStreamWaitEvent(sin_, (cudaEvent_t)p->chunk_ev[2][0], 0) != cudaSuccess ||
+         cudaStreamWaitEvent(sout, (cudaEvent_t)p->chunk_ev[2][0], 0) != cudaSuccess)
+          goto cuerr;
+     for (c = 0; c < nc; ++c) {
+          const int s = (int)(c % GB_CHUNK_SLOTS);
+          const long long mm = (c == nc - 1) ? nd - c * m : m;
+          gb_plan *cp = (mm == m) ? p->chunk_plan[0] : p->chunk_plan[1];
+          const size_t bin = (size_t)(((mm - 1) * prb->vec[d].is + ei.hi + 1) * esin);
+          const size_t bout = (size_t)(mm * prb->vec[d].os * esout);
+          const size_t oin = (size_t)(c * m * prb->vec[d].is * esin), oout = (size_t)(c * m * prb->vec[d].os * esout);
+          char *slot_in = (char *)p->chunk_buf[0][s], *slot_out = inplace ? slot_in : (char *)p->chunk_buf[1][s];
+          cudaEvent_t ev_in = (cudaEvent_t)p->chunk_ev[0][s], ev_tr = (cudaEvent_t)p->chunk_ev[1][s],
+                      ev_out = (cudaEvent_t)p->chunk_ev[2][s];
+          if (c >= GB_CHUNK_SLOTS && cudaStreamWaitEvent(sin_, inplace ? ev_out : ev_tr, 0) != cudaSuccess) goto cuerr;
+          if (cudaMemcpyAsync(slot_in, in + oin, bin, cudaMemcpyHostToDevice, sin_) != cudaSuccess) goto cuerr;
+          if (cudaEventRecord(ev_in, sin_) != cudaSuccess) goto cuerr;
+          if (cudaStreamWaitEvent(st, ev_in, 0) != cudaSuccess) goto cuerr;
+          if (c >= GB_CHUNK_SLOTS && !inplace && cudaStreamWaitEvent(st, ev_out, 0) != cudaSuccess) goto cuerr;
+          cp->stream = p->stream;
+          cp->async = 1;
+          if (gb_execute(cp, slot_in, slot_out)) return -1;
+          if (cudaEventRecord(ev_tr, st) != cudaSuccess) goto cuerr;
+          if (cudaStreamWaitEvent(sout, ev_tr, 0) != cudaSuccess) goto cuerr;
+          if (cudaMemcpyAsync(out + oout, slot_out, bout, cudaMemcpyDeviceToHost, sout) != cudaSuccess) goto cuerr;
+          if (cudaEventRecord(ev_out, sout) != cudaSuccess) goto cuerr;
+     }
+     if (cudaStreamSynchronize(sout) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess ||
+         cudaStreamSynchronize(sin_) != cudaSuccess)
+          goto cuerr;
+     return 0;
+cuerr:
+     gb_set_error("CUDA error during pipelined staging: %s", cudaGetErrorString(cudaGetLastError()));
+     return -1;
+}
+
 int gb_execute(gb_plan *p, void *in, void *out)
 {
      const gb_problem *prb = &p->prb;
@@ -176,6 +306,16 @@ int gb_execute(gb_plan *p, void *in, void *out)
                stage_i = stage_o = 0;
                direct_host = 1;
           }
+     }
+     /* other host input and output (multi-pass plans, pageable memory):
+      * pipelined chunks when the batch can be cut, so copies in, passes and
+      * copies out overlap */
+     if (!direct_host && !device_accessible(in) && !device_accessible(out) && !getenv("FFTW_GB300_STAGE_HOST")) {
+          int r = chunk_prepare(p, inplace);
+          if (r < 0) return -1;
+          /* the slots were laid out for the in-place-ness of the first call */
+          if (r > 0 && (p->chunk_buf[1][0] == 0) == inplace)
+               return chunk_execute(p, (const char *)in, (char *)out, inplace);
      }
      if (inplace && stage_i) {
           long long lo = ein.lo * esin < eout.lo * esout ? ein.lo * esin : eout.lo * esout;

@@ -46,6 +46,8 @@ typedef struct gb_step {
      gb_dim loop[GB_MAXLOOP];
 } gb_step;
 
+#define GB_CHUNK_SLOTS 3
+
 struct gb_plan {
      int refcnt;
      gb_problem prb;
@@ -57,6 +59,17 @@ struct gb_plan {
      /* staging buffers for host arrays */
      void *stage_in, *stage_out;
      size_t stage_in_bytes, stage_out_bytes;
+     /* pipelined staging of host arrays: the batch is cut along one vector
+      * dimension into chunks; a chunk plan transforms chunk c on the plan's
+      * stream while chunk c+1 is copied in and chunk c-1 copied out */
+     int chunk_state;           /* 0 = not tried yet, 1 = ready, -1 = not applicable */
+     int chunk_dim;             /* the vector dimension cut into chunks */
+     long long chunk_m;         /* transforms per chunk (vec[chunk_dim] entries) */
+     struct gb_plan *chunk_plan[2];   /* chunk of chunk_m; the shorter last chunk */
+     void *chunk_buf[2][GB_CHUNK_SLOTS];   /* device slots: [input/output][slot] */
+     size_t chunk_bytes[2];
+     void *chunk_stream[2];     /* copy-in and copy-out streams */
+     void *chunk_ev[3][GB_CHUNK_SLOTS];    /* copied in / transformed / copied out, per slot */
      void *stream;              /* cudaStream_t; 0 = legacy default stream */
      int async;                 /* 1: execute does not wait for completion */
      int in_align, out_align;   /* alignment of the planning arrays (bytes, capped at 16) */

@@ -1048,12 +1048,23 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
 
 void gb_destroy(gb_plan *p)
 {
+     int i, j;
      if (!p) return;
      if (!gb_dry) {
           if (p->scratch) cudaFree(p->scratch);
           if (p->scratch2) cudaFree(p->scratch2);
           if (p->stage_in) cudaFree(p->stage_in);
           if (p->stage_out) cudaFree(p->stage_out);
+          for (i = 0; i < 2; ++i) {
+               for (j = 0; j < GB_CHUNK_SLOTS; ++j)
+                    if (p->chunk_buf[i][j]) cudaFree(p->chunk_buf[i][j]);
+               if (p->chunk_stream[i]) cudaStreamDestroy((cudaStream_t)p->chunk_stream[i]);
+          }
+          for (i = 0; i < 3; ++i)
+               for (j = 0; j < GB_CHUNK_SLOTS; ++j)
+                    if (p->chunk_ev[i][j]) cudaEventDestroy((cudaEvent_t)p->chunk_ev[i][j]);
      }
+     for (i = 0; i < 2; ++i)
+          if (p->chunk_plan[i]) gb_destroy(p->chunk_plan[i]);
      free(p);
 }
