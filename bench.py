@@ -541,6 +541,8 @@ def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
     hin = getattr(lib, pfx + "malloc")(in_bytes)
     hout = hin if inplace else getattr(lib, pfx + "malloc")(out_bytes)
     ctypes.memset(hin, 0, in_bytes)
+    if not inplace:
+        ctypes.memset(hout, 0, out_bytes)
     if kind == "c2c":
         p = g.plan_many_dft(shape, howmany, hin, hout, -1, g.FFTW_ESTIMATE, prec)
         ex = lambda: p.execute_dft(hin, hout)
@@ -549,17 +551,23 @@ def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
         ex = lambda: p.execute_dft_r2c(hin, hout)
     ex()
     steps = max(2, min(args.steps, 5))
-    t0 = time.perf_counter()
+    each = []
     for _ in range(steps):
+        t0 = time.perf_counter()
         ex()
-    dt = (time.perf_counter() - t0) / steps
+        each.append(time.perf_counter() - t0)
+    dt = sum(each) / steps
+    path = ("direct host access" if len(p.passes()) == 1 else
+            "pipelined chunk staging" if howmany >= 2 else "staged copies around the passes")
     p.destroy()
     getattr(lib, pfx + "free")(hin)
     if not inplace:
         getattr(lib, pfx + "free")(hout)
     v = flops_per_step(kind, shape, howmany) / dt / 1e9
     return {"value": round(v, 2), "unit": "Gflop/s", "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": out_bytes,
-            "ms_per_step": round(dt * 1e3, 3), "timer": "host wall clock around fftwf_execute_dft (synchronous)"}
+            "ms_per_step": round(dt * 1e3, 3), "ms_min": round(min(each) * 1e3, 3), "ms_max": round(max(each) * 1e3, 3),
+            "path": path,
+            "timer": "host wall clock around fftwf_execute_dft (synchronous)"}
 
 
 def main():

@@ -126,15 +126,73 @@ template <typename C> __device__ __forceinline__ C post_twiddle(const gb_pass &P
      return w;
 }
 
+/* Column tiles with a power-of-two tb that divides the CTA: each thread
+ * keeps one column t = threadIdx mod tb for the whole tile and walks its
+ * rows j = threadIdx / tb, j + J, j + 2J, ... (J = threads / tb) with one
+ * pointer that advances by J rows, so a load costs a pointer add and a
+ * compare instead of a division-free but 64-bit index computation.
+ * Eight loads are in flight per thread before their shared-memory stores. */
+template <typename C, bool PADDED>
+__device__ __forceinline__ void cols_load(const gb_pass &P, const void *in, C *sm, int sms, const tile_t &tl, int L,
+                                          int nfft)
+{
+     constexpr int U = 4;
+     const int t = threadIdx.x & (P.tb - 1);
+     const int j0 = threadIdx.x >> P.ltb;
+     const int J = blockDim.x >> P.ltb;
+     const long long v = tl.v0 + t;
+     if (v >= P.vn[0]) return;
+     const C *src = (const C *)in + tl.bi + v * P.vis[0] + (long long)j0 * P.is;
+     const long long sj = (long long)J * P.is;
+     C *dst = sm + t * sms;
+     for (int j = j0; j < L; j += U * J) {
+          C x[U];
+          const C *q = src;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+               if (j + u * J < L) x[u] = *q;
+               q += sj;
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+               const int jj = j + u * J;
+               if (jj < L) dst[PADDED ? pad_for(nfft, jj) : jj] = x[u];
+          }
+          src += U * sj;
+     }
+}
+
+template <typename C, bool PADDED>
+__device__ __forceinline__ void cols_store(const gb_pass &P, void *out, const C *sm, int sms, const tile_t &tl, int L,
+                                           int nfft)
+{
+     const int t = threadIdx.x & (P.tb - 1);
+     const int j0 = threadIdx.x >> P.ltb;
+     const int J = blockDim.x >> P.ltb;
+     const long long v = tl.v0 + t;
+     if (v >= P.vn[0]) return;
+     C *dst = (C *)out + tl.bo + v * P.vos[0] + (long long)j0 * P.os;
+     const long long sj = (long long)J * P.os;
+     const C *src = sm + t * sms;
+     for (int j = j0; j < L; j += J) {
+          *dst = src[PADDED ? pad_for(nfft, j) : j];
+          dst += sj;
+     }
+}
+
 /* Cooperative copy of L complex elements per transform between HBM and
  * shared memory, for the tb transforms of one tile.  ROWS walks the element
  * index fastest (unit-stride transforms); COLS walks the transform index
  * fastest (transforms adjacent in memory, e.g. columns of a row-major
  * array).  PADDED applies the k_reg shared-memory swizzle. */
-template <typename C, bool PADDED, bool PAIRS_REAL>
+template <typename C, bool PADDED, bool PAIRS_REAL, bool COLS_FAST = true>
 __device__ __forceinline__ void coop_load(const gb_pass &P, const void *in, C *sm, int sms, const tile_t &tl,
                                           int L, int mode, int nfft = 0)
 {
+     if (COLS_FAST && !PAIRS_REAL && mode == GB_MOVE_COLS && P.ltb >= 0 && (blockDim.x & (P.tb - 1)) == 0) {
+          cols_load<C, PADDED>(P, in, sm, sms, tl, L, nfft);
+          return;
+     }
      /* eight loads in flight per thread before their shared-memory stores, so
       * the memory latency is paid once per batch instead of once per element */
      constexpr int U = 8;
@@ -167,10 +225,14 @@ __device__ __forceinline__ void coop_load(const gb_pass &P, const void *in, C *s
      }
 }
 
-template <typename C, bool PADDED, bool PAIRS_REAL>
+template <typename C, bool PADDED, bool PAIRS_REAL, bool COLS_FAST = true>
 __device__ __forceinline__ void coop_store(const gb_pass &P, void *out, const C *sm, int sms, const tile_t &tl,
                                            int L, int mode, int nfft = 0)
 {
+     if (COLS_FAST && !PAIRS_REAL && mode == GB_MOVE_COLS && P.ltb >= 0 && (blockDim.x & (P.tb - 1)) == 0) {
+          cols_store<C, PADDED>(P, out, sm, sms, tl, L, nfft);
+          return;
+     }
      const int tb = P.tb;
      const int total = tb * L;
      for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
@@ -346,7 +408,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
                          x[e] = a;
                     }
                } else {
-                    coop_load<C, true, false>(P, in, sm, SMS, tile, nn, P.load_mode, N);
+                    coop_load<C, true, false, (N <= 8192 && sizeof(C) == 8 && KIND == GB_KIND_C2C)>(P, in, sm, SMS, tile, nn, P.load_mode, N);
                     __syncthreads();
 #pragma unroll
                     for (int e = 0; e < E; ++e) {
@@ -377,7 +439,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
 #pragma unroll
                     for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
                     __syncthreads();
-                    coop_store<C, true, false>(P, out, sm, SMS, tile, nn, P.store_mode, N);
+                    coop_store<C, true, false, (N <= 8192 && sizeof(C) == 8 && KIND == GB_KIND_C2C)>(P, out, sm, SMS, tile, nn, P.store_mode, N);
                     __syncthreads();
                }
                continue;
@@ -387,7 +449,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
           if constexpr (KIND == GB_KIND_C2R) {
                /* X[0..N] -> shared, then Z'[k] = (X[k] + conj X[N-k])
                 *                 + i conj(W_2N^k) (X[k] - conj X[N-k])  */
-               coop_load<C, true, false>(P, in, sm, SMS, tile, N + 1, P.load_mode, N);
+               coop_load<C, true, false, (N <= 8192 && sizeof(C) == 8 && KIND == GB_KIND_C2C)>(P, in, sm, SMS, tile, N + 1, P.load_mode, N);
                __syncthreads();
                const C *__restrict__ th = (const C *)P.tw_half;
 #pragma unroll
@@ -416,7 +478,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
                     for (int e = 0; e < E; ++e) x[e] = mk<C>(0, 0);
                }
           } else {
-               coop_load<C, true, KIND == GB_KIND_R2C>(P, in, sm, SMS, tile, N, P.load_mode, N);
+               coop_load<C, true, KIND == GB_KIND_R2C, (N <= 8192 && sizeof(C) == 8 && KIND == GB_KIND_C2C)>(P, in, sm, SMS, tile, N, P.load_mode, N);
                __syncthreads();
 #pragma unroll
                for (int e = 0; e < E; ++e) x[e] = smt[pad_for(N, tid + T * e)];
@@ -457,7 +519,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
                     for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
                     if (tid == 0) smt[pad_for(N, N)] = mk<C>(last.x - last.y, 0);
                     __syncthreads();
-                    coop_store<C, true, false>(P, out, sm, SMS, tile, N + 1, P.store_mode, N);
+                    coop_store<C, true, false, (N <= 8192 && sizeof(C) == 8 && KIND == GB_KIND_C2C)>(P, out, sm, SMS, tile, N + 1, P.store_mode, N);
                     __syncthreads();
                }
           } else {
@@ -481,7 +543,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
 #pragma unroll
                     for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
                     __syncthreads();
-                    coop_store<C, true, RP>(P, out, sm, SMS, tile, N, P.store_mode, N);
+                    coop_store<C, true, RP, (N <= 8192 && sizeof(C) == 8 && KIND == GB_KIND_C2C)>(P, out, sm, SMS, tile, N, P.store_mode, N);
                     __syncthreads();
                }
           }
