@@ -1,0 +1,197 @@
+/*
+ * k_cols_tma: persistent kernel for f32 c2c column tiles (tb transforms
+ * adjacent in memory, elements at stride is) fed by the TMA engine through
+ * a tensor map: the passes along the strided axes of multi-dimensional
+ * plans and the passes of the four-step split of long 1D lengths.
+ *
+ * The tensor map views the pass input as [outer dims][row j < N][column];
+ * one tile is tb columns x N rows, fetched as boxes of at most 16 columns
+ * (128 bytes) x 256 rows with cp.async.bulk.tensor into one of two shared
+ * slots while the tile in the other slot is transformed.  The boxes land
+ * row-major with the 16-byte-chunk swizzle that matches their row width
+ * (32/64/128 bytes), so the transform-major gather that follows touches
+ * eight different 16-byte chunks per eight consecutive rows.  From there the
+ * tile runs through the same register stages as k_reg (radix 16, shared
+ * exchanges in the slot), the four-step twiddle if any, and is stored
+ * directly (unit output stride) or as column tiles.
+ *
+ * Every wait on a slot is bounded (2 s of wall time); a copy that never
+ * completes sets GB_STATUS_COPY_TIMEOUT and the CTA returns.
+ */
+#include <cuda.h>
+#include "fft_kernels.cuh"
+
+namespace gb {
+
+/* columns per box: 16 (128-byte rows) or the whole tile when narrower */
+__host__ __device__ constexpr int ct_cb(int tb) { return tb < 16 ? tb : 16; }
+
+/* bytes of one slot: the tile as boxes, or the k_reg exchange layout */
+__host__ __device__ inline int ct_slot_bytes(int nfft, int tb)
+{
+     const int a = nfft * tb * 8, b = tb * reg_sms(nfft) * 8;
+     return a > b ? a : b;
+}
+
+/* 16-byte chunk swizzle of a box with rows of cb * 8 bytes (the tensor
+ * map's 32B / 64B / 128B mode): chunk bits [4, 4+k) ^= offset bits [7, 7+k) */
+__device__ __forceinline__ int ct_swz(int o, int mask) { return o ^ (((o >> 7) & mask) << 4); }
+
+__device__ __forceinline__ void tma_tile_load(void *dst, const CUtensorMap *tm, int rank, const int *c,
+                                              unsigned long long *bar)
+{
+     const unsigned d = smem_u32(dst), b = smem_u32(bar);
+     const unsigned long long t = (unsigned long long)tm;
+     switch (rank) {
+     case 2:
+          asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                       ::"r"(d), "l"(t), "r"(c[0]), "r"(c[1]), "r"(b) : "memory");
+          break;
+     case 3:
+          asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+                       ::"r"(d), "l"(t), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(b) : "memory");
+          break;
+     case 4:
+          asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+                       ::"r"(d), "l"(t), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(b) : "memory");
+          break;
+     default:
+          asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                       ::"r"(d), "l"(t), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(b) : "memory");
+          break;
+     }
+}
+
+/* Issue the boxes of tile blk into slot dst (thread 0 only). */
+template <int N>
+__device__ __forceinline__ void ct_issue(const gb_pass &P, const CUtensorMap *tm, long long blk, unsigned char *dst,
+                                         unsigned long long *bar)
+{
+     constexpr int ROWS = N < 256 ? N : 256;
+     const int tb = P.tb, cb = ct_cb(tb);
+     int c[5] = {0, 0, 0, 0, 0};
+     long long rest = blk / P.ntiles0;
+     c[0] = (int)((blk - rest * P.ntiles0) * tb);
+     for (int d = 1; d < P.nv; ++d) {
+          const long long q = rest / P.vn[d];
+          c[1 + d] = (int)(rest - q * P.vn[d]);
+          rest = q;
+     }
+     mbar_expect_tx(bar, (unsigned)(tb * N * 8));
+     const int c0 = c[0];
+     for (int k = 0; k < tb / cb; ++k)
+          for (int r = 0; r < N / ROWS; ++r) {
+               c[0] = c0 + k * cb;
+               c[1] = r * ROWS;
+               tma_tile_load(dst + (k * N + r * ROWS) * cb * 8, tm, 1 + P.nv, c, bar);
+          }
+}
+
+template <int LOGN, int DIR>
+__global__ void __launch_bounds__(256, 3)
+k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out, const __grid_constant__ CUtensorMap tmap)
+{
+     typedef float2 C;
+     constexpr int N = 1 << LOGN;
+     constexpr int E = reg_e(N);
+     constexpr int T = N / E;
+     constexpr int SMS = reg_sms(N);
+     extern __shared__ __align__(1024) unsigned char gb_smem[];
+     __shared__ __align__(8) unsigned long long bar[2];
+     const int tb = P.tb, cb = ct_cb(tb);
+     const int mask = cb >= 16 ? 7 : cb == 8 ? 3 : cb == 4 ? 1 : 0;
+     /* slots on 1024-byte boundaries (the swizzle pattern's period) */
+     unsigned char *base = (unsigned char *)(((unsigned long long)gb_smem + 1023) & ~1023ull);
+     const int sb = (ct_slot_bytes(N, tb) + 1023) & ~1023;
+     unsigned char *const s0 = base, *const s1 = base + sb;
+     const int tl = threadIdx.x / T;
+     const int tid = threadIdx.x - tl * T;
+     const C *__restrict__ tw = (const C *)P.tw;
+
+     if (threadIdx.x == 0) {
+          mbar_init(&bar[0], 1);
+          mbar_init(&bar[1], 1);
+          mbar_fence_init();
+     }
+     __syncthreads();
+     const long long stride = gridDim.x;
+     long long blk = blockIdx.x;
+     if (threadIdx.x == 0 && blk < P.nblocks) ct_issue<N>(P, &tmap, blk, s0, &bar[0]);
+     unsigned parity = 0;
+
+     for (int it = 0; blk < P.nblocks; blk += stride, ++it) {
+          const int b = it & 1;
+          unsigned char *const cur = b ? s1 : s0;
+          const long long nxt = blk + stride;
+          const bool issued = nxt < P.nblocks;
+          if (threadIdx.x == 0 && issued) {
+               fence_proxy_async_smem();
+               ct_issue<N>(P, &tmap, nxt, b ? s0 : s1, &bar[b ^ 1]);
+          }
+          const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u, GB_WAIT_NS);
+          if (!__syncthreads_and(ok)) {
+               if (threadIdx.x == 0) {
+                    if (issued) mbar_wait(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u, GB_WAIT_NS);
+                    if (P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
+               }
+               return;
+          }
+          parity ^= 1u << b;
+
+          const tile_t tile = tile_of(P, blk);
+          const long long v = tile.v0 + tl;
+          const bool valid = v < P.vn[0];
+          /* element j of column tl: box tl / cb, row j, chunk-swizzled */
+          const int colbase = (tl / cb) * N * cb * 8 + (tl % cb) * 8;
+          C x[E];
+#pragma unroll
+          for (int e = 0; e < E; ++e) {
+               const int o = colbase + (tid + T * e) * cb * 8;
+               x[e] = *(const C *)(cur + ct_swz(o, mask));
+          }
+          __syncthreads();
+          C *const sm = (C *)cur;
+          C *const smt = sm + tl * SMS;
+          reg_stages<C, N, DIR, 1>(x, tid, smt, tw);
+          if (P.post_N) {
+#pragma unroll
+               for (int e = 0; e < E; ++e)
+                    x[e] = cmul(x[e], post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)(tid + T * e)));
+          }
+          if (P.store_mode == GB_MOVE_DIRECT) {
+               if (valid) {
+                    const long long bo = tile.bo + v * P.vos[0];
+#pragma unroll
+                    for (int e = 0; e < E; ++e) io<C>::stc(out, bo, tid + T * e, P.os, x[e]);
+               }
+          } else {
+#pragma unroll
+               for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
+               __syncthreads();
+               coop_store<C, true, false>(P, out, sm, SMS, tile, N, P.store_mode, N);
+          }
+          __syncthreads();   /* the slot is the target of a later tile's boxes */
+     }
+}
+
+template <int L>
+static const void *ct_lookup(int logn, int dir)
+{
+     if constexpr (L > 11) return 0;
+     else {
+          if (logn == L) return dir < 0 ? (const void *)k_cols_tma<L, -1> : (const void *)k_cols_tma<L, 1>;
+          return ct_lookup<L + 1>(logn, dir);
+     }
+}
+
+} /* namespace gb */
+
+extern "C" const void *gb_cols_tma_kernel(int logn, int dir) { return gb::ct_lookup<4>(logn, dir); }
+
+/* Shared memory of a k_cols_tma CTA: two slots on 1024-byte boundaries and
+ * the slack to align the first one. */
+extern "C" int gb_cols_tma_smem(int nfft, int tb)
+{
+     const int sb = (gb::ct_slot_bytes(nfft, tb) + 1023) & ~1023;
+     return sb + gb::ct_slot_bytes(nfft, tb) + 1024;
+}

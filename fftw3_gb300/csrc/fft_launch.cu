@@ -7,8 +7,11 @@
  * each factor is computed in FP64 with an exact integer argument reduction
  * and rounded once to the working precision.
  */
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
 #include "fft_kernels.cuh"
@@ -18,6 +21,7 @@ extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
 extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir);
 extern "C" const void *gb_tma_kernel_d(int logn, int kind, int dir);
 extern "C" const void *gb_tc_kernel(int nfft, int dir);
+extern "C" const void *gb_cols_tma_kernel(int logn, int dir);
 extern "C" int gb_tc_smem(int nfft);
 
 namespace gb {
@@ -129,6 +133,8 @@ __global__ void __launch_bounds__(256) k_pointwise(const gb_pass P, const void *
 using namespace gb;
 
 static __thread char gb_errbuf[256];
+/* FFTW_GB300_TRACE set: every launch is logged with its grid */
+static const int gb_trace = getenv("FFTW_GB300_TRACE") != 0;
 static unsigned long long gb_launches = 0;
 
 extern "C" long long gb_launch_count(void) { return (long long)__atomic_load_n(&gb_launches, __ATOMIC_RELAXED); }
@@ -196,6 +202,11 @@ static const void *pick_kernel(const gb_pass *p)
      if (p->kind == GB_KIND_COPY)
           return p->prec == 4 ? (const void *)k_copy<float2> : (const void *)k_copy<double2>;
      if (p->variant == GB_VAR_TC) return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_tc_kernel(p->nfft, p->sign) : 0;
+     if (p->variant == GB_VAR_TMA_COLS) {
+          int logn = 0;
+          while ((1 << logn) < p->nfft) ++logn;
+          return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_cols_tma_kernel(logn, p->sign) : 0;
+     }
      if (p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA) {
           int logn = 0;
           while ((1 << logn) < p->nfft) ++logn;
@@ -214,11 +225,14 @@ static const void *pick_kernel(const gb_pass *p)
 static unsigned grid_of(const gb_pass *p, const void *fn)
 {
      long long g = p->nblocks;
-     if (p->variant == GB_VAR_TMA || p->variant == GB_VAR_TC) {
+     if (p->variant == GB_VAR_TMA || p->variant == GB_VAR_TC || p->variant == GB_VAR_TMA_COLS) {
           int dev = 0, sms = 0, per = 0;
           cudaGetDevice(&dev);
           cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-          if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, p->threads, (size_t)p->smem) != cudaSuccess) {
+          const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, p->threads, (size_t)p->smem);
+          if (gb_trace)
+               fprintf(stderr, "[fftw_gb300] occupancy of variant %d: %d CTAs/SM (%s)\n", p->variant, per, cudaGetErrorString(e));
+          if (e != cudaSuccess) {
                cudaGetLastError();
                per = 1;
           }
@@ -252,6 +266,64 @@ extern "C" int gb_device_status(void)
      return v;
 }
 
+/* ---- tensor maps for column tiles (k_cols_tma) ---- */
+
+static PFN_cuTensorMapEncodeTiled_v12000 gb_encode_tiled = 0;
+
+/* Plan-time and launch-time conditions of a tensor-map column pass: the
+ * tensor map views the input as [outer dims][N rows at stride is][columns]
+ * with 8-byte elements, so every stride must be a positive multiple of 16
+ * bytes and the base 16-byte aligned; boxes are at most 16 columns x 256
+ * rows. */
+static int cols_tma_ok(const gb_pass *p, const void *in)
+{
+     int d;
+     const int T = p->nfft / reg_e(p->nfft);
+     if (p->kind != GB_KIND_C2C || p->prec != 4 || p->load_mode != GB_MOVE_COLS) return 0;
+     if (p->nfft < 16 || p->nfft > 2048 || p->tb < 2 || p->tb > 64 || (p->tb & (p->tb - 1)) || p->ltb < 0) return 0;
+     if (p->threads != p->tb * T || p->threads > 256 || p->nv > 4) return 0;
+     if (p->smem < gb_cols_tma_smem(p->nfft, p->tb)) return 0;
+     if ((uintptr_t)in % 16 || p->vis[0] != 1 || p->is <= 0 || (p->is * 8) % 16 || p->is * 8 >= (1LL << 40)) return 0;
+     if (p->vn[0] >= (1LL << 31)) return 0;
+     for (d = 1; d < p->nv; ++d)
+          if (p->vis[d] <= 0 || (p->vis[d] * 8) % 16 || p->vis[d] * 8 >= (1LL << 40) || p->vn[d] >= (1LL << 31)) return 0;
+     return 1;
+}
+
+extern "C" int gb_cols_tma_plan_ok(const gb_pass *p) { return cols_tma_ok(p, (const void *)0); }
+
+static int encode_cols_map(CUtensorMap *tm, const gb_pass *p, const void *in)
+{
+     cuuint64_t gdim[5], gstr[4];
+     cuuint32_t box[5] = {1, 1, 1, 1, 1}, es[5] = {1, 1, 1, 1, 1};
+     const int cb = p->tb < 16 ? p->tb : 16, rank = 1 + p->nv;
+     CUtensorMapSwizzle sw = cb == 16 ? CU_TENSOR_MAP_SWIZZLE_128B : cb == 8 ? CU_TENSOR_MAP_SWIZZLE_64B
+                           : cb == 4 ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_NONE;
+     int d;
+     if (!gb_encode_tiled) {
+          void *fp = 0;
+          cudaDriverEntryPointQueryResult q;
+          if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fp, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+              q != cudaDriverEntryPointSuccess || !fp) {
+               cudaGetLastError();
+               return -1;
+          }
+          gb_encode_tiled = (PFN_cuTensorMapEncodeTiled_v12000)fp;
+     }
+     gdim[0] = (cuuint64_t)p->vn[0];
+     gdim[1] = (cuuint64_t)p->nfft;
+     gstr[0] = (cuuint64_t)p->is * 8;
+     for (d = 1; d < p->nv; ++d) {
+          gdim[1 + d] = (cuuint64_t)p->vn[d];
+          gstr[d] = (cuuint64_t)p->vis[d] * 8;
+     }
+     box[0] = (cuuint32_t)cb;
+     box[1] = (cuuint32_t)(p->nfft < 256 ? p->nfft : 256);
+     return gb_encode_tiled(tm, CU_TENSOR_MAP_DATA_TYPE_INT64, (cuuint32_t)rank, (void *)in, gdim, gstr, box, es,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS ? 0 : -1;
+}
+
 extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void *stream)
 {
      const void *fn = pick_kernel(p);
@@ -280,7 +352,8 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->post_vdim < 0 || p->post_vdim >= p->nv || (p->post_vdim && !p->post_N))
                bad = "four-step twiddle dimension is not a vector dimension of the pass";
           else if (p->threads < 1 || p->threads > 1024 || p->tb < 1 || p->nv < 1 || p->nv > GB_MAXV) bad = "bad launch shape";
-          else if ((p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA) && p->kind != GB_KIND_COPY &&
+          else if ((p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA || p->variant == GB_VAR_TMA_COLS) &&
+                   p->kind != GB_KIND_COPY &&
                    p->threads != p->tb * (p->nfft / reg_e(p->nfft))) bad = "thread count does not match the tile";
           else if (p->variant == GB_VAR_REG && p->threads > reg_maxthreads(p->nfft)) bad = "tile exceeds the kernel's launch bounds";
           else if (reg_sms(p->nfft) != gb_reg_sms(p->nfft)) bad = "host and device shared-memory layouts disagree";
@@ -294,6 +367,9 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
                                                 p->smem < 2 * p->tb * tma_sms(p->nfft) * 2 * p->prec))
                bad = "persistent bulk-copy pass needs unit-stride c2c/r2c in and out and two smem slots";
           else if (p->variant == GB_VAR_TMA && ((uintptr_t)in % 16 != 0)) bad = "bulk copies need a 16-byte aligned input";
+          else if (p->variant == GB_VAR_TMA_COLS && !cols_tma_ok(p, in))
+               bad = "tensor-map column pass needs f32 c2c column tiles of 2..64 columns, 16..2048 points, even positive "
+                     "strides, a 16-byte aligned input and two shared slots";
           else if (p->variant == GB_VAR_TC && (p->prec != 4 || (p->nfft != 256 && p->nfft != 4096) ||
                                                p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||
                                                p->smem < gb_tc_smem(p->nfft) || (p->store_mode == GB_MOVE_DIRECT && p->os != 1)))
@@ -310,9 +386,26 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
      }
      gb_pass pv = *p;
      if (!pv.status) pv.status = gb_device_status_ptr();
-     void *args[3] = {(void *)&pv, (void *)&in, (void *)&out};
-     cudaError_t e = cudaLaunchKernel(fn, dim3(grid_of(p, fn)), dim3(p->threads), args, (size_t)p->smem,
-                                      (cudaStream_t)stream);
+     CUtensorMap tmap;
+     void *args[4] = {(void *)&pv, (void *)&in, (void *)&out, (void *)&tmap};
+     if (p->variant == GB_VAR_TMA_COLS && encode_cols_map(&tmap, p, in)) {
+          /* the driver refused this view of the array: same tile through
+           * the register kernel's plain loads */
+          pv.variant = GB_VAR_REG;
+          pv.smem = p->tb * reg_sms(p->nfft) * 2 * p->prec;
+          fn = pick_kernel(&pv);
+          if (!fn) return -1;
+          if (pv.smem > 48 * 1024 &&
+              gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pv.smem),
+                       "cudaFuncSetAttribute(max dynamic smem)"))
+               return -1;
+          p = &pv;
+     }
+     const unsigned grid = grid_of(p, fn);
+     if (gb_trace)
+          fprintf(stderr, "[fftw_gb300] launch kind %d variant %d nfft %d tb %d: grid %u x %d threads, %d B smem\n",
+                  p->kind, p->variant, p->nfft, p->tb, grid, p->threads, p->smem);
+     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(p->threads), args, (size_t)pv.smem, (cudaStream_t)stream);
      __atomic_add_fetch(&gb_launches, 1ull, __ATOMIC_RELAXED);
      return gb_check(e, "kernel launch");
 }

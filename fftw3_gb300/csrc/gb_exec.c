@@ -109,6 +109,11 @@ static int run_step(const gb_plan *p, const gb_step *s, char *bufs[4], int esz[4
           if (s->dst_off % 2) ok = 0;
           P.real_pairs = ok;
      }
+     if (P.variant == GB_VAR_TMA_COLS && (direct_host || ((uintptr_t)(bufs[si] + s->src_off * esz[si]) % 16) || s->nloop)) {
+          /* host memory or an input not 16-byte aligned: same tile, plain loads */
+          P.variant = GB_VAR_REG;
+          P.smem = P.tb * gb_reg_sms(P.nfft) * 2 * P.prec;
+     }
      if (P.variant == GB_VAR_TMA && (direct_host || ((uintptr_t)(bufs[si] + s->src_off * esz[si]) % 16))) {
           /* host memory or an input not 16-byte aligned: same tile, plain loads
            * (register kernel) instead of bulk copies */

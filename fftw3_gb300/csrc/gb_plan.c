@@ -400,6 +400,21 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
           else P->store_mode = GB_MOVE_DIRECT;
           if (kind == GB_KIND_R2C && P->store_mode == GB_MOVE_DIRECT && llabs_(os) == 1 && T < 32)
                P->store_mode = GB_MOVE_ROWS;
+          /* f32 c2c column tiles whose strides the TMA engine can walk:
+           * persistent CTAs fed by tensor-map boxes (k_cols_tma) */
+          if (kind == GB_KIND_C2C && prec == 4 && P->load_mode == GB_MOVE_COLS && !cfg_no_tma &&
+              !getenv("FFTW_GB300_NO_TMA")) {
+               gb_pass t = *P;
+               int l = 0;
+               while ((1 << l) < tb) ++l;
+               t.ltb = ((1 << l) == tb) ? l : -1;
+               t.variant = GB_VAR_TMA_COLS;
+               t.smem = gb_cols_tma_smem((int)nfft, tb);
+               if (t.smem <= smax && gb_cols_tma_plan_ok(&t)) {
+                    P->variant = GB_VAR_TMA_COLS;
+                    P->smem = t.smem;
+               }
+          }
           /* unit-stride c2c with 16-byte aligned transform starts: persistent
            * CTAs fed by bulk async copies (k_reg_tma) */
           if ((kind == GB_KIND_C2C || kind == GB_KIND_R2C) && is == 1 && os == 1 && nfft >= 64 && nfft <= 8192 &&
@@ -929,6 +944,7 @@ static void describe(gb_plan *p)
           off += snprintf(p->desc + off, sizeof p->desc - off,
                           "\n  (pass %s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
                           kk[P->kind], P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" :
+                          P->variant == GB_VAR_TMA_COLS ? "cols-tma" :
                           P->variant == GB_VAR_TC ? "tc-split-fp16" : "gen", P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
                           P->vn[0], P->post_N ? " +twiddle" : "");

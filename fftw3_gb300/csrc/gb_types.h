@@ -45,7 +45,8 @@ enum gb_variant {
      GB_VAR_REG = 0,   /* power-of-two length, register-resident Stockham stages of radix <= 16 */
      GB_VAR_GEN = 1,   /* any smooth length, shared-memory Stockham stages, runtime radix list */
      GB_VAR_TMA = 2,   /* as GB_VAR_REG, persistent CTAs fed by bulk async copies (unit-stride c2c) */
-     GB_VAR_TC = 3     /* radix-16 stages as split-FP16 tcgen05 GEMMs (nfft 256 or 4096, f32, unit stride) */
+     GB_VAR_TC = 3,    /* radix-16 stages as split-FP16 tcgen05 GEMMs (nfft 256 or 4096, f32, unit stride) */
+     GB_VAR_TMA_COLS = 4   /* as GB_VAR_REG for f32 c2c column tiles, persistent CTAs fed by tensor-map TMA boxes */
 };
 
 /* How a tile of transforms moves between HBM and the CTA. */
@@ -141,6 +142,8 @@ int gb_launch_queue(const gb_qitem *items, int nitems, int *head, int *ctrs, int
 int gb_queue_grid(int prec, int threads, int smem);
 int gb_pass_configure(gb_pass *p, int max_smem_optin);
 int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream);
+int gb_cols_tma_smem(int nfft, int tb);
+int gb_cols_tma_plan_ok(const gb_pass *p);
 int gb_chirp(void *dst, int prec, long long n, int sign, void *stream);
 int gb_device_max_smem(void);
 const char *gb_last_cuda_error(void);
