@@ -96,14 +96,16 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
      constexpr int E = reg_e(N);
      constexpr int T = N / E;
      constexpr int SMS = reg_sms(N);
+     /* no static shared memory (it would be padded to 1 KB and cost the third
+      * CTA per SM): slots and barriers all live in the dynamic allocation */
      extern __shared__ __align__(1024) unsigned char gb_smem[];
-     __shared__ __align__(8) unsigned long long bar[2];
      const int tb = P.tb, cb = ct_cb(tb);
      const int mask = cb >= 16 ? 7 : cb == 8 ? 3 : cb == 4 ? 1 : 0;
      /* slots on 1024-byte boundaries (the swizzle pattern's period) */
      unsigned char *base = (unsigned char *)(((unsigned long long)gb_smem + 1023) & ~1023ull);
      const int sb = (ct_slot_bytes(N, tb) + 1023) & ~1023;
      unsigned char *const s0 = base, *const s1 = base + sb;
+     unsigned long long *const bar = (unsigned long long *)(s1 + ((ct_slot_bytes(N, tb) + 15) & ~15));
      const int tl = threadIdx.x / T;
      const int tid = threadIdx.x - tl * T;
      const C *__restrict__ tw = (const C *)P.tw;
@@ -188,10 +190,10 @@ static const void *ct_lookup(int logn, int dir)
 
 extern "C" const void *gb_cols_tma_kernel(int logn, int dir) { return gb::ct_lookup<4>(logn, dir); }
 
-/* Shared memory of a k_cols_tma CTA: two slots on 1024-byte boundaries and
- * the slack to align the first one. */
+/* Shared memory of a k_cols_tma CTA: two slots on 1024-byte boundaries, the
+ * two mbarriers, and the slack to align the first slot. */
 extern "C" int gb_cols_tma_smem(int nfft, int tb)
 {
      const int sb = (gb::ct_slot_bytes(nfft, tb) + 1023) & ~1023;
-     return sb + gb::ct_slot_bytes(nfft, tb) + 1024;
+     return sb + ((gb::ct_slot_bytes(nfft, tb) + 15) & ~15) + 16 + 1024;
 }

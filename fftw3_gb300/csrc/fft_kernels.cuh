@@ -69,9 +69,27 @@ struct tile_t {
 __device__ __forceinline__ tile_t tile_of(const gb_pass &P, long long blk)
 {
      tile_t t;
+     t.bi = 0; t.bo = 0; t.vpost = 0;
+     if (P.nblocks <= 0x7fffffffLL) {
+          /* every index fits 32 bits: 32-bit divisions, a few times cheaper
+           * than the 64-bit ones every thread would otherwise run per tile */
+          unsigned rest = (unsigned)blk / (unsigned)P.ntiles0;
+          t.v0 = (long long)((unsigned)blk - rest * (unsigned)P.ntiles0) * P.tb;
+#pragma unroll
+          for (int d = 1; d < GB_MAXV; ++d) {
+               if (d < P.nv) {
+                    const unsigned q = rest / (unsigned)P.vn[d];
+                    const long long i = rest - q * (unsigned)P.vn[d];
+                    rest = q;
+                    t.bi += i * P.vis[d];
+                    t.bo += i * P.vos[d];
+                    if (d == P.post_vdim) t.vpost = i;
+               }
+          }
+          return t;
+     }
      long long rest = blk / P.ntiles0;
      t.v0 = (blk - rest * P.ntiles0) * P.tb;
-     t.bi = 0; t.bo = 0; t.vpost = 0;
 #pragma unroll
      for (int d = 1; d < GB_MAXV; ++d) {
           if (d < P.nv) {

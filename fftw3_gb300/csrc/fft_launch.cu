@@ -236,6 +236,11 @@ static unsigned grid_of(const gb_pass *p, const void *fn)
                cudaGetLastError();
                per = 1;
           }
+          /* the calculator reports one CTA per SM for the tensor-core kernel,
+           * whose shared memory (and TMEM: 64 columns) leaves room for two;
+           * its CTAs never wait on one another, so a second wave is harmless
+           * if they cannot all be resident */
+          if (p->variant == GB_VAR_TC && per < 2) per = 2;
           if (per < 1) per = 1;
           if (g > (long long)per * sms) g = (long long)per * sms;
      }
@@ -382,6 +387,12 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
      if (p->smem > 48 * 1024) {
           if (gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, p->smem),
                        "cudaFuncSetAttribute(max dynamic smem)"))
+               return -1;
+          /* largest shared-memory carveout, so the occupancy the grid is sized
+           * for (persistent kernels) is the one the SMs are configured for */
+          if (gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                            cudaSharedmemCarveoutMaxShared),
+                       "cudaFuncSetAttribute(shared memory carveout)"))
                return -1;
      }
      gb_pass pv = *p;
