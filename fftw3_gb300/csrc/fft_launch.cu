@@ -237,10 +237,10 @@ static unsigned grid_of(const gb_pass *p, const void *fn)
                per = 1;
           }
           /* the calculator reports one CTA per SM for the tensor-core kernel,
-           * whose shared memory (and TMEM: 64 columns) leaves room for two;
-           * its CTAs never wait on one another, so a second wave is harmless
-           * if they cannot all be resident */
-          if (p->variant == GB_VAR_TC && per < 2) per = 2;
+           * whose registers, shared memory and TMEM (64 columns) leave room for
+           * three; its CTAs never wait on one another, so a second wave is
+           * harmless if they cannot all be resident */
+          if (p->variant == GB_VAR_TC && per < 3) per = 3;
           if (per < 1) per = 1;
           if (g > (long long)per * sms) g = (long long)per * sms;
      }

@@ -100,7 +100,10 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
      __shared__ __align__(8) unsigned long long bar;
      unsigned char *As = sm;                           /* 2 groups x 24 KB */
      unsigned char *Bs = sm + 2 * TC_A_BYTES;          /* 6 KB */
-     float2 *dat = (float2 *)(Bs + TC_B_BYTES);        /* TB x N complex */
+     /* the tile (TB x N complex, 32 KB) shares the A operand's 48 KB: a
+      * stage reads it into registers before A is written, and the MMA has
+      * completed before the stage's results are written back */
+     float2 *dat = (float2 *)As;
      const float2 *__restrict__ tw = (const float2 *)P.tw;
      const int m = threadIdx.x;          /* butterfly row */
      const int tl = m / T, j = m - tl * T;
@@ -157,6 +160,8 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
 #pragma unroll
                for (int r = 0; r < 16; ++r) mx = fmaxf(mx, fmaxf(fabsf(x[r].x), fabsf(x[r].y)));
                const float sc = row_scale(mx), inv = 1.f / sc;
+               /* every thread has its x: the tile's memory becomes A */
+               __syncthreads();
                /* A row: [hi.re | hi.im | lo.re | lo.im | hi.re | hi.im] */
                {
                     __half hr[16], hi[16], lr[16], li[16];
@@ -265,7 +270,7 @@ extern "C" int *gb_device_status_ptr(void);
 /* bytes of dynamic shared memory the tensor-core FFT needs */
 extern "C" int gb_tc_smem(int nfft)
 {
-     return (int)(2 * TC_A_BYTES + TC_B_BYTES) + 256 * 16 * 8 + 0 * nfft;
+     return (int)(2 * TC_A_BYTES + TC_B_BYTES) + 0 * nfft;
 }
 
 extern "C" const void *gb_tc_kernel(int nfft, int dir)
