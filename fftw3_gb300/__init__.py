@@ -71,6 +71,9 @@ def _sigs(lib, pfx):
     f("plan_guru_dft_r2c", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, cu])
     f("plan_guru_dft_c2r", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, cu])
     f("plan_many_r2r", vp, [ci, ip, ci, vp, ip, ci, ci, vp, ip, ci, ci, vp, cu])
+    f("plan_guru_split_dft", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, vp, vp, cu])
+    f("plan_guru64_split_dft", vp, [ci, ctypes.POINTER(IODim64), ci, ctypes.POINTER(IODim64), vp, vp, vp, vp, cu])
+    f("execute_split_dft", None, [vp, vp, vp, vp, vp])
     f("execute", None, [vp])
     f("execute_dft", None, [vp, vp, vp])
     f("execute_dft_r2c", None, [vp, vp, vp])
@@ -171,6 +174,9 @@ class Plan:
     def execute_dft_c2r(self, i, o):
         self._f("execute_dft_c2r")(self.ptr, i, o)
 
+    def execute_split_dft(self, ri, ii, ro, io):
+        self._f("execute_split_dft")(self.ptr, ri, ii, ro, io)
+
     def set_stream(self, stream_ptr: int):
         return self._f("gb300_set_stream")(self.ptr, stream_ptr)
 
@@ -257,6 +263,16 @@ def plan_guru_dft(dims, howmany_dims, inp, out, sign=FFTW_FORWARD, flags=FFTW_ES
     d = (IODim * max(1, len(dims)))(*[IODim(*x) for x in dims])
     h = (IODim * max(1, len(howmany_dims)))(*[IODim(*x) for x in howmany_dims])
     p = getattr(lib, pfx + "plan_guru_dft")(len(dims), d, len(howmany_dims), h, inp, out, sign, flags)
+    return Plan(p, prec)
+
+
+def plan_guru_split_dft(dims, howmany_dims, ri, ii, ro, io, flags=FFTW_ESTIMATE, prec="f") -> Plan:
+    """Forward DFT of ri + i*ii into ro + i*io; (n, is, os) strides in reals."""
+    lib = load()
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    d = (IODim * max(1, len(dims)))(*[IODim(*x) for x in dims])
+    h = (IODim * max(1, len(howmany_dims)))(*[IODim(*x) for x in howmany_dims])
+    p = getattr(lib, pfx + "plan_guru_split_dft")(len(dims), d, len(howmany_dims), h, ri, ii, ro, io, flags)
     return Plan(p, prec)
 
 

@@ -23,6 +23,8 @@ CSRC = os.path.join(PKG, "csrc")
 INC = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libfftw3_gb300.so")
+# the wisdom tool (fftw-wisdom counterpart), one binary per precision
+TOOLS = {os.path.join(PKG, "fftw-wisdom-gb300"): [], os.path.join(PKG, "fftwf-wisdom-gb300"): ["-DGB_TOOL_SINGLE"]}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -38,7 +40,8 @@ def _cuda_home() -> str:
 
 
 def _newest_dep() -> float:
-    deps = glob.glob(os.path.join(CSRC, "*")) + glob.glob(os.path.join(INC, "*.h")) + [__file__]
+    deps = (glob.glob(os.path.join(CSRC, "*")) + glob.glob(os.path.join(CSRC, "cli", "*")) +
+            glob.glob(os.path.join(INC, "*.h")) + [__file__])
     return max(os.path.getmtime(d) for d in deps)
 
 
@@ -54,7 +57,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
     newest = _newest_dep()
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+    if all(os.path.exists(f) and os.path.getmtime(f) >= newest for f in [LIB, *TOOLS]):
         return LIB
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     cc = sorted(glob.glob(os.path.join(CSRC, "*.c")))
@@ -85,6 +88,10 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     _run([nvcc, "-shared", *ARCH, "-cudart=static", "-o", tmp, *objs, "-Xlinker", "-Bsymbolic-functions",
           "-lpthread", "-lm"])
     os.replace(tmp, LIB)
+    tool_src = os.path.join(CSRC, "cli", "wisdom_tool.c")
+    for exe, defs in TOOLS.items():
+        _run(["gcc", "-std=gnu11", "-O2", "-Wall", *defs, "-I", INC, tool_src, "-o", exe, "-L", PKG,
+              "-lfftw3_gb300", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -158,6 +158,57 @@ extern "C" int gb_device_max_smem(void)
      return v;
 }
 
+/* Split arrays <-> dense interleaved buffer: element L of the dense buffer
+ * (row-major over the nd dims) is (re[o], im[o]) with o = sum idx_d * s_d. */
+struct gb_split_dims {
+     int nd;
+     long long n[GB_SPLIT_MAXD], s[GB_SPLIT_MAXD];
+};
+
+template <typename R, bool PACK>
+__global__ void k_split_copy(const gb_split_dims D, long long total, R *re, R *im, void *buf)
+{
+     typedef typename cplx_of<R>::T C;
+     C *b = (C *)buf;
+     for (long long L = blockIdx.x * (long long)blockDim.x + threadIdx.x; L < total;
+          L += (long long)gridDim.x * blockDim.x) {
+          long long rest = L, o = 0;
+          for (int d = D.nd - 1; d >= 0; --d) {
+               const long long q = rest / D.n[d];
+               o += (rest - q * D.n[d]) * D.s[d];
+               rest = q;
+          }
+          if (PACK) b[L] = mk<C>(re[o], im[o]);
+          else {
+               const C v = b[L];
+               re[o] = v.x;
+               im[o] = v.y;
+          }
+     }
+}
+
+extern "C" int gb_split_copy(int pack, int prec, int nd, const long long *n, const long long *s, long long total,
+                             void *re, void *im, void *buf, void *stream)
+{
+     gb_split_dims D;
+     long long blocks = (total + 255) / 256;
+     if (nd < 0 || nd > GB_SPLIT_MAXD) return -1;
+     if (total <= 0) return 0;
+     D.nd = nd;
+     for (int d = 0; d < nd; ++d) { D.n[d] = n[d]; D.s[d] = s[d]; }
+     if (blocks > 65536) blocks = 65536;
+     cudaStream_t st = (cudaStream_t)stream;
+     if (prec == 4) {
+          if (pack) k_split_copy<float, true><<<(unsigned)blocks, 256, 0, st>>>(D, total, (float *)re, (float *)im, buf);
+          else k_split_copy<float, false><<<(unsigned)blocks, 256, 0, st>>>(D, total, (float *)re, (float *)im, buf);
+     } else {
+          if (pack) k_split_copy<double, true><<<(unsigned)blocks, 256, 0, st>>>(D, total, (double *)re, (double *)im, buf);
+          else k_split_copy<double, false><<<(unsigned)blocks, 256, 0, st>>>(D, total, (double *)re, (double *)im, buf);
+     }
+     __atomic_add_fetch(&gb_launches, 1ull, __ATOMIC_RELAXED);
+     return gb_check(cudaGetLastError(), pack ? "split pack" : "split unpack");
+}
+
 extern "C" int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream)
 {
      int blocks = (int)((count + 255) / 256);

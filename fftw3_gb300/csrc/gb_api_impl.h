@@ -16,7 +16,11 @@
  */
 
 typedef R PFX(cpx)[2];
-struct PFX(plan_s) { gb_plan *g; };
+/* view: how the plan was made — 0 complex interface; split interface as
+ * 1 interleaved (ii = ri + 1, io = ro + 1: the complex plan on ri -> ro),
+ * 2 swapped interleaved (ri = ii + 1: the backward complex plan on ii -> io),
+ * 3 general split arrays (pack, c2c, unpack) */
+struct PFX(plan_s) { gb_plan *g; int view; };
 
 static PFX(plan) PFX(wrap)(gb_plan *g)
 {
@@ -24,6 +28,7 @@ static PFX(plan) PFX(wrap)(gb_plan *g)
      if (!g) return 0;
      p = (PFX(plan))malloc(sizeof *p);
      p->g = g;
+     p->view = 0;
      return p;
 }
 
@@ -173,19 +178,77 @@ PFX(plan) PFX(plan_guru64_dft)(int rank, const PFX(iodim64) *dims, int howmany_r
      }
 }
 
+/* api/plan-guru-split-dft.h:23-38: the forward DFT of ri + i ii into
+ * ro + i io, strides in reals. */
+static PFX(plan) PFX(split_common)(int rank, const long long *dn, const long long *dis, const long long *dos,
+                                   int hrank, const long long *hn, const long long *his, const long long *hos,
+                                   R *ri, R *ii, R *ro, R *io_, unsigned flags)
+{
+     gb_dim d[GB_MAXRANK], v[GB_MAXRANK];
+     int i, even = 1;
+     if (rank < 0 || rank > GB_MAXRANK || hrank < 0 || hrank > GB_MAXRANK) return 0;
+     for (i = 0; i < rank; ++i) {
+          if (dn[i] <= 0) return 0;
+          if (dis[i] % 2 || dos[i] % 2) even = 0;
+     }
+     for (i = 0; i < hrank; ++i) {
+          if (hn[i] < 0) return 0;
+          if (his[i] % 2 || hos[i] % 2) even = 0;
+     }
+     if (even && ((ii - ri == 1 && io_ - ro == 1) || (ri - ii == 1 && ro - io_ == 1))) {
+          /* interleaved complex arrays: an ordinary plan on half the strides */
+          const int swapped = (ri - ii == 1);
+          long long a[GB_MAXRANK], b[GB_MAXRANK], c[GB_MAXRANK], e[GB_MAXRANK];
+          PFX(plan) p;
+          for (i = 0; i < rank; ++i) { a[i] = dis[i] / 2; b[i] = dos[i] / 2; }
+          for (i = 0; i < hrank; ++i) { c[i] = his[i] / 2; e[i] = hos[i] / 2; }
+          p = PFX(guru_common)(GB_PROB_DFT, rank, dn, a, b, hrank, hn, c, e, swapped ? (void *)ii : (void *)ri,
+                               swapped ? (void *)io_ : (void *)ro, swapped ? FFTW_BACKWARD : FFTW_FORWARD, flags);
+          if (p) p->view = swapped ? 2 : 1;
+          return p;
+     }
+     for (i = 0; i < rank; ++i) { d[i].n = dn[i]; d[i].is = dis[i]; d[i].os = dos[i]; }
+     for (i = 0; i < hrank; ++i) { v[i].n = hn[i]; v[i].is = his[i]; v[i].os = hos[i]; }
+     {
+          gb_plan *g;
+          PFX(plan) p;
+          if (!gb_dry_run() && !gb_cuda_ready()) {
+               gb_set_error("no CUDA device: libfftw3_gb300 runs transforms on the GPU only");
+               return 0;
+          }
+          gb_lock();
+          g = gb_mksplit((int)sizeof(R), rank, d, hrank, v, ri, ii, ro, io_, flags);
+          if (g && !(flags & FFTW_ESTIMATE) && !gb_dry_run()) gb_tune(g->split_inner, flags);
+          gb_unlock();
+          p = PFX(wrap)(g);
+          if (p) p->view = 3;
+          return p;
+     }
+}
+
 PFX(plan) PFX(plan_guru_split_dft)(int rank, const PFX(iodim) *dims, int howmany_rank,
                                    const PFX(iodim) *howmany_dims, R *ri, R *ii, R *ro, R *io_, unsigned flags)
 {
-     (void)rank; (void)dims; (void)howmany_rank; (void)howmany_dims; (void)ri; (void)ii; (void)ro; (void)io_; (void)flags;
-     gb_set_error("split-array plans are not provided by this library");
-     return 0;
+     if (rank < 0 || howmany_rank < 0) return 0;
+     {
+          GB_UNPACK(dims, rank, dn, dis, dos);
+          {
+               GB_UNPACK(howmany_dims, howmany_rank, hn, his, hos);
+               return PFX(split_common)(rank, dn, dis, dos, howmany_rank, hn, his, hos, ri, ii, ro, io_, flags);
+          }
+     }
 }
 PFX(plan) PFX(plan_guru64_split_dft)(int rank, const PFX(iodim64) *dims, int howmany_rank,
                                      const PFX(iodim64) *howmany_dims, R *ri, R *ii, R *ro, R *io_, unsigned flags)
 {
-     (void)rank; (void)dims; (void)howmany_rank; (void)howmany_dims; (void)ri; (void)ii; (void)ro; (void)io_; (void)flags;
-     gb_set_error("split-array plans are not provided by this library");
-     return 0;
+     if (rank < 0 || howmany_rank < 0) return 0;
+     {
+          GB_UNPACK(dims, rank, dn, dis, dos);
+          {
+               GB_UNPACK(howmany_dims, howmany_rank, hn, his, hos);
+               return PFX(split_common)(rank, dn, dis, dos, howmany_rank, hn, his, hos, ri, ii, ro, io_, flags);
+          }
+     }
 }
 
 /* ---------------------------------------------------------------- r2c / c2r */
@@ -357,6 +420,11 @@ GB_NULL_PLANNER(PFX(plan) PFX(plan_guru64_r2r)(int rank, const PFX(iodim64) *dim
 static void PFX(run)(const PFX(plan) p, void *in, void *out, int kind)
 {
      if (!p) return;
+     if (p->view == 3) {
+          gb_set_error("execute: a split-array plan runs through execute or execute_split_dft");
+          fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
+          return;
+     }
      if (kind >= 0 && p->g->prb.kind != kind) {
           gb_set_error("execute: plan kind does not match the new-array execute function");
           fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
@@ -368,16 +436,37 @@ static void PFX(run)(const PFX(plan) p, void *in, void *out, int kind)
      }
 }
 
+static void PFX(run_split)(const PFX(plan) p, R *ri, R *ii, R *ro, R *io_)
+{
+     if (gb_execute_split(p->g, ri, ii, ro, io_)) {
+          gb_note_failure();
+          fprintf(stderr, "[fftw_gb300] execute failed: %s\n", gb_last_error());
+     }
+}
+
 void PFX(execute)(const PFX(plan) p)
 {
-     if (p) PFX(run)(p, p->g->prb.in, p->g->prb.out, -1);
+     if (!p) return;
+     if (p->view == 3)
+          PFX(run_split)(p, (R *)p->g->split_arr[0], (R *)p->g->split_arr[1], (R *)p->g->split_arr[2],
+                         (R *)p->g->split_arr[3]);
+     else PFX(run)(p, p->g->prb.in, p->g->prb.out, -1);
 }
 void PFX(execute_dft)(const PFX(plan) p, C *in, C *out) { PFX(run)(p, in, out, GB_PROB_DFT); }
 void PFX(execute_dft_r2c)(const PFX(plan) p, R *in, C *out) { PFX(run)(p, in, out, GB_PROB_R2C); }
 void PFX(execute_dft_c2r)(const PFX(plan) p, C *in, R *out) { PFX(run)(p, in, out, GB_PROB_C2R); }
+/* api/execute-split-dft.c:23-27: the plan's transform on new split arrays
+ * of the same layout */
 void PFX(execute_split_dft)(const PFX(plan) p, R *ri, R *ii, R *ro, R *io_)
 {
-     (void)p; (void)ri; (void)ii; (void)ro; (void)io_;
+     if (!p) return;
+     if (p->view == 3) PFX(run_split)(p, ri, ii, ro, io_);
+     else if (p->view == 1) PFX(run)(p, ri, ro, GB_PROB_DFT);
+     else if (p->view == 2) PFX(run)(p, ii, io_, GB_PROB_DFT);
+     else {
+          gb_set_error("execute_split_dft: the plan was not made by the split-array interface");
+          fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
+     }
 }
 void PFX(execute_split_dft_r2c)(const PFX(plan) p, R *in, R *ro, R *io_) { (void)p; (void)in; (void)ro; (void)io_; }
 void PFX(execute_split_dft_c2r)(const PFX(plan) p, R *ri, R *ii, R *out) { (void)p; (void)ri; (void)ii; (void)out; }
@@ -392,6 +481,7 @@ PFX(plan) PFX(copy_plan)(PFX(plan) p)
           {
                PFX(plan) q = (PFX(plan))malloc(sizeof *q);
                q->g = p->g;
+               q->view = p->view;
                return q;
           }
      }

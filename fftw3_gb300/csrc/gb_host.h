@@ -70,6 +70,15 @@ struct gb_plan {
      size_t chunk_bytes[2];
      void *chunk_stream[2];     /* copy-in and copy-out streams */
      void *chunk_ev[3][GB_CHUNK_SLOTS];    /* copied in / transformed / copied out, per slot */
+     /* split-array problems (separate real and imaginary arrays): dims
+      * [vector dims..., transform dims...] with strides in reals; the
+      * transform runs as the forward c2c plan split_inner on dense
+      * interleaved buffers, between a pack and an unpack kernel */
+     int split_nd;
+     long long split_n[2 * GB_MAXRANK], split_is[2 * GB_MAXRANK], split_os[2 * GB_MAXRANK];
+     void *split_arr[4];        /* ri, ii, ro, io at planning time */
+     struct gb_plan *split_inner;
+     void *split_buf[2];        /* dense complex input and output of split_inner */
      void *stream;              /* cudaStream_t; 0 = legacy default stream */
      int async;                 /* 1: execute does not wait for completion */
      int in_align, out_align;   /* alignment of the planning arrays (bytes, capped at 16) */
@@ -106,6 +115,9 @@ int gb_tune(gb_plan *p, unsigned flags);
 
 /* execution (gb_exec.c) */
 int gb_execute(gb_plan *p, void *in, void *out);
+gb_plan *gb_mksplit(int prec, int rank, const gb_dim *dims, int vrank, const gb_dim *vdims, void *ri, void *ii,
+                    void *ro, void *io, unsigned flags);
+int gb_execute_split(gb_plan *p, void *ri, void *ii, void *ro, void *io);
 
 /* wisdom (gb_wisdom.c) */
 typedef struct gb_wisdom_entry {

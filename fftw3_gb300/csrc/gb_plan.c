@@ -1080,7 +1080,10 @@ void gb_destroy(gb_plan *p)
                for (j = 0; j < GB_CHUNK_SLOTS; ++j)
                     if (p->chunk_ev[i][j]) cudaEventDestroy((cudaEvent_t)p->chunk_ev[i][j]);
      }
-     for (i = 0; i < 2; ++i)
+     for (i = 0; i < 2; ++i) {
           if (p->chunk_plan[i]) gb_destroy(p->chunk_plan[i]);
+          if (p->split_buf[i] && !gb_dry) cudaFree(p->split_buf[i]);
+     }
+     if (p->split_inner) gb_destroy(p->split_inner);
      free(p);
 }

@@ -183,7 +183,7 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           const gb_problem *pr;
           if (!plans[i]) { gb_set_error("plan set: plan %d is NULL", i); return 0; }
           pr = &plans[i]->prb;
-          if (pr->kind != GB_PROB_DFT || pr->rank != 1 || pr->vrank > 1 || pr->prec != prec) {
+          if (pr->kind != GB_PROB_DFT || pr->rank != 1 || pr->vrank > 1 || pr->prec != prec || plans[i]->split_inner) {
                gb_set_error("plan set: plan %d is not a rank-1 c2c plan of this precision", i);
                return 0;
           }

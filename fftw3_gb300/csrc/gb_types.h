@@ -143,6 +143,11 @@ int gb_queue_grid(int prec, int threads, int smem);
 int gb_pass_configure(gb_pass *p, int max_smem_optin);
 int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream);
 int gb_cols_tma_smem(int nfft, int tb);
+#define GB_SPLIT_MAXD 32   /* dims of a split-array problem: vector + transform dims */
+/* split-array pack (pack != 0: re/im strided -> dense complex buf) and
+ * unpack (dense complex buf -> re/im strided); n/s: nd dims, strides in reals */
+int gb_split_copy(int pack, int prec, int nd, const long long *n, const long long *s, long long total, void *re,
+                  void *im, void *buf, void *stream);
 int gb_cols_tma_plan_ok(const gb_pass *p);
 int gb_chirp(void *dst, int prec, long long n, int sign, void *stream);
 int gb_device_max_smem(void);

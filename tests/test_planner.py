@@ -142,3 +142,16 @@ def test_prime_rader_when_asked(monkeypatch):
     # p-1 with a prime factor > 13 falls back to Bluestein
     p = g.plan_many_dft([1021], 10, 1 << 20, 1 << 30, prec="f")
     assert passes(p)[0]["kind"] == 3
+
+
+def test_split_array_plans(lib):
+    """plan_guru_split_dft: interleaved arrays (ii = ri + 1) become an ordinary
+    complex plan; separate arrays a pack / c2c / unpack plan."""
+    base = 1 << 20
+    p = g.plan_guru_split_dft([(64, 2, 2)], [(10, 128, 128)], base, base + 4, base + 8192, base + 8196, prec="f")
+    assert p.describe().startswith("(gb300-dft-f32")
+    q = g.plan_guru_split_dft([(64, 1, 1)], [(10, 64, 64)], base, base + 4096, base + 8192, base + 12288, prec="f")
+    assert q.describe().startswith("(gb300-split-dft-f32") and len(q.passes()) == 1
+    r = g.plan_guru_split_dft([(12, 20, 1), (20, 1, 12)], [(3, 240, 240)], base, base + 8192, base + 16384,
+                              base + 24576, prec="d")
+    assert r.describe().startswith("(gb300-split-dft-f64")
