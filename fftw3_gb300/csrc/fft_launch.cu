@@ -336,7 +336,7 @@ static int cols_tma_ok(const gb_pass *p, const void *in)
      int d;
      const int T = p->nfft / reg_e(p->nfft);
      if (p->kind != GB_KIND_C2C || p->prec != 4 || p->load_mode != GB_MOVE_COLS) return 0;
-     if (p->nfft < 16 || p->nfft > 2048 || p->tb < 2 || p->tb > 64 || (p->tb & (p->tb - 1)) || p->ltb < 0) return 0;
+     if (p->nfft < 16 || p->nfft > 2048 || p->tb < 2 || p->tb > 128 || (p->tb & (p->tb - 1)) || p->ltb < 0) return 0;
      if (p->threads != p->tb * T || p->threads > 256 || p->nv > 4) return 0;
      if (p->smem < gb_cols_tma_smem(p->nfft, p->tb)) return 0;
      if ((uintptr_t)in % 16 || p->vis[0] != 1 || p->is <= 0 || (p->is * 8) % 16 || p->is * 8 >= (1LL << 40)) return 0;
@@ -424,7 +424,7 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
                bad = "persistent bulk-copy pass needs unit-stride c2c/r2c in and out and two smem slots";
           else if (p->variant == GB_VAR_TMA && ((uintptr_t)in % 16 != 0)) bad = "bulk copies need a 16-byte aligned input";
           else if (p->variant == GB_VAR_TMA_COLS && !cols_tma_ok(p, in))
-               bad = "tensor-map column pass needs f32 c2c column tiles of 2..64 columns, 16..2048 points, even positive "
+               bad = "tensor-map column pass needs f32 c2c column tiles of 2..128 columns, 16..2048 points, even positive "
                      "strides, a 16-byte aligned input and two shared slots";
           else if (p->variant == GB_VAR_TC && (p->prec != 4 || (p->nfft != 256 && p->nfft != 4096) ||
                                                p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||

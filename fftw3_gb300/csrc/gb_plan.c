@@ -647,14 +647,15 @@ static void dense_dims(const gb_dim *v, int nv, long long L, gb_dim *out, int ke
  * row is a contiguous run of columns.  Scratch holds [outer][n2][k1][u].
  * Pass A: n1-point transforms at element stride n2*is, twiddle
  * W_n^(n2*k1) indexed by vector dimension 1 (n2); pass B: n2-point
- * transforms at scratch stride n1*nu, written to k1 + n1*k2.
+ * transforms at scratch stride n1*nup (nup = nu rounded up to 8), written to
+ * k1 + n1*k2.
  * Returns 0 when added, -1 when the layout or lengths do not allow it. */
 static int add_fourstep_cols(builder *b, long long n, int sign, long long is, long long os,
                              int nvk, const gb_dim *v, int src, int dst, int mid)
 {
      gb_plan *p = b->p;
      int prec = p->prb.prec, i, u = -1, no = 0;
-     long long n1 = 0, d, nu, dense, outer = 1;
+     long long n1 = 0, d, nu, nup, dense, outer = 1;
      gb_dim va[GB_MAXV], vb[GB_MAXV], vo[GB_MAXRANK];
      gb_step *sa, *sb;
      for (i = 0; i < nvk; ++i)
@@ -671,30 +672,33 @@ static int add_fourstep_cols(builder *b, long long n, int sign, long long is, lo
      }
      if (!n1) return -1;
      nu = v[u].n;
+     /* the scratch rows hold nup >= nu columns: a multiple of 8 complex
+      * values, so the second pass's strides suit tensor-map copies */
+     nup = (nu + 7) & ~7LL;
      for (i = 0; i < nvk; ++i) if (i != u) { vo[no++] = v[i]; outer *= v[i].n; }
-     need_scratch(p, mid, (size_t)(n * nu * outer) * csize(prec));
+     need_scratch(p, mid, (size_t)(n * nup * outer) * csize(prec));
      /* pass A */
      va[0].n = nu; va[0].is = v[u].is; va[0].os = 1;
-     va[1].n = n / n1; va[1].is = is; va[1].os = n1 * nu;
-     dense = n * nu;
+     va[1].n = n / n1; va[1].is = is; va[1].os = n1 * nup;
+     dense = n * nup;
      for (i = 0; i < no; ++i) { va[2 + i].n = vo[i].n; va[2 + i].is = vo[i].is; va[2 + i].os = dense; dense *= vo[i].n; }
      sa = new_step(b);
      if (!sa) return -1;
      sa->src = src; sa->dst = mid;
-     if (config_pass(&sa->pass, prec, GB_KIND_C2C, n1, sign, (n / n1) * is, nu, 2 + no, va, 0, 1)) { --p->nstep; return -1; }
+     if (config_pass(&sa->pass, prec, GB_KIND_C2C, n1, sign, (n / n1) * is, nup, 2 + no, va, 0, 1)) { --p->nstep; return -1; }
      sa->pass.post_N = n;
      sa->pass.post_vdim = 1;
      if (p->flags & GB_FLAG_TENSOR_CORE) use_tensor_cores(&sa->pass);
      if (pass_tables(&sa->pass)) { b->err = 1; return 0; }
      /* pass B */
      vb[0].n = nu; vb[0].is = 1; vb[0].os = v[u].os;
-     vb[1].n = n1; vb[1].is = nu; vb[1].os = os;
-     dense = n * nu;
+     vb[1].n = n1; vb[1].is = nup; vb[1].os = os;
+     dense = n * nup;
      for (i = 0; i < no; ++i) { vb[2 + i].n = vo[i].n; vb[2 + i].is = dense; vb[2 + i].os = vo[i].os; dense *= vo[i].n; }
      sb = new_step(b);
      if (!sb) return -1;
      sb->src = mid; sb->dst = dst;
-     if (config_pass(&sb->pass, prec, GB_KIND_C2C, n / n1, sign, n1 * nu, n1 * os, 2 + no, vb, 0, 1)) {
+     if (config_pass(&sb->pass, prec, GB_KIND_C2C, n / n1, sign, n1 * nup, n1 * os, 2 + no, vb, 0, 1)) {
           p->nstep -= 2;
           return -1;
      }
@@ -995,6 +999,31 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
           long long nl = prb->sz[r - 1].n;
           gb_dim v[2 * GB_MAXRANK];
           int nv = 0;
+          const long long nc = nl / 2 + 1, n0 = prb->sz[0].n;
+          if (r == 2 && prb->prec == 4 && prb->vrank <= 1 && prb->sz[1].os == 1 && (prb->sz[0].os & 1) &&
+              n0 >= 16 && (n0 & (n0 - 1)) == 0 && nl >= 32 && nl <= 16384 && (nl & (nl - 1)) == 0 &&
+              !getenv("FFTW_GB300_NO_TMA")) {
+               /* (both lengths powers of two: one r2c pass that needs no scratch of
+                * its own, and column passes that use only the first scratch) */
+               /* rows of an odd number of complex values (FFTW's n/2+1 layout)
+                * cannot be walked by tensor-map copies: the r2c pass writes rows
+                * padded to a multiple of 8 complex values into scratch, and the
+                * column pass reads them from there with TMA-fed column tiles */
+               const long long P = (nc + 7) & ~7LL;
+               const long long hm = prb->vrank ? prb->vec[0].n : 1;
+               gb_dim vc[2];
+               v[0].n = n0; v[0].is = prb->sz[0].is; v[0].os = P;
+               nv = 1;
+               if (prb->vrank) { v[1].n = hm; v[1].is = prb->vec[0].is; v[1].os = n0 * P; nv = 2; }
+               need_scratch(p, GB_BUF_SCRATCH2, (size_t)(n0 * P * hm) * csize(prb->prec));
+               add_1d(&b, GB_KIND_R2C, nl, -1, prb->sz[1].is, 1, nv, v, GB_BUF_IN, GB_BUF_SCRATCH2);
+               vc[0].n = nc; vc[0].is = 1; vc[0].os = 1;
+               if (prb->vrank) { vc[1].n = hm; vc[1].is = n0 * P; vc[1].os = prb->vec[0].os; }
+               if (!b.err)
+                    add_1d_mid(&b, GB_KIND_C2C, n0, -1, P, prb->sz[0].os, nv, vc, GB_BUF_SCRATCH2, GB_BUF_OUT,
+                               GB_BUF_SCRATCH);
+               goto built;
+          }
           for (i = 0; i < r - 1; ++i) { v[nv] = prb->sz[i]; ++nv; }
           for (i = 0; i < prb->vrank; ++i) v[nv++] = prb->vec[i];
           add_1d(&b, GB_KIND_R2C, nl, -1, prb->sz[r - 1].is, prb->sz[r - 1].os, nv, v, GB_BUF_IN, GB_BUF_OUT);
@@ -1037,6 +1066,7 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
           for (i = 0; i < prb->vrank; ++i) v[nv++] = prb->vec[i];
           add_1d(&b, GB_KIND_C2R, nl, 1, prb->sz[r - 1].is, prb->sz[r - 1].os, nv, v, GB_BUF_IN, GB_BUF_OUT);
      }
+built:
      if (b.err) {
           free(p);
           return 0;
