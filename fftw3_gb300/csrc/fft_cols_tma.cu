@@ -13,7 +13,9 @@
  * eight different 16-byte chunks per eight consecutive rows.  From there the
  * tile runs through the same register stages as k_reg (radix 16, shared
  * exchanges in the slot), the four-step twiddle if any, and is stored
- * directly (unit output stride) or as column tiles.
+ * directly (unit output stride), or as column tiles: through a second tensor
+ * map (cp.async.bulk.tensor stores of the same swizzled boxes) when the
+ * output's strides allow, else with plain stores.
  *
  * Every wait on a slot is bounded (2 s of wall time); a copy that never
  * completes sets GB_STATUS_COPY_TIMEOUT and the CTA returns.
@@ -62,6 +64,49 @@ __device__ __forceinline__ void tma_tile_load(void *dst, const CUtensorMap *tm, 
      }
 }
 
+__device__ __forceinline__ void tma_tile_store(const CUtensorMap *tm, int rank, const int *c, const void *src)
+{
+     const unsigned sa = smem_u32(src);
+     const unsigned long long t = (unsigned long long)tm;
+     switch (rank) {
+     case 2:
+          asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];"
+                       ::"l"(t), "r"(c[0]), "r"(c[1]), "r"(sa) : "memory");
+          break;
+     case 3:
+          asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
+                       ::"l"(t), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(sa) : "memory");
+          break;
+     case 4:
+          asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];"
+                       ::"l"(t), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(sa) : "memory");
+          break;
+     default:
+          asm volatile("cp.async.bulk.tensor.5d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4, %5}], [%6];"
+                       ::"l"(t), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(sa) : "memory");
+          break;
+     }
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+/* the committed stores have finished reading shared memory */
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+/* the committed stores have completed */
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+/* Tensor coordinates of tile blk: c[0] first column, c[2..] the outer
+ * vector indices (c[1], the row, is set per box). */
+__device__ __forceinline__ void ct_coords(const gb_pass &P, long long blk, int *c)
+{
+     long long rest = blk / P.ntiles0;
+     c[0] = (int)((blk - rest * P.ntiles0) * P.tb);
+     c[1] = 0;
+     for (int d = 1; d < P.nv; ++d) {
+          const long long q = rest / P.vn[d];
+          c[1 + d] = (int)(rest - q * P.vn[d]);
+          rest = q;
+     }
+}
+
 /* Issue the boxes of tile blk into slot dst (thread 0 only). */
 template <int N>
 __device__ __forceinline__ void ct_issue(const gb_pass &P, const CUtensorMap *tm, long long blk, unsigned char *dst,
@@ -70,13 +115,7 @@ __device__ __forceinline__ void ct_issue(const gb_pass &P, const CUtensorMap *tm
      constexpr int ROWS = N < 256 ? N : 256;
      const int tb = P.tb, cb = ct_cb(tb);
      int c[5] = {0, 0, 0, 0, 0};
-     long long rest = blk / P.ntiles0;
-     c[0] = (int)((blk - rest * P.ntiles0) * tb);
-     for (int d = 1; d < P.nv; ++d) {
-          const long long q = rest / P.vn[d];
-          c[1 + d] = (int)(rest - q * P.vn[d]);
-          rest = q;
-     }
+     ct_coords(P, blk, c);
      mbar_expect_tx(bar, (unsigned)(tb * N * 8));
      const int c0 = c[0];
      for (int k = 0; k < tb / cb; ++k)
@@ -89,7 +128,8 @@ __device__ __forceinline__ void ct_issue(const gb_pass &P, const CUtensorMap *tm
 
 template <int LOGN, int DIR>
 __global__ void __launch_bounds__(256, 3)
-k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out, const __grid_constant__ CUtensorMap tmap)
+k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out, const __grid_constant__ CUtensorMap tmap,
+           const __grid_constant__ CUtensorMap omap, const int tstore)
 {
      typedef float2 C;
      constexpr int N = 1 << LOGN;
@@ -127,6 +167,8 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
           const long long nxt = blk + stride;
           const bool issued = nxt < P.nblocks;
           if (threadIdx.x == 0 && issued) {
+               /* that slot's boxes may still be going out to global memory */
+               if (tstore) bulk_wait_read();
                fence_proxy_async_smem();
                ct_issue<N>(P, &tmap, nxt, b ? s0 : s1, &bar[b ^ 1]);
           }
@@ -166,6 +208,35 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
 #pragma unroll
                     for (int e = 0; e < E; ++e) io<C>::stc(out, bo, tid + T * e, P.os, x[e]);
                }
+          } else if (tstore) {
+               /* column tiles out through the output tensor map: the results
+                * take the boxes' swizzled layout in the slot, and one thread
+                * hands the boxes to the TMA engine */
+               /* layout constants recomputed from the launch parameters
+                * rather than kept live across the stages */
+               const int cbs = ct_cb(P.tb);
+               const int ms = cbs >= 16 ? 7 : cbs == 8 ? 3 : cbs == 4 ? 1 : 0;
+               const int cbase = (tl / cbs) * N * cbs * 8 + (tl % cbs) * 8;
+#pragma unroll
+               for (int e = 0; e < E; ++e) {
+                    const int o = cbase + (tid + T * e) * cbs * 8;
+                    *(C *)(cur + ct_swz(o, ms)) = x[e];
+               }
+               fence_proxy_async_smem();
+               __syncthreads();
+               if (threadIdx.x == 0) {
+                    constexpr int ROWS = N < 256 ? N : 256;
+                    int c[5] = {0, 0, 0, 0, 0};
+                    ct_coords(P, blk, c);
+                    const int c0 = c[0];
+                    for (int k = 0; k < P.tb / cbs; ++k)
+                         for (int r = 0; r < N / ROWS; ++r) {
+                              c[0] = c0 + k * cbs;
+                              c[1] = r * ROWS;
+                              tma_tile_store(&omap, 1 + P.nv, c, cur + (k * N + r * ROWS) * cbs * 8);
+                         }
+                    bulk_commit();
+               }
           } else {
 #pragma unroll
                for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
@@ -174,6 +245,7 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
           }
           __syncthreads();   /* the slot is the target of a later tile's boxes */
      }
+     if (tstore && threadIdx.x == 0) bulk_wait_all();
 }
 
 template <int L>

@@ -348,7 +348,22 @@ static int cols_tma_ok(const gb_pass *p, const void *in)
 
 extern "C" int gb_cols_tma_plan_ok(const gb_pass *p) { return cols_tma_ok(p, (const void *)0); }
 
-static int encode_cols_map(CUtensorMap *tm, const gb_pass *p, const void *in)
+/* The output of a column pass as a tensor map for TMA stores: the same
+ * view and boxes as the input's, over (out, os, vos). */
+static int cols_out_ok(const gb_pass *p, const void *out)
+{
+     int d;
+     if (p->store_mode != GB_MOVE_COLS || p->vos[0] != 1 || (uintptr_t)out % 16 || p->os <= 0 || (p->os * 8) % 16 ||
+         p->os * 8 >= (1LL << 40))
+          return 0;
+     for (d = 1; d < p->nv; ++d)
+          if (p->vos[d] <= 0 || (p->vos[d] * 8) % 16 || p->vos[d] * 8 >= (1LL << 40)) return 0;
+     return 1;
+}
+
+static int encode_cols_map(CUtensorMap *tm, const gb_pass *p, const void *in, int output);
+
+static int encode_cols_map(CUtensorMap *tm, const gb_pass *p, const void *in, int output)
 {
      cuuint64_t gdim[5], gstr[4];
      cuuint32_t box[5] = {1, 1, 1, 1, 1}, es[5] = {1, 1, 1, 1, 1};
@@ -368,10 +383,10 @@ static int encode_cols_map(CUtensorMap *tm, const gb_pass *p, const void *in)
      }
      gdim[0] = (cuuint64_t)p->vn[0];
      gdim[1] = (cuuint64_t)p->nfft;
-     gstr[0] = (cuuint64_t)p->is * 8;
+     gstr[0] = (cuuint64_t)(output ? p->os : p->is) * 8;
      for (d = 1; d < p->nv; ++d) {
           gdim[1 + d] = (cuuint64_t)p->vn[d];
-          gstr[d] = (cuuint64_t)p->vis[d] * 8;
+          gstr[d] = (cuuint64_t)(output ? p->vos[d] : p->vis[d]) * 8;
      }
      box[0] = (cuuint32_t)cb;
      box[1] = (cuuint32_t)(p->nfft < 256 ? p->nfft : 256);
@@ -448,9 +463,13 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
      }
      gb_pass pv = *p;
      if (!pv.status) pv.status = gb_device_status_ptr();
-     CUtensorMap tmap;
-     void *args[4] = {(void *)&pv, (void *)&in, (void *)&out, (void *)&tmap};
-     if (p->variant == GB_VAR_TMA_COLS && encode_cols_map(&tmap, p, in)) {
+     CUtensorMap tmap, omap;
+     int tstore = 0;
+     void *args[6] = {(void *)&pv, (void *)&in, (void *)&out, (void *)&tmap, (void *)&omap, (void *)&tstore};
+     memset(&omap, 0, sizeof omap);
+     if (p->variant == GB_VAR_TMA_COLS && cols_out_ok(p, out) && !getenv("FFTW_GB300_NO_TMA_STORE"))
+          tstore = encode_cols_map(&omap, p, out, 1) == 0;
+     if (p->variant == GB_VAR_TMA_COLS && encode_cols_map(&tmap, p, in, 0)) {
           /* the driver refused this view of the array: same tile through
            * the register kernel's plain loads */
           pv.variant = GB_VAR_REG;
