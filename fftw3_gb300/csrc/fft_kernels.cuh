@@ -765,6 +765,10 @@ struct gen_addr {
      void *out;
      const void *const *pin;
      void *const *pout;
+     /* 1: the input was written earlier in this launch by other CTAs (a
+      * work-queue item that waited on a counter): load it from L2, never
+      * from this SM's L1, which is not kept coherent with other SMs' writes */
+     int l2only;
 };
 
 template <typename C> __device__ __forceinline__ const C *src_of(const gb_pass &P, const tile_t &tl, const gen_addr &A, int t)
@@ -823,7 +827,10 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                               if (kind == GB_KIND_R2C) {
                                    const R *r = (const R *)src_of<R>(P, tile, A, t);
                                    x[u] = P.real_pairs ? ((const C *)r)[j] : mk<C>(r[2 * j * P.is], r[(2 * j + 1) * P.is]);
-                              } else x[u] = src_of<C>(P, tile, A, t)[j * P.is];
+                              } else {
+                                   const C *sp = src_of<C>(P, tile, A, t) + (long long)j * P.is;
+                                   x[u] = A.l2only ? __ldcg(sp) : *sp;
+                              }
                               slot[u] = t * sms + j;
                          }
                     }
@@ -987,7 +994,7 @@ __global__ void __launch_bounds__(512) k_gen(const gb_pass P, const void *__rest
      C *b0 = (C *)gb_smem;
      C *b1 = b0 + P.tb * (P.nfft + 1);
      gen_addr A;
-     A.in = in; A.out = out; A.pin = 0; A.pout = 0;
+     A.in = in; A.out = out; A.pin = 0; A.pout = 0; A.l2only = 0;
      for (long long blk = blockIdx.x; blk < P.nblocks; blk += gridDim.x) {
           const tile_t tile = tile_of(P, blk);
           gen_tile<C>(P, tile, A, b0, b1);

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_queue(const
                tile.bi = it.bi; tile.bo = it.bo; tile.v0 = it.v0; tile.vpost = 0;
                gen_addr A;
                A.in = it.in; A.out = it.out; A.pin = it.pin; A.pout = it.pout;
+               A.l2only = it.wait_ctr >= 0;
                gen_tile<C>(it.P, tile, A, b0, b1);
                if (it.signal_ctr >= 0) {
                     __threadfence();

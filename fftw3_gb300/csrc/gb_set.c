@@ -284,7 +284,9 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                     q->wait_ctr = ctr; q->wait_target = nta; q->signal_ctr = -1;
                }
                if (pb.smem > smem) smem = pb.smem;
-               scratch_elems += n;
+               /* next transform's scratch on a fresh 256-byte boundary, so no
+                * cache line holds two transforms' intermediates */
+               scratch_elems += (n + 31) & ~31LL;
           }
           ++i;
      }
@@ -372,7 +374,10 @@ static int build_graph(gb_set *S)
           if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return -1;
           own = 1;
      } else st = (cudaStream_t)S->stream;
-     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = -1;
+     /* the status word the queue kernels report to is allocated on first
+      * use, which must not happen inside the capture */
+     if (!gb_device_status_ptr()) rc = -1;
+     if (!rc && cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = -1;
      if (!rc) {
           cudaMemsetAsync(S->d_head, 0, 2 * sizeof(int), st);
           if (S->nctr) cudaMemsetAsync(S->d_ctrs, 0, sizeof(int) * (size_t)S->nctr, st);

@@ -154,6 +154,7 @@ int gb_device_max_smem(void);
 const char *gb_last_cuda_error(void);
 long long gb_launch_count(void);
 int gb_device_status(void);
+int *gb_device_status_ptr(void);
 
 #ifdef __cplusplus
 }
