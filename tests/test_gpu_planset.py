@@ -115,3 +115,26 @@ def torch_cuda_set():
     import torch
     assert torch.cuda.is_available()
     return torch
+
+
+def test_planset_first_use_in_fresh_process(lib):
+    """A plan set built and executed before any other launch of the library in
+    the process (its device status word is allocated outside the capture)."""
+    import subprocess
+    code = (
+        "import sys, ctypes, numpy as np, torch; sys.path.insert(0, %r)\n"
+        "import fftw3_gb300 as g\n"
+        "x = torch.randn(3000, dtype=torch.complex64, device='cuda'); y = torch.zeros_like(x)\n"
+        "ps = [g.plan_many_dft([n], 1, x.data_ptr() + o * 8, y.data_ptr() + o * 8, -1, g.FFTW_ESTIMATE, 'f')"
+        " for n, o in ((1000, 0), (2000, 1000))]\n"
+        "lib = g.load(); f = lib.fftwf_gb300_plan_set; f.restype = ctypes.c_void_p\n"
+        "f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint]\n"
+        "arr = (ctypes.c_void_p * 2)(*[p.ptr for p in ps]); s = f(2, arr, 0)\n"
+        "lib.fftwf_gb300_execute_set.argtypes = [ctypes.c_void_p]\n"
+        "rc = lib.fftwf_gb300_execute_set(s); torch.cuda.synchronize()\n"
+        "ref = np.concatenate([np.fft.fft(x[:1000].cpu().numpy().astype(np.complex128)),"
+        " np.fft.fft(x[1000:].cpu().numpy().astype(np.complex128))])\n"
+        "err = np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref)\n"
+        "print(rc, err); sys.exit(0 if rc == 0 and err < 1e-6 else 1)\n" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
