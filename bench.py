@@ -26,12 +26,14 @@ scaling, no collective: the transforms are independent) and rank 0 prints.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import math
 import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -138,29 +140,39 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples (every 20 ms) of the SM clock and throttle reasons
+    around the timed region.  The sampler is running before the region starts;
+    the summary uses the samples whose timestamps fall inside the region, or
+    the two nearest ones when the region is shorter than the interval."""
 
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="fftw_gb300_clocks_", suffix=".csv")
+        os.close(fd)
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index),
-                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "--query-gpu=timestamp,clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
                  "clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.f, stderr=subprocess.DEVNULL)
+            deadline = time.time() + 3.0
+            while time.time() < deadline and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
+        self.t0 = datetime.datetime.now()
         return self
 
     def __exit__(self, *a):
+        self.t1 = datetime.datetime.now()
         if self.proc:
+            time.sleep(0.05)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -170,14 +182,32 @@ class ClockSampler:
 
     def summary(self):
         try:
-            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
-            sm = [float(r[0]) for r in rows]
-            mx = [float(r[1]) for r in rows]
+            rows = []
+            for r in open(self.path).read().strip().splitlines():
+                f = [x.strip() for x in r.split(",")]
+                if len(f) < 7:
+                    continue
+                rows.append((datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f"), f))
+            inside = [f for t, f in rows if self.t0 <= t <= self.t1]
+            nearest = not inside
+            if nearest:
+                mid = self.t0 + (self.t1 - self.t0) / 2
+                inside = [f for _, f in sorted(rows, key=lambda tf: abs((tf[0] - mid).total_seconds()))[:2]]
+            sm = [float(f[1]) for f in inside]
+            mx = [float(f[2]) for f in inside]
             names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-            reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[2 + i] and "Not" not in r[2 + i]})
-            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": reasons, "samples": len(rows)}
+            reasons = sorted({names[i] for f in inside for i in range(4) if f[3 + i] == "Active"})
+            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": reasons,
+                    "samples": len(inside), "window_ms": round((self.t1 - self.t0).total_seconds() * 1e3, 1),
+                    "samples_are": "nearest to the timed region (shorter than the 20 ms interval)" if nearest
+                    else "inside the timed region"}
         except Exception:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
 
 
 def committed_traffic(workload):
