@@ -198,9 +198,7 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
           C *const smt = sm + tl * SMS;
           reg_stages<C, N, DIR, 1>(x, tid, smt, tw);
           if (P.post_N) {
-#pragma unroll
-               for (int e = 0; e < E; ++e)
-                    x[e] = cmul(x[e], post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)(tid + T * e)));
+               apply_post_twiddles<C, E, T>(P, P.post_vdim ? tile.vpost : v, tid, x);
           }
           if (P.store_mode == GB_MOVE_DIRECT) {
                if (valid) {

@@ -144,6 +144,32 @@ template <typename C> __device__ __forceinline__ C post_twiddle(const gb_pass &P
      return w;
 }
 
+/* Four-step twiddles of one thread's elements k = tid + T*e (e < E) for
+ * vector index v: W(v k) = W(v tid) * W(v T e), W(m) = exp(sign 2 pi i m/N).
+ * For E = 16, W(v tid) and W(v T e) for e = 1, 2, 4, 8 come from the
+ * two-level table (10 reads instead of 32) and the element factors are
+ * b_r * W(v T 4q) for e = 4q + r, with b_r = W(v tid) W(v T r) and
+ * W(v T 4q) products of the read powers: every factor is a product of at
+ * most four correctly rounded table entries, as the stage twiddles are.
+ * Indices stay below N (v < N / (T E), so 8 v T < N). */
+template <typename C, int E, int T>
+__device__ __forceinline__ void apply_post_twiddles(const gb_pass &P, long long v, int tid, C (&x)[E])
+{
+     if constexpr (E != 16) {
+#pragma unroll
+          for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
+     } else {
+          const long long s = v * T;
+          const C a = post_twiddle<C>(P, v * tid);
+          const C w1 = post_twiddle<C>(P, s), w2 = post_twiddle<C>(P, 2 * s), w4 = post_twiddle<C>(P, 4 * s),
+                  w8 = post_twiddle<C>(P, 8 * s);
+          const C b[4] = {a, cmul(a, w1), cmul(a, w2), cmul(a, cmul(w1, w2))};
+          const C q[4] = {mk<C>(1, 0), w4, w8, cmul(w8, w4)};
+#pragma unroll
+          for (int e = 0; e < 16; ++e) x[e] = cmul(x[e], (e < 4) ? b[e & 3] : cmul(b[e & 3], q[e >> 2]));
+     }
+}
+
 /* Column tiles with a power-of-two tb that divides the CTA: each thread
  * keeps one column t = threadIdx mod tb for the whole tile and walks its
  * rows j = threadIdx / tb, j + J, j + 2J, ... (J = threads / tb) with one
@@ -543,9 +569,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
           } else {
                if constexpr (KIND == GB_KIND_C2C) {
                     if (P.post_N) {
-#pragma unroll
-                         for (int e = 0; e < E; ++e)
-                              x[e] = cmul(x[e], post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)(tid + T * e)));
+                         apply_post_twiddles<C, E, T>(P, P.post_vdim ? tile.vpost : v, tid, x);
                     }
                }
                constexpr bool RP = (KIND == GB_KIND_C2R);
@@ -687,8 +711,7 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
                __syncthreads();   /* the slot is the next bulk copy's target */
           } else {
                if (P.post_N) {
-#pragma unroll
-                    for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)(tid + T * e)));
+                    apply_post_twiddles<C, E, T>(P, P.post_vdim ? tile.vpost : v, tid, x);
                }
                if (valid) {
                     /* unit output stride (checked at launch): constant offsets */
