@@ -579,6 +579,7 @@ def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
     else:
         p = g.plan_many_dft_r2c(shape, howmany, hin, hout, g.FFTW_ESTIMATE, prec)
         ex = lambda: p.execute_dft_r2c(hin, hout)
+    fails0 = lib.fftw_gb300_failures()
     ex()
     steps = max(2, min(args.steps, 5))
     each = []
@@ -587,6 +588,8 @@ def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
         ex()
         each.append(time.perf_counter() - t0)
     dt = sum(each) / steps
+    if lib.fftw_gb300_failures() != fails0:
+        raise RuntimeError("e2e: fftw execute failed: " + g.last_error())
     path = ("direct host access" if len(p.passes()) == 1 else
             "pipelined chunk staging" if howmany >= 2 else "staged copies around the passes")
     p.destroy()

@@ -162,8 +162,8 @@ static int chunk_prepare(gb_plan *p, int inplace)
      extent ei, eo;
      long long ci, co, nd, m, bi, bo;
      int d = -1, i, j, esin = elsize(prb, 0), esout = elsize(prb, 1);
-     if (p->chunk_state) return p->chunk_state;
-     p->chunk_state = -1;
+     if (p->chunk_state) return p->chunk_state > 0 ? 1 : 0;
+     p->chunk_state = -1;   /* not applicable, unless set up below */
      for (i = 0; i < prb->vrank; ++i)
           if (prb->vec[i].n >= 2 && prb->vec[i].is > 0 && prb->vec[i].os > 0 &&
               (d < 0 || prb->vec[i].is * esin > prb->vec[d].is * esin))
@@ -316,8 +316,9 @@ int gb_execute(gb_plan *p, void *in, void *out)
       * pipelined chunks when the batch can be cut, so copies in, passes and
       * copies out overlap */
      if (!direct_host && !device_accessible(in) && !device_accessible(out) && !getenv("FFTW_GB300_STAGE_HOST")) {
+          /* (a preparation that fails leaves the plan on the whole-extent
+           * staging below) */
           int r = chunk_prepare(p, inplace);
-          if (r < 0) return -1;
           /* the slots were laid out for the in-place-ness of the first call */
           if (r > 0 && (p->chunk_buf[1][0] == 0) == inplace)
                return chunk_execute(p, (const char *)in, (char *)out, inplace);

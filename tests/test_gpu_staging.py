@@ -114,3 +114,27 @@ def test_pageable_numpy_chunks(lib, torch_cuda, restatement):
     assert rel_l2(y.reshape(hm, n)[rows].ravel(), ref) <= 1e-6
     # untouched by the transform: the input
     assert np.isfinite(x).all()
+
+
+def test_whole_extent_staging_repeats(lib, restatement):
+    """A multi-pass plan on page-locked host arrays that cannot be cut into
+    chunks (one transform) stages the whole extent, on every execute."""
+    import fftw3_gb300 as g
+    shape = [256, 512]
+    tot = 256 * 512
+    ptr_in, ain = _pinned(lib, "fftwf_", tot * 8, np.complex64)
+    ptr_out, aout = _pinned(lib, "fftwf_", tot * 8, np.complex64)
+    p = g.plan_many_dft(shape, 1, ptr_in, ptr_out, -1, g.FFTW_ESTIMATE, "f")
+    assert len(p.passes()) > 1
+    before = lib.fftw_gb300_failures()
+    rng = np.random.default_rng(36)
+    for _ in range(3):
+        x = (rng.standard_normal(tot) + 1j * rng.standard_normal(tot)).astype(np.complex64)
+        ain[:] = x
+        p.execute()
+        ref = restatement.c2c(x.astype(np.complex128), shape, -1, "d", nthreads=4)
+        assert rel_l2(aout.copy(), ref) <= 1e-6
+    assert lib.fftw_gb300_failures() == before
+    p.destroy()
+    lib.fftwf_free(ptr_in)
+    lib.fftwf_free(ptr_out)
