@@ -94,13 +94,35 @@ __global__ void __launch_bounds__(256) k_pointwise(const gb_pass P, const void *
 {
      typedef typename real_of<C>::T R;
      const int M = P.nfft;
-     const int L = (P.pw == GB_PW_HC2C_POST) ? M + 1 : (P.pw == GB_PW_CHIRP_OUT) ? P.n : M;
+     const int L = (P.pw == GB_PW_HC2C_POST) ? M + 1
+                 : (P.pw == GB_PW_CHIRP_OUT) ? P.n
+                 : (P.pw == GB_PW_HALF_COPY) ? P.n / 2 + 1 : M;
      for (long long blk = blockIdx.x; blk < P.nblocks; blk += gridDim.x) {
           const long long tr = blk / P.pw_chunks;
           const int k0 = (int)(blk - tr * P.pw_chunks) * 4096;
           const tile_t tile = tile_of(P, tr);
-          const C *src = (const C *)in + tile.bi + tile.v0 * P.vis[0];
-          C *dst = (C *)out + tile.bo + tile.v0 * P.vos[0];
+          const long long ioff = tile.bi + tile.v0 * P.vis[0], ooff = tile.bo + tile.v0 * P.vos[0];
+          const C *src = (const C *)in + ioff;
+          C *dst = (C *)out + ooff;
+          if (P.pw == GB_PW_PROMOTE || P.pw == GB_PW_REAL_PART || P.pw == GB_PW_HERM_EXT || P.pw == GB_PW_HALF_COPY) {
+               /* odd-length real transforms around a c2c: offsets and strides of
+                * the real side count reals */
+               const R *rs = (const R *)in + ioff;
+               R *rd = (R *)out + ooff;
+               for (int k = k0 + threadIdx.x; k < L && k < k0 + 4096; k += blockDim.x) {
+                    if (P.pw == GB_PW_PROMOTE) dst[(long long)k * P.os] = mk<C>(rs[(long long)k * P.is], (R)0);
+                    else if (P.pw == GB_PW_REAL_PART) rd[(long long)k * P.os] = src[(long long)k * P.is].x;
+                    else if (P.pw == GB_PW_HALF_COPY) dst[(long long)k * P.os] = src[(long long)k * P.is];
+                    else {
+                         const int h = (2 * k <= P.n) ? k : P.n - k;
+                         C z = src[(long long)h * P.is];
+                         if (k == 0) z.y = 0;
+                         else if (h != k) z.y = -z.y;
+                         dst[(long long)k * P.os] = z;
+                    }
+               }
+               continue;
+          }
           for (int k = k0 + threadIdx.x; k < L && k < k0 + 4096; k += blockDim.x) {
                C y;
                if (P.pw == GB_PW_HC2C_POST) {

@@ -400,28 +400,92 @@ GB_NULL_PLANNER(PFX(plan) PFX(plan_guru64_split_dft_r2c)(int rank, const PFX(iod
                 const PFX(iodim64) *howmany_dims, R *in, R *ro, R *io_, unsigned flags))
 GB_NULL_PLANNER(PFX(plan) PFX(plan_guru64_split_dft_c2r)(int rank, const PFX(iodim64) *dims, int howmany_rank,
                 const PFX(iodim64) *howmany_dims, R *ri, R *ii, R *out, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_many_r2r)(int rank, const int *n, int howmany, R *in, const int *inembed,
-                int istride, int idist, R *out, const int *onembed, int ostride, int odist,
-                const PFX(r2r_kind) *kind, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_r2r)(int rank, const int *n, R *in, R *out, const PFX(r2r_kind) *kind,
-                unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_r2r_1d)(int n, R *in, R *out, PFX(r2r_kind) kind, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_r2r_2d)(int n0, int n1, R *in, R *out, PFX(r2r_kind) kind0,
-                PFX(r2r_kind) kind1, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_r2r_3d)(int n0, int n1, int n2, R *in, R *out, PFX(r2r_kind) kind0,
-                PFX(r2r_kind) kind1, PFX(r2r_kind) kind2, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_guru_r2r)(int rank, const PFX(iodim) *dims, int howmany_rank,
-                const PFX(iodim) *howmany_dims, R *in, R *out, const PFX(r2r_kind) *kind, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_guru64_r2r)(int rank, const PFX(iodim64) *dims, int howmany_rank,
-                const PFX(iodim64) *howmany_dims, R *in, R *out, const PFX(r2r_kind) *kind, unsigned flags))
+/* r2r: rank 1 (plan_r2r_1d, plan_r2r / plan_many_r2r / guru of rank 1 with
+ * at most one howmany dimension); multi-dimensional r2r returns NULL.
+ * Strides and distances count reals (api/plan-many-r2r.c, api/plan-r2r.c). */
+static PFX(plan) PFX(r2r_common)(int kind, long long n, long long hm, long long is, long long idist, long long os,
+                                 long long odist, R *in, R *out, unsigned flags)
+{
+     gb_plan *g;
+     PFX(plan) p;
+     if (n <= 0 || hm < 0) return 0;
+     if (!gb_dry_run() && !gb_cuda_ready()) {
+          gb_set_error("no CUDA device: libfftw3_gb300 runs transforms on the GPU only");
+          return 0;
+     }
+     gb_lock();
+     g = gb_mkr2r((int)sizeof(R), kind, n, hm, is, idist, os, odist, in, out, flags);
+     if (g && !(flags & FFTW_ESTIMATE) && !gb_dry_run()) gb_tune(g->r2r_inner, flags);
+     gb_unlock();
+     p = PFX(wrap)(g);
+     if (p) p->view = 4;
+     return p;
+}
+
+static PFX(plan) PFX(r2r_multid)(void)
+{
+     gb_set_error("multi-dimensional r2r is not provided by this library (rank 1 only)");
+     return 0;
+}
+
+PFX(plan) PFX(plan_many_r2r)(int rank, const int *n, int howmany, R *in, const int *inembed, int istride, int idist,
+                             R *out, const int *onembed, int ostride, int odist, const PFX(r2r_kind) *kind,
+                             unsigned flags)
+{
+     (void)inembed; (void)onembed;
+     if (rank != 1) return rank > 1 ? PFX(r2r_multid)() : 0;
+     if (!n || !kind || n[0] <= 0 || howmany < 0) return 0;
+     return PFX(r2r_common)((int)kind[0], n[0], howmany, istride, idist, ostride, odist, in, out, flags);
+}
+PFX(plan) PFX(plan_r2r)(int rank, const int *n, R *in, R *out, const PFX(r2r_kind) *kind, unsigned flags)
+{
+     if (rank != 1) return rank > 1 ? PFX(r2r_multid)() : 0;
+     if (!n || !kind || n[0] <= 0) return 0;
+     return PFX(r2r_common)((int)kind[0], n[0], 1, 1, n[0], 1, n[0], in, out, flags);
+}
+PFX(plan) PFX(plan_r2r_1d)(int n, R *in, R *out, PFX(r2r_kind) kind, unsigned flags)
+{
+     if (n <= 0) return 0;
+     return PFX(r2r_common)((int)kind, n, 1, 1, n, 1, n, in, out, flags);
+}
+PFX(plan) PFX(plan_r2r_2d)(int n0, int n1, R *in, R *out, PFX(r2r_kind) kind0, PFX(r2r_kind) kind1, unsigned flags)
+{
+     (void)n0; (void)n1; (void)in; (void)out; (void)kind0; (void)kind1; (void)flags;
+     return PFX(r2r_multid)();
+}
+PFX(plan) PFX(plan_r2r_3d)(int n0, int n1, int n2, R *in, R *out, PFX(r2r_kind) kind0, PFX(r2r_kind) kind1,
+                           PFX(r2r_kind) kind2, unsigned flags)
+{
+     (void)n0; (void)n1; (void)n2; (void)in; (void)out; (void)kind0; (void)kind1; (void)kind2; (void)flags;
+     return PFX(r2r_multid)();
+}
+PFX(plan) PFX(plan_guru_r2r)(int rank, const PFX(iodim) *dims, int howmany_rank, const PFX(iodim) *howmany_dims,
+                             R *in, R *out, const PFX(r2r_kind) *kind, unsigned flags)
+{
+     if (rank != 1 || howmany_rank > 1 || howmany_rank < 0) return rank > 1 ? PFX(r2r_multid)() : 0;
+     if (!dims || !kind || dims[0].n <= 0) return 0;
+     return PFX(r2r_common)((int)kind[0], dims[0].n, howmany_rank ? howmany_dims[0].n : 1, dims[0].is,
+                            howmany_rank ? howmany_dims[0].is : 0, dims[0].os, howmany_rank ? howmany_dims[0].os : 0,
+                            in, out, flags);
+}
+PFX(plan) PFX(plan_guru64_r2r)(int rank, const PFX(iodim64) *dims, int howmany_rank,
+                               const PFX(iodim64) *howmany_dims, R *in, R *out, const PFX(r2r_kind) *kind,
+                               unsigned flags)
+{
+     if (rank != 1 || howmany_rank > 1 || howmany_rank < 0) return rank > 1 ? PFX(r2r_multid)() : 0;
+     if (!dims || !kind || dims[0].n <= 0) return 0;
+     return PFX(r2r_common)((int)kind[0], dims[0].n, howmany_rank ? howmany_dims[0].n : 1, dims[0].is,
+                            howmany_rank ? howmany_dims[0].is : 0, dims[0].os, howmany_rank ? howmany_dims[0].os : 0,
+                            in, out, flags);
+}
 
 /* ---------------------------------------------------------------- execute */
 
 static void PFX(run)(const PFX(plan) p, void *in, void *out, int kind)
 {
      if (!p) return;
-     if (p->view == 3) {
-          gb_set_error("execute: a split-array plan runs through execute or execute_split_dft");
+     if (p->view >= 3) {
+          gb_set_error("execute: a split-array or r2r plan runs through execute, execute_split_dft or execute_r2r");
           fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
           return;
      }
@@ -450,6 +514,7 @@ void PFX(execute)(const PFX(plan) p)
      if (p->view == 3)
           PFX(run_split)(p, (R *)p->g->split_arr[0], (R *)p->g->split_arr[1], (R *)p->g->split_arr[2],
                          (R *)p->g->split_arr[3]);
+     else if (p->view == 4) PFX(execute_r2r)(p, (R *)p->g->prb.in, (R *)p->g->prb.out);
      else PFX(run)(p, p->g->prb.in, p->g->prb.out, -1);
 }
 void PFX(execute_dft)(const PFX(plan) p, C *in, C *out) { PFX(run)(p, in, out, GB_PROB_DFT); }
@@ -470,7 +535,20 @@ void PFX(execute_split_dft)(const PFX(plan) p, R *ri, R *ii, R *ro, R *io_)
 }
 void PFX(execute_split_dft_r2c)(const PFX(plan) p, R *in, R *ro, R *io_) { (void)p; (void)in; (void)ro; (void)io_; }
 void PFX(execute_split_dft_c2r)(const PFX(plan) p, R *ri, R *ii, R *out) { (void)p; (void)ri; (void)ii; (void)out; }
-void PFX(execute_r2r)(const PFX(plan) p, R *in, R *out) { (void)p; (void)in; (void)out; }
+/* api/execute-r2r.c: the plan's transform on new arrays of the same layout */
+void PFX(execute_r2r)(const PFX(plan) p, R *in, R *out)
+{
+     if (!p) return;
+     if (p->view != 4) {
+          gb_set_error("execute_r2r: the plan is not an r2r plan");
+          fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
+          return;
+     }
+     if (gb_execute_r2r(p->g, in, out)) {
+          gb_note_failure();
+          fprintf(stderr, "[fftw_gb300] execute failed: %s\n", gb_last_error());
+     }
+}
 
 PFX(plan) PFX(copy_plan)(PFX(plan) p)
 {

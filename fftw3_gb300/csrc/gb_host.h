@@ -20,7 +20,7 @@
 #define GB_MAXPASS 16
 #define GB_MAXLOOP 8
 
-enum gb_prob_kind { GB_PROB_DFT = 0, GB_PROB_R2C = 1, GB_PROB_C2R = 2 };
+enum gb_prob_kind { GB_PROB_DFT = 0, GB_PROB_R2C = 1, GB_PROB_C2R = 2, GB_PROB_R2R = 3 };
 
 typedef struct { long long n, is, os; } gb_dim;
 
@@ -79,6 +79,11 @@ struct gb_plan {
      void *split_arr[4];        /* ri, ii, ro, io at planning time */
      struct gb_plan *split_inner;
      void *split_buf[2];        /* dense complex input and output of split_inner */
+     /* 1D r2r (fftw_r2r_kind r2r_kind): a pre kernel, the real DFT r2r_inner
+      * on dense buffers, a post kernel */
+     int r2r_kind;
+     struct gb_plan *r2r_inner;
+     void *r2r_buf[2];
      void *stream;              /* cudaStream_t; 0 = legacy default stream */
      int async;                 /* 1: execute does not wait for completion */
      int in_align, out_align;   /* alignment of the planning arrays (bytes, capped at 16) */
@@ -118,6 +123,9 @@ int gb_execute(gb_plan *p, void *in, void *out);
 gb_plan *gb_mksplit(int prec, int rank, const gb_dim *dims, int vrank, const gb_dim *vdims, void *ri, void *ii,
                     void *ro, void *io, unsigned flags);
 int gb_execute_split(gb_plan *p, void *ri, void *ii, void *ro, void *io);
+gb_plan *gb_mkr2r(int prec, int kind, long long n, long long hm, long long is, long long idist, long long os,
+                  long long odist, void *in, void *out, unsigned flags);
+int gb_execute_r2r(gb_plan *p, void *in, void *out);
 
 /* wisdom (gb_wisdom.c) */
 typedef struct gb_wisdom_entry {

@@ -588,7 +588,8 @@ static gb_step *add_pointwise(builder *b, int pw, long long n, long long nfft, i
 {
      gb_plan *p = b->p;
      int prec = p->prb.prec, i;
-     long long L = (pw == GB_PW_HC2C_POST) ? nfft + 1 : (pw == GB_PW_CHIRP_OUT) ? n : nfft;
+     long long L = (pw == GB_PW_HC2C_POST) ? nfft + 1 : (pw == GB_PW_CHIRP_OUT) ? n
+                 : (pw == GB_PW_HALF_COPY) ? n / 2 + 1 : nfft;
      gb_step *s = new_step(b);
      gb_pass *P;
      if (!s) return 0;
@@ -608,7 +609,9 @@ static gb_step *add_pointwise(builder *b, int pw, long long n, long long nfft, i
      P->pw_chunks = (L + 4095) / 4096;
      P->nblocks = P->pw_chunks;
      for (i = 0; i < P->nv; ++i) P->nblocks *= P->vn[i];
-     if (pw == GB_PW_HC2C_POST || pw == GB_PW_HC2C_PRE) {
+     if (pw == GB_PW_PROMOTE || pw == GB_PW_HALF_COPY || pw == GB_PW_HERM_EXT || pw == GB_PW_REAL_PART) {
+          /* no tables */
+     } else if (pw == GB_PW_HC2C_POST || pw == GB_PW_HC2C_PRE) {
           P->tw_half = gb_table_twiddle(prec, 2 * nfft, nfft + 1, 1);
           if (!P->tw_half) { b->err = 1; return 0; }
      } else {
@@ -895,8 +898,9 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           count_ops(p, &s->pass, howmany * n1);
           return;
      }
-     if ((kind == GB_KIND_R2C || kind == GB_KIND_C2R) && rc == 1 && n % 2 == 0) {
-          /* even length beyond one CTA: the half-length complex FFT runs as
+     if ((kind == GB_KIND_R2C || kind == GB_KIND_C2R) && rc != 0 && n % 2 == 0) {
+          /* even length beyond one CTA (or with a prime factor beyond the
+           * stage kernels): the half-length complex FFT runs as
            * its own (multi-pass) c2c on the real array viewed as pairs, and
            * the hc2c post-pass (r2c) or pre-pass (c2r) as an element-wise
            * pass through scratch (rdft/ct-hc2c.c:31-83) */
@@ -928,6 +932,33 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
                add_pointwise(b, GB_PW_HC2C_PRE, n, M, 1, is, 1, nvk, vd, src, GB_BUF_SCRATCH);
                for (i = 0; i < nvk; ++i) { vp[i].n = v[i].n; vp[i].is = vd[i].os; vp[i].os = v[i].os / 2; }
                add_1d_mid(b, GB_KIND_C2C, M, 1, 1, 1, nvk, vp, GB_BUF_SCRATCH, dst, GB_BUF_SCRATCH2);
+          }
+          return;
+     }
+     if ((kind == GB_KIND_R2C || kind == GB_KIND_C2R) && n % 2 == 1 && n <= (prec == 4 ? 4096 : 2048) &&
+         src != GB_BUF_SCRATCH && dst != GB_BUF_SCRATCH && src != GB_BUF_SCRATCH2 && dst != GB_BUF_SCRATCH2) {
+          /* odd length with a prime factor beyond the stage kernels: the real
+           * array as n complex values with zero imaginary parts, one c2c of
+           * length n (Bluestein or Rader in one CTA) in scratch, then the half
+           * spectrum (r2c); c2r extends the half spectrum by Hermitian
+           * symmetry, runs the backward c2c and keeps the real parts */
+          gb_dim vi[GB_MAXRANK + 2], vd[GB_MAXRANK + 2], vo[GB_MAXRANK + 2];
+          long long dense = n;
+          for (i = nvk - 1; i >= 0; --i) {
+               vd[i].n = v[i].n; vd[i].is = dense; vd[i].os = dense;
+               vi[i].n = v[i].n; vi[i].is = v[i].is; vi[i].os = dense;
+               vo[i].n = v[i].n; vo[i].is = dense; vo[i].os = v[i].os;
+               dense *= v[i].n;
+          }
+          need_scratch(p, GB_BUF_SCRATCH, (size_t)dense * csize(prec));
+          if (kind == GB_KIND_R2C) {
+               if (!add_pointwise(b, GB_PW_PROMOTE, n, n, -1, is, 1, nvk, vi, src, GB_BUF_SCRATCH)) return;
+               add_1d_mid(b, GB_KIND_C2C, n, -1, 1, 1, nvk, vd, GB_BUF_SCRATCH, GB_BUF_SCRATCH, GB_BUF_SCRATCH2);
+               if (!b->err) add_pointwise(b, GB_PW_HALF_COPY, n, n, -1, 1, os, nvk, vo, GB_BUF_SCRATCH, dst);
+          } else {
+               if (!add_pointwise(b, GB_PW_HERM_EXT, n, n, 1, is, 1, nvk, vi, src, GB_BUF_SCRATCH)) return;
+               add_1d_mid(b, GB_KIND_C2C, n, 1, 1, 1, nvk, vd, GB_BUF_SCRATCH, GB_BUF_SCRATCH, GB_BUF_SCRATCH2);
+               if (!b->err) add_pointwise(b, GB_PW_REAL_PART, n, n, 1, 1, os, nvk, vo, GB_BUF_SCRATCH, dst);
           }
           return;
      }
@@ -1115,5 +1146,8 @@ void gb_destroy(gb_plan *p)
           if (p->split_buf[i] && !gb_dry) cudaFree(p->split_buf[i]);
      }
      if (p->split_inner) gb_destroy(p->split_inner);
+     if (p->r2r_inner) gb_destroy(p->r2r_inner);
+     for (i = 0; i < 2; ++i)
+          if (p->r2r_buf[i] && !gb_dry) cudaFree(p->r2r_buf[i]);
      free(p);
 }

@@ -37,7 +37,11 @@ enum gb_pw {
      GB_PW_HC2C_PRE = 1,    /* c2r: X (n/2+1) -> Z' (n/2): hc2c pre-pass */
      GB_PW_CHIRP_IN = 2,    /* Bluestein: x conj(w), zero-padded to nfft */
      GB_PW_SPEC_MUL = 3,    /* Bluestein: multiply by the chirp spectrum, in place */
-     GB_PW_CHIRP_OUT = 4    /* Bluestein: conv conj(w), first n */
+     GB_PW_CHIRP_OUT = 4,   /* Bluestein: conv conj(w), first n */
+     GB_PW_PROMOTE = 5,     /* odd r2c: n reals -> n complex with zero imaginary parts */
+     GB_PW_HALF_COPY = 6,   /* odd r2c: first n/2+1 of n complex */
+     GB_PW_HERM_EXT = 7,    /* odd c2r: n/2+1 complex -> n complex, X[n-k] = conj X[k] */
+     GB_PW_REAL_PART = 8    /* odd c2r: n complex -> n reals (real parts) */
 };
 
 /* How the transform is computed inside one CTA. */
@@ -155,6 +159,11 @@ const char *gb_last_cuda_error(void);
 long long gb_launch_count(void);
 int gb_device_status(void);
 int *gb_device_status_ptr(void);
+/* 1D r2r pre- and post-processing around the real DFT (fft_r2r.cu) */
+int gb_r2r_pre(int prec, int kind, long long n, long long hm, const void *in, long long is, long long idist, void *buf,
+               void *stream);
+int gb_r2r_post(int prec, int kind, long long n, long long hm, const void *buf, void *out, long long os, long long odist,
+                void *stream);
 
 #ifdef __cplusplus
 }

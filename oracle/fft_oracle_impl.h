@@ -580,3 +580,59 @@ void P(twiddle)(I m, I n, int sign, R *out2)
      out2[0] = (R)c;
      out2[1] = (R)(sign < 0 ? -s : s);
 }
+
+/* r2r kinds by their defining sums, O(n^2) per transform with the trig
+ * argument reduced exactly (cos/sin of 2 pi m / M with integer m, M), as the
+ * reference's manual states them (doc/reference.texi:1923-2020 R2HC/HC2R,
+ * 2022-2175 REDFT, 2176-2300 RODFT, and the DHT); kinds use the
+ * fftw_r2r_kind values (api/fftw3.h:96-100).  Returns -1 for a kind not
+ * restated here. */
+static T r2r_cos(I m, I M) { T c, s; m %= M; if (m < 0) m += M; cexp_t(m, M, &c, &s); return c; }
+static T r2r_sin(I m, I M) { T c, s; m %= M; if (m < 0) m += M; cexp_t(m, M, &c, &s); return s; }
+
+int P(r2r)(int kind, I n, I howmany, const R *in, R *out)
+{
+     I t, j, k;
+     for (t = 0; t < howmany; ++t) {
+          const R *x = in + t * n;
+          R *y = out + t * n;
+          for (k = 0; k < n; ++k) {
+               T acc = 0;
+               switch (kind) {
+               case 0: /* R2HC: Re Y_k (k <= n/2), Im Y_{n-k} at n-k */
+                    if (2 * k <= n) for (j = 0; j < n; ++j) acc += (T)x[j] * r2r_cos(j * k, n);
+                    else for (j = 0; j < n; ++j) acc -= (T)x[j] * r2r_sin(j * (n - k), n);
+                    break;
+               case 1: /* HC2R: backward DFT of the Hermitian array held in halfcomplex order */
+                    for (j = 0; j < n; ++j) {
+                         T re, im;
+                         if (2 * j <= n) { re = x[j]; im = (j == 0 || 2 * j == n) ? 0 : x[n - j]; }
+                         else { re = x[n - j]; im = -(T)x[j]; }
+                         acc += re * r2r_cos(j * k, n) - im * r2r_sin(j * k, n);
+                    }
+                    break;
+               case 2: /* DHT: sum x_j (cos + sin)(2 pi j k / n) */
+                    for (j = 0; j < n; ++j) acc += (T)x[j] * (r2r_cos(j * k, n) + r2r_sin(j * k, n));
+                    break;
+               case 4: /* REDFT01: x_0 + 2 sum_{j>=1} x_j cos(pi j (2k+1) / 2n) */
+                    acc = x[0];
+                    for (j = 1; j < n; ++j) acc += 2 * (T)x[j] * r2r_cos(j * (2 * k + 1), 4 * n);
+                    break;
+               case 5: /* REDFT10: 2 sum x_j cos(pi (2j+1) k / 2n) */
+                    for (j = 0; j < n; ++j) acc += 2 * (T)x[j] * r2r_cos((2 * j + 1) * k, 4 * n);
+                    break;
+               case 8: /* RODFT01: (-1)^k x_{n-1} + 2 sum_{j<n-1} x_j sin(pi (j+1)(2k+1) / 2n) */
+                    acc = (k & 1) ? -(T)x[n - 1] : (T)x[n - 1];
+                    for (j = 0; j + 1 < n; ++j) acc += 2 * (T)x[j] * r2r_sin((j + 1) * (2 * k + 1), 4 * n);
+                    break;
+               case 9: /* RODFT10: 2 sum x_j sin(pi (2j+1)(k+1) / 2n) */
+                    for (j = 0; j < n; ++j) acc += 2 * (T)x[j] * r2r_sin((2 * j + 1) * (k + 1), 4 * n);
+                    break;
+               default:
+                    return -1;
+               }
+               y[k] = (R)acc;
+          }
+     }
+     return 0;
+}

@@ -71,6 +71,7 @@ class Restatement:
                 getattr(lib, f"orc_{p}_c2r").argtypes = [ctypes.c_int, ctypes.c_void_p, I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
                 getattr(lib, f"orc_{p}_dft_method").argtypes = [I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
                 getattr(lib, f"orc_{p}_twiddle").argtypes = [I, I, ctypes.c_int, ctypes.c_void_p]
+                getattr(lib, f"orc_{p}_r2r").argtypes = [ctypes.c_int, I, I, ctypes.c_void_p, ctypes.c_void_p]
             Restatement._lib = lib
         self.lib = Restatement._lib
 
@@ -108,6 +109,15 @@ class Restatement:
         n = (ctypes.c_int * len(shape))(*shape)
         rc = getattr(self.lib, f"orc_{prec}_c2r")(len(shape), n, howmany, x.ctypes.data, y.ctypes.data, nthreads)
         assert rc == 0
+        return y
+
+    def r2r(self, x, n, kind, prec="d"):
+        """Batched 1D r2r of length n by its defining sum (kinds: fftw_r2r_kind values)."""
+        rt, _ = _PREC[prec]
+        x = _as(x, rt)
+        y = np.empty(x.size, dtype=rt)
+        rc = getattr(self.lib, f"orc_{prec}_r2r")(int(kind), int(n), x.size // int(n), x.ctypes.data, y.ctypes.data)
+        assert rc == 0, f"r2r kind {kind} is not restated"
         return y
 
     def dft_method(self, x, sign=FFTW_FORWARD, method=1, prec="d"):

@@ -60,9 +60,15 @@ def test_invalid_arguments_return_null(lib):
             assert not f(1, n, -1, 16, None, 1, 64, 32, None, 1, 64, -1, g.FFTW_ESTIMATE)
             assert not f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, 0, g.FFTW_ESTIMATE)   # sign must be +-1
             assert f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, -1, g.FFTW_ESTIMATE)
-            # r2r and split planners exist but return NULL
-            kinds = (ctypes.c_int * 1)(0)
-            assert not getattr(lib, pfx + "plan_many_r2r")(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, kinds, 64)
+            # r2r: rank 1 of the kinds built here; other kinds and rank > 1 return NULL
+            f = getattr(lib, pfx + "plan_many_r2r")
+            f.restype = ctypes.c_void_p
+            for kind, ok in ((0, True), (1, True), (2, True), (4, True), (5, True), (8, True), (9, True),
+                             (3, False), (6, False), (7, False), (10, False)):
+                kinds = (ctypes.c_int * 2)(kind, kind)
+                assert bool(f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, kinds, 64)) == ok, kind
+            n2 = (ctypes.c_int * 2)(8, 8)
+            assert not f(2, n2, 1, 16, None, 1, 64, 32, None, 1, 64, (ctypes.c_int * 2)(5, 5), 64)
     finally:
         g.set_dry_run(False)
 

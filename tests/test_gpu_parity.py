@@ -226,7 +226,8 @@ def test_strided_embedded(lib, torch_cuda, restatement):
     assert rel_l2(_host(yo), ref) <= 1e-6
 
 
-R2C_SIZES = [2, 4, 6, 15, 16, 30, 64, 100, 1024, 1000, 4096, 16384, 32768]
+R2C_SIZES = [2, 4, 6, 15, 16, 30, 64, 100, 1024, 1000, 4096, 16384, 32768,
+             17, 97, 1021, 34, 2042]   # odd and even lengths with a prime factor > 13
 
 
 @pytest.mark.parametrize("prec", ["f", "d"])

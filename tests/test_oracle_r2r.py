@@ -1,0 +1,41 @@
+"""The oracle's r2r restatement against the defining sums of the reference
+manual, evaluated independently here with numpy in float64 (CPU only)."""
+import numpy as np
+import pytest
+
+KINDS = {0: "R2HC", 1: "HC2R", 2: "DHT", 4: "REDFT01", 5: "REDFT10", 8: "RODFT01", 9: "RODFT10"}
+
+
+def definition(kind, x):
+    n = len(x)
+    j = np.arange(n)
+    k = j[:, None]
+    if kind == 0:
+        X = np.fft.fft(x)
+        return np.concatenate([X.real[: n // 2 + 1], X.imag[1:(n + 1) // 2][::-1]])
+    if kind == 1:
+        X = np.zeros(n, dtype=complex)
+        X[: n // 2 + 1] = x[: n // 2 + 1]
+        for m in range(1, (n + 1) // 2):
+            X[m] += 1j * x[n - m]
+            X[n - m] = np.conj(X[m])
+        return np.real(np.fft.ifft(X) * n)
+    if kind == 2:
+        return (np.cos(2 * np.pi * j * k / n) + np.sin(2 * np.pi * j * k / n)) @ x
+    if kind == 4:
+        return x[0] + 2 * np.cos(np.pi * j[1:] * (2 * k + 1) / (2 * n)) @ x[1:]
+    if kind == 5:
+        return 2 * np.cos(np.pi * (2 * j + 1) * k / (2 * n)) @ x
+    if kind == 8:
+        return ((-1.0) ** j) * x[-1] + 2 * np.sin(np.pi * (j[:-1] + 1) * (2 * k + 1) / (2 * n)) @ x[:-1]
+    return 2 * np.sin(np.pi * (2 * j + 1) * (k + 1) / (2 * n)) @ x
+
+
+@pytest.mark.parametrize("kind", sorted(KINDS), ids=[KINDS[k] for k in sorted(KINDS)])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 7, 16, 33, 100])
+def test_r2r_oracle_matches_definition(restatement, kind, n):
+    rng = np.random.default_rng(n * 16 + kind)
+    x = rng.standard_normal((3, n))
+    y = restatement.r2r(x.ravel(), n, kind, "l").astype(np.float64).reshape(3, n)
+    ref = np.stack([definition(kind, r) for r in x])
+    assert np.abs(y - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
