@@ -224,10 +224,7 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
                     float2 y[16];
 #pragma unroll
                     for (int q = 0; q < 16; ++q) y[q] = make_float2(v[q] * inv, v[16 + q] * inv);
-                    if (P.post_N) {
-#pragma unroll
-                         for (int q = 0; q < 16; ++q) y[q] = cmul(y[q], post_twiddle<float2>(P, (P.post_vdim ? tile.vpost : vv) * (long long)(j + q * T)));
-                    }
+                    if (P.post_N) apply_post_twiddles<float2, 16, T>(P, P.post_vdim ? tile.vpost : vv, j, y);
                     if (P.store_mode == GB_MOVE_DIRECT) {
                          if (vv < P.vn[0]) {
                               float2 *o = (float2 *)out + tile.bo + vv * P.vos[0] + j;
