@@ -74,6 +74,10 @@ def _sigs(lib, pfx):
     f("plan_guru_split_dft", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, vp, vp, cu])
     f("plan_guru64_split_dft", vp, [ci, ctypes.POINTER(IODim64), ci, ctypes.POINTER(IODim64), vp, vp, vp, vp, cu])
     f("execute_split_dft", None, [vp, vp, vp, vp, vp])
+    f("plan_guru_split_dft_r2c", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, vp, cu])
+    f("plan_guru_split_dft_c2r", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, vp, cu])
+    f("execute_split_dft_r2c", None, [vp, vp, vp, vp])
+    f("execute_split_dft_c2r", None, [vp, vp, vp, vp])
     f("execute", None, [vp])
     f("execute_dft", None, [vp, vp, vp])
     f("execute_dft_r2c", None, [vp, vp, vp])
@@ -177,6 +181,12 @@ class Plan:
     def execute_split_dft(self, ri, ii, ro, io):
         self._f("execute_split_dft")(self.ptr, ri, ii, ro, io)
 
+    def execute_split_dft_r2c(self, inp, ro, io):
+        self._f("execute_split_dft_r2c")(self.ptr, inp, ro, io)
+
+    def execute_split_dft_c2r(self, ri, ii, out):
+        self._f("execute_split_dft_c2r")(self.ptr, ri, ii, out)
+
     def set_stream(self, stream_ptr: int):
         return self._f("gb300_set_stream")(self.ptr, stream_ptr)
 
@@ -273,6 +283,26 @@ def plan_guru_split_dft(dims, howmany_dims, ri, ii, ro, io, flags=FFTW_ESTIMATE,
     d = (IODim * max(1, len(dims)))(*[IODim(*x) for x in dims])
     h = (IODim * max(1, len(howmany_dims)))(*[IODim(*x) for x in howmany_dims])
     p = getattr(lib, pfx + "plan_guru_split_dft")(len(dims), d, len(howmany_dims), h, ri, ii, ro, io, flags)
+    return Plan(p, prec)
+
+
+def plan_guru_split_dft_r2c(dims, howmany_dims, inp, ro, io, flags=FFTW_ESTIMATE, prec="f") -> Plan:
+    """r2c of the real array inp into ro + i*io (last dim n/2+1); (n, is, os) strides in reals."""
+    lib = load()
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    d = (IODim * max(1, len(dims)))(*[IODim(*x) for x in dims])
+    h = (IODim * max(1, len(howmany_dims)))(*[IODim(*x) for x in howmany_dims])
+    p = getattr(lib, pfx + "plan_guru_split_dft_r2c")(len(dims), d, len(howmany_dims), h, inp, ro, io, flags)
+    return Plan(p, prec)
+
+
+def plan_guru_split_dft_c2r(dims, howmany_dims, ri, ii, out, flags=FFTW_ESTIMATE, prec="f") -> Plan:
+    """c2r of ri + i*ii (last dim n/2+1) into the real array out; (n, is, os) strides in reals."""
+    lib = load()
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    d = (IODim * max(1, len(dims)))(*[IODim(*x) for x in dims])
+    h = (IODim * max(1, len(howmany_dims)))(*[IODim(*x) for x in howmany_dims])
+    p = getattr(lib, pfx + "plan_guru_split_dft_c2r")(len(dims), d, len(howmany_dims), h, ri, ii, out, flags)
     return Plan(p, prec)
 
 

@@ -9,9 +9,10 @@
  * fftw_import_wisdom_from_filename or the system wisdom file.
  *
  * Size syntax (as the reference's): <type><inplace><direction><geometry>,
- * type c (complex) or r (r2c forward / c2r backward), inplace i or o,
- * direction f or b, geometry n1[xn2[x...]].  r2r (type k) is not on this
- * library's path and is reported as unsupported.
+ * type c (complex), r (r2c forward / c2r backward) or k (r2r, no
+ * direction), inplace i or o, direction f or b, geometry n1[xn2[x...]];
+ * for k each dim is followed by its kind, f/b/h/e00/e01/e10/e11/o00/o01/
+ * o10/o11 for R2HC/HC2R/DHT/REDFT00/.../RODFT11 (R2HC when omitted).
  *
  * Built twice by fftw3_gb300/build.py: with GB_TOOL_SINGLE for the fftwf_
  * API, without for fftw_.
@@ -65,8 +66,11 @@ static void usage(FILE *f)
              "  -w FILE, --wisdom-file=FILE  read wisdom from FILE first (- for stdin)\n"
              "  -T N, --threads=N          accepted; the GPU replaces the thread pool\n\n"
              "Size syntax: <type><inplace><direction><geometry>\n"
-             "  <type> = c or r (complex, or real r2c/c2r); <inplace> = i or o;\n"
-             "  <direction> = f or b; <geometry> = n1[xn2[x...]], e.g. cof4096, rib512x512\n"
+             "  <type> = c, r or k (complex, real r2c/c2r, or r2r); <inplace> = i or o;\n"
+             "  <direction> = f or b (omitted for k); <geometry> = n1[xn2[x...]],\n"
+             "  e.g. cof4096, rib512x512; for k each dim is followed by its kind,\n"
+             "  f/b/h/e00/e01/e10/e11/o00/o01/o10/o11 (R2HC/HC2R/DHT/REDFT00/.../RODFT11),\n"
+             "  e.g. koe10x16o11\n"
              "  Sizes may also be read from stdin by giving - as a size.\n");
 }
 
@@ -74,7 +78,32 @@ typedef struct {
      char type, place, dir;
      int rank;
      int n[8];
+     int kind[8];           /* r2r kinds (fftw_r2r_kind values) */
 } problem;
+
+/* an r2r kind after a dim of a k size: f, b, h, e<ab>, o<ab> */
+static int parse_kind(const char **q, int *kind)
+{
+     const char c = **q;
+     char *end;
+     long ab;
+     *kind = FFTW_R2HC;
+     if (c == 'f' || c == 'b' || c == 'h') {
+          *kind = c == 'f' ? FFTW_R2HC : c == 'b' ? FFTW_HC2R : FFTW_DHT;
+          ++*q;
+          return 0;
+     }
+     if (c != 'e' && c != 'o') return 0;
+     ab = strtol(*q + 1, &end, 10);
+     if (end == *q + 1) return -1;
+     *q = end;
+     if (ab == 0) *kind = c == 'e' ? FFTW_REDFT00 : FFTW_RODFT00;
+     else if (ab == 1) *kind = c == 'e' ? FFTW_REDFT01 : FFTW_RODFT01;
+     else if (ab == 10) *kind = c == 'e' ? FFTW_REDFT10 : FFTW_RODFT10;
+     else if (ab == 11) *kind = c == 'e' ? FFTW_REDFT11 : FFTW_RODFT11;
+     else return -1;
+     return 0;
+}
 
 static int parse(const char *s, problem *p)
 {
@@ -84,13 +113,20 @@ static int parse(const char *s, problem *p)
      if (strlen(s) < 4) return -1;
      p->type = *q++;
      p->place = *q++;
-     p->dir = *q++;
-     if ((p->type != 'c' && p->type != 'r') || (p->place != 'i' && p->place != 'o') || (p->dir != 'f' && p->dir != 'b'))
+     p->dir = p->type == 'k' ? 'f' : *q++;
+     if ((p->type != 'c' && p->type != 'r' && p->type != 'k') || (p->place != 'i' && p->place != 'o') ||
+         (p->dir != 'f' && p->dir != 'b'))
           return -1;
      for (;;) {
           long v = strtol(q, &end, 10);
           if (end == q || v <= 0 || v > (1L << 30) || p->rank >= 8) return -1;
-          p->n[p->rank++] = (int)v;
+          p->n[p->rank] = (int)v;
+          if (p->type == 'k') {
+               const char *e = end;
+               if (parse_kind(&e, &p->kind[p->rank])) return -1;
+               end = (char *)e;
+          }
+          p->rank++;
           if (*end == 'x') { q = end + 1; continue; }
           if (*end) return -1;
           break;
@@ -109,7 +145,14 @@ static int plan_one(const problem *p, unsigned flags, int verbose, const char *s
      for (i = 0; i < p->rank; ++i) tot *= (size_t)p->n[i];
      last = (size_t)p->n[p->rank - 1];
      if (verbose) fprintf(stderr, "Planning transform: %s\n", spec);
-     if (p->type == 'c') {
+     if (p->type == 'k') {
+          FX(r2r_kind) k[8];
+          for (i = 0; i < p->rank; ++i) k[i] = (FX(r2r_kind))p->kind[i];
+          in = FX(malloc)(tot * sizeof(real_t));
+          out = p->place == 'i' ? in : FX(malloc)(tot * sizeof(real_t));
+          if (!in || !out) return -1;
+          pl = FX(plan_r2r)(p->rank, p->n, (real_t *)in, (real_t *)out, k, flags);
+     } else if (p->type == 'c') {
           in = FX(malloc)(tot * sizeof(cpx_t));
           out = p->place == 'i' ? in : FX(malloc)(tot * sizeof(cpx_t));
           if (!in || !out) return -1;
@@ -205,7 +248,7 @@ int main(int argc, char **argv)
                break;
           }
           if (parse(probs[i], &p)) {
-               fprintf(stderr, TOOL_NAME ": cannot parse size %s (r2r sizes are not supported)\n", probs[i]);
+               fprintf(stderr, TOOL_NAME ": cannot parse size %s\n", probs[i]);
                failed = 1;
                continue;
           }

@@ -95,8 +95,8 @@ __global__ void __launch_bounds__(256) k_pointwise(const gb_pass P, const void *
      typedef typename real_of<C>::T R;
      const int M = P.nfft;
      const int L = (P.pw == GB_PW_HC2C_POST) ? M + 1
-                 : (P.pw == GB_PW_CHIRP_OUT) ? P.n
-                 : (P.pw == GB_PW_HALF_COPY) ? P.n / 2 + 1 : M;
+                 : (P.pw == GB_PW_CHIRP_OUT || P.pw == GB_PW_CHIRP_OUT_REAL) ? P.n
+                 : (P.pw == GB_PW_HALF_COPY || P.pw == GB_PW_CHIRP_OUT_HALF) ? P.n / 2 + 1 : M;
      for (long long blk = blockIdx.x; blk < P.nblocks; blk += gridDim.x) {
           const long long tr = blk / P.pw_chunks;
           const int k0 = (int)(blk - tr * P.pw_chunks) * 4096;
@@ -104,11 +104,11 @@ __global__ void __launch_bounds__(256) k_pointwise(const gb_pass P, const void *
           const long long ioff = tile.bi + tile.v0 * P.vis[0], ooff = tile.bo + tile.v0 * P.vos[0];
           const C *src = (const C *)in + ioff;
           C *dst = (C *)out + ooff;
+          /* real transforms around a c2c or a convolution: offsets and strides
+           * of the real side count reals */
+          const R *rs = (const R *)in + ioff;
+          R *rd = (R *)out + ooff;
           if (P.pw == GB_PW_PROMOTE || P.pw == GB_PW_REAL_PART || P.pw == GB_PW_HERM_EXT || P.pw == GB_PW_HALF_COPY) {
-               /* odd-length real transforms around a c2c: offsets and strides of
-                * the real side count reals */
-               const R *rs = (const R *)in + ioff;
-               R *rd = (R *)out + ooff;
                for (int k = k0 + threadIdx.x; k < L && k < k0 + 4096; k += blockDim.x) {
                     if (P.pw == GB_PW_PROMOTE) dst[(long long)k * P.os] = mk<C>(rs[(long long)k * P.is], (R)0);
                     else if (P.pw == GB_PW_REAL_PART) rd[(long long)k * P.os] = src[(long long)k * P.is].x;
@@ -140,10 +140,27 @@ __global__ void __launch_bounds__(256) k_pointwise(const gb_pass P, const void *
                     y = mk<C>(sm.x - cd.y, sm.y + cd.x);
                } else if (P.pw == GB_PW_CHIRP_IN) {
                     y = (k < P.n) ? cmul(src[(long long)k * P.is], cconj(__ldg((const C *)P.chirp + k))) : mk<C>(0, 0);
+               } else if (P.pw == GB_PW_CHIRP_IN_REAL) {
+                    y = (k < P.n) ? cscale(cconj(__ldg((const C *)P.chirp + k)), rs[(long long)k * P.is]) : mk<C>(0, 0);
+               } else if (P.pw == GB_PW_CHIRP_IN_HERM) {
+                    y = mk<C>(0, 0);
+                    if (k < P.n) {
+                         /* X_k = X_h (k <= n/2) or conj X_{n-k}; the imaginary
+                          * parts of X_0 and X_{n/2} are ignored */
+                         const int h = (2 * k <= P.n) ? k : P.n - k;
+                         C z = src[(long long)h * P.is];
+                         if (k == 0 || 2 * k == P.n) z.y = 0;
+                         else if (h != k) z.y = -z.y;
+                         y = cmul(z, cconj(__ldg((const C *)P.chirp + k)));
+                    }
                } else if (P.pw == GB_PW_SPEC_MUL) {
                     y = cmul(src[(long long)k * P.is], __ldg((const C *)P.chirp_spec + k));
                } else {
                     y = cmul(src[(long long)k * P.is], cconj(__ldg((const C *)P.chirp + k)));
+                    if (P.pw == GB_PW_CHIRP_OUT_REAL) {
+                         rd[(long long)k * P.os] = y.x;
+                         continue;
+                    }
                }
                dst[(long long)k * P.os] = y;
           }
@@ -200,8 +217,13 @@ __global__ void k_split_copy(const gb_split_dims D, long long total, R *re, R *i
                o += (rest - q * D.n[d]) * D.s[d];
                rest = q;
           }
-          if (PACK) b[L] = mk<C>(re[o], im[o]);
-          else {
+          if (!im) {
+               /* one real array: dense reals in buf */
+               if (PACK) ((R *)buf)[L] = re[o];
+               else re[o] = ((const R *)buf)[L];
+          } else if (PACK) {
+               b[L] = mk<C>(re[o], im[o]);
+          } else {
                const C v = b[L];
                re[o] = v.x;
                im[o] = v.y;
@@ -432,7 +454,10 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           const char *bad = 0;
           if (p->kind == GB_KIND_POINTWISE) {
                if ((p->pw == GB_PW_HC2C_POST || p->pw == GB_PW_HC2C_PRE) && !p->tw_half) bad = "hc2c table missing";
-               else if ((p->pw == GB_PW_CHIRP_IN || p->pw == GB_PW_CHIRP_OUT) && !p->chirp) bad = "chirp missing";
+               else if ((p->pw == GB_PW_CHIRP_IN || p->pw == GB_PW_CHIRP_OUT || p->pw == GB_PW_CHIRP_IN_REAL ||
+                         p->pw == GB_PW_CHIRP_IN_HERM || p->pw == GB_PW_CHIRP_OUT_HALF ||
+                         p->pw == GB_PW_CHIRP_OUT_REAL) && !p->chirp)
+                    bad = "chirp missing";
                else if (p->pw == GB_PW_SPEC_MUL && !p->chirp_spec) bad = "chirp spectrum missing";
                else if (p->pw_chunks < 1 || p->threads != 256 || p->tb != 1) bad = "bad pointwise launch shape";
           } else if (p->kind != GB_KIND_COPY && !p->tw) bad = "twiddle table missing";

@@ -1,27 +1,34 @@
 /*
- * Pre- and post-processing kernels of the 1D r2r transforms that run as a
- * real DFT of the same length n (see gb_r2r.c for the algorithms and the
- * reference definitions).  Each thread handles one output element of one
- * transform of the batch; twiddles exp(+-i pi k / 2n) come from the FP64
- * octant-reduced cexp rounded once.
+ * Pre- and post-processing kernels of the r2r transforms.  Each kind of
+ * length n runs as one core transform of length L (gb_r2r_core) on dense
+ * buffers between these two kernels; gb_r2r.c holds the algorithms with the
+ * reference definitions.  Each thread handles one element of one transform
+ * of the batch; the batch is a vector loop of up to GB_R2R_MAXV dims with
+ * strides in reals.  Twiddles exp(+-i pi m / 2n) and exp(-i pi m / 4n) come
+ * from the FP64 octant-reduced cexp rounded once.
  *
- * Buffers: v (pre output / r2c input) dense real [hm][n]; V (r2c output /
- * c2r input) dense complex [hm][n/2+1].
+ * Core buffers per transform (row t of the batch):
+ *   r2c core: pre writes L reals, post reads L/2+1 complex
+ *   c2r core: pre writes L/2+1 complex, post reads L reals
+ *   c2c core: pre writes L complex, post reads L complex
  */
 #include <cuda_runtime.h>
 #include "fft_kernels.cuh"
 
 namespace gb {
 
-enum { R2R_R2HC = 0, R2R_HC2R = 1, R2R_DHT = 2, R2R_REDFT01 = 4, R2R_REDFT10 = 5, R2R_RODFT01 = 8, R2R_RODFT10 = 9 };
+enum {
+     R2R_R2HC = 0, R2R_HC2R = 1, R2R_DHT = 2, R2R_REDFT00 = 3, R2R_REDFT01 = 4, R2R_REDFT10 = 5, R2R_REDFT11 = 6,
+     R2R_RODFT00 = 7, R2R_RODFT01 = 8, R2R_RODFT10 = 9, R2R_RODFT11 = 10
+};
 
-/* exp(i pi k / 2n) for dir > 0, exp(-i pi k / 2n) for dir < 0 */
+/* exp(dir * 2 pi i m / M), rounded once from FP64 */
 template <typename C>
-__device__ __forceinline__ C quarter_twiddle(long long k, long long n, int dir)
+__device__ __forceinline__ C r2r_twiddle(long long m, long long M, int dir)
 {
      typedef typename real_of<C>::T R;
      double c, s;
-     cexp_fp64(k, 4 * n, dir, &c, &s);
+     cexp_fp64(m, M, dir, &c, &s);
      return mk<C>((R)c, (R)s);
 }
 
@@ -34,17 +41,31 @@ __device__ __forceinline__ C half_spec(const C *V, long long n, long long k)
      return mk<C>(z.x, -z.y);
 }
 
+/* element offset (reals) of vector index t on the input (out = 0) or output side */
+__device__ __forceinline__ long long vec_offset(const gb_r2r_vec &v, long long t, int out)
+{
+     if (v.nv == 1) return t * (out ? v.os[0] : v.is[0]);
+     long long off = 0;
+     for (int d = v.nv - 1; d >= 0; --d) {
+          const long long i = t % v.n[d];
+          t /= v.n[d];
+          off += i * (out ? v.os[d] : v.is[d]);
+     }
+     return off;
+}
+
 template <typename R>
-__global__ void k_r2r_pre(int kind, long long n, long long hm, const R *__restrict__ in, long long is, long long idist,
-                          void *__restrict__ buf)
+__global__ void k_r2r_pre(int kind, long long n, long long L, long long V, const R *__restrict__ in, long long is,
+                          const gb_r2r_vec vec, void *__restrict__ buf)
 {
      typedef typename cplx_of<R>::T C;
-     const long long nc = n / 2 + 1;
-     const long long per = (kind == R2R_HC2R || kind == R2R_REDFT01 || kind == R2R_RODFT01) ? nc : n;
-     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < per * hm;
+     long long Lc;
+     const int core = gb_r2r_core(kind, n, &Lc);
+     const long long per = core == GB_R2R_CORE_C2R ? L / 2 + 1 : L;
+     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < per * V;
           g += (long long)gridDim.x * blockDim.x) {
           const long long t = g / per, m = g - t * per;
-          const R *x = in + t * idist;
+          const R *x = in + vec_offset(vec, t, 0);
           switch (kind) {
           case R2R_R2HC:
           case R2R_DHT:
@@ -60,6 +81,19 @@ __global__ void k_r2r_pre(int kind, long long n, long long hm, const R *__restri
                ((R *)buf)[g] = v;
                break;
           }
+          case R2R_REDFT00:
+               /* even extension of length 2(n-1): e_m = x_m, e_{L-m} = x_m */
+               ((R *)buf)[g] = x[(m < n ? m : L - m) * is];
+               break;
+          case R2R_RODFT00: {
+               /* odd extension of length 2(n+1): o_0 = o_{n+1} = 0,
+                * o_{m} = x_{m-1}, o_{L-1-j} = -x_j */
+               R v = (R)0;
+               if (m >= 1 && m <= n) v = x[(m - 1) * is];
+               else if (m > n + 1) v = -x[(L - 1 - m) * is];
+               ((R *)buf)[g] = v;
+               break;
+          }
           case R2R_HC2R: {
                /* X_0 = h_0, X_k = h_k + i h_{n-k}, X_{n/2} = h_{n/2} (even n) */
                const R re = x[m * is];
@@ -67,15 +101,37 @@ __global__ void k_r2r_pre(int kind, long long n, long long hm, const R *__restri
                ((C *)buf)[g] = mk<C>(re, im);
                break;
           }
-          default: {
+          case R2R_REDFT01:
+          case R2R_RODFT01: {
                /* REDFT01: V_k = (x_k - i x_{n-k}) exp(i pi k / 2n), x_n = 0;
                 * RODFT01 on x reversed */
                const bool rev = (kind == R2R_RODFT01);
                const R a = x[(rev ? n - 1 - m : m) * is];
                const R b = (m == 0) ? (R)0 : x[(rev ? m - 1 : n - m) * is];
-               const C w = quarter_twiddle<C>(m, n, 1);
+               const C w = r2r_twiddle<C>(m, 4 * n, 1);
                /* (a - i b) * w */
                ((C *)buf)[g] = mk<C>(a * w.x + b * w.y, a * w.y - b * w.x);
+               break;
+          }
+          default: {
+               /* REDFT11 (RODFT11 on x reversed).  Even n: z_m = (x_{2m} +
+                * i x_{n-1-2m}) exp(-i pi (4m+1) / 4n), m < n/2.  Odd n: z_m =
+                * x_m exp(-i pi m / 2n) for m < n, zero up to 2n. */
+               const bool rev = (kind == R2R_RODFT11);
+               C z;
+               if (!(n & 1)) {
+                    const long long ja = 2 * m, jb = n - 1 - 2 * m;
+                    const R a = x[(rev ? jb : ja) * is], b = x[(rev ? ja : jb) * is];
+                    const C w = r2r_twiddle<C>(4 * m + 1, 8 * n, -1);
+                    z = mk<C>(a * w.x - b * w.y, a * w.y + b * w.x);
+               } else if (m < n) {
+                    const R a = x[(rev ? n - 1 - m : m) * is];
+                    const C w = r2r_twiddle<C>(m, 4 * n, -1);
+                    z = mk<C>(a * w.x, a * w.y);
+               } else {
+                    z = mk<C>((R)0, (R)0);
+               }
+               ((C *)buf)[g] = z;
                break;
           }
           }
@@ -83,24 +139,26 @@ __global__ void k_r2r_pre(int kind, long long n, long long hm, const R *__restri
 }
 
 template <typename R>
-__global__ void k_r2r_post(int kind, long long n, long long hm, const void *__restrict__ buf, R *__restrict__ out,
-                           long long os, long long odist)
+__global__ void k_r2r_post(int kind, long long n, long long L, long long V, const void *__restrict__ buf,
+                           R *__restrict__ out, long long os, const gb_r2r_vec vec)
 {
      typedef typename cplx_of<R>::T C;
-     const long long nc = n / 2 + 1;
-     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n * hm;
+     long long Lc;
+     const int core = gb_r2r_core(kind, n, &Lc);
+     const long long rowc = core == GB_R2R_CORE_R2C ? L / 2 + 1 : L;   /* complex row length */
+     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n * V;
           g += (long long)gridDim.x * blockDim.x) {
           const long long t = g / n, k = g - t * n;
-          R *y = out + t * odist;
-          const C *V = (const C *)buf + t * nc;
-          const R *v = (const R *)buf + t * n;
+          R *y = out + vec_offset(vec, t, 1);
+          const C *Z = (const C *)buf + t * rowc;
+          const R *v = (const R *)buf + t * L;
           R r;
           switch (kind) {
           case R2R_R2HC:
-               r = (2 * k <= n) ? V[k].x : V[n - k].y;
+               r = (2 * k <= n) ? Z[k].x : Z[n - k].y;
                break;
           case R2R_DHT: {
-               const C z = half_spec(V, n, k);
+               const C z = half_spec(Z, n, k);
                r = z.x - z.y;
                break;
           }
@@ -109,19 +167,43 @@ __global__ void k_r2r_post(int kind, long long n, long long hm, const void *__re
                /* DCT-II_q = 2 Re(exp(-i pi q / 2n) V_q); DST-II_k = DCT-II_{n-1-k}
                 * of the sign-alternated input */
                const long long q = (kind == R2R_RODFT10) ? n - 1 - k : k;
-               const C z = half_spec(V, n, q), w = quarter_twiddle<C>(q, n, -1);
+               const C z = half_spec(Z, n, q), w = r2r_twiddle<C>(q, 4 * n, -1);
                r = 2 * (w.x * z.x - w.y * z.y);
                break;
           }
+          case R2R_REDFT00:
+               /* the DFT of the even extension is real: y_k = Re E_k */
+               r = Z[k].x;
+               break;
+          case R2R_RODFT00:
+               /* the DFT of the odd extension is imaginary: y_k = -Im O_{k+1} */
+               r = -Z[k + 1].y;
+               break;
           case R2R_HC2R:
                r = v[k];
                break;
-          default: {
+          case R2R_REDFT01:
+          case R2R_RODFT01: {
                /* REDFT01: y_{2m} = v_m, y_{2m+1} = v_{n-1-m}; RODFT01 also
                 * multiplies y_k by (-1)^k */
                const long long src = (k & 1) ? n - 1 - (k >> 1) : (k >> 1);
                r = v[src];
                if (kind == R2R_RODFT01 && (k & 1)) r = -r;
+               break;
+          }
+          default: {
+               /* REDFT11.  Even n: u_p = Z_p exp(-i pi p / n), y_{2p} = 2 Re u_p,
+                * y_{n-1-2p} = -2 Im u_p.  Odd n: y_k = 2 Re(Z_k exp(-i pi (2k+1) / 4n)).
+                * RODFT11_k = (-1)^k REDFT11_k of x reversed. */
+               if (!(n & 1)) {
+                    const long long p = (k & 1) ? (n - 1 - k) >> 1 : k >> 1;
+                    const C z = Z[p], w = r2r_twiddle<C>(p, 2 * n, -1);
+                    r = (k & 1) ? -2 * (z.x * w.y + z.y * w.x) : 2 * (z.x * w.x - z.y * w.y);
+               } else {
+                    const C z = Z[k], w = r2r_twiddle<C>(2 * k + 1, 8 * n, -1);
+                    r = 2 * (z.x * w.x - z.y * w.y);
+               }
+               if (kind == R2R_RODFT11 && (k & 1)) r = -r;
                break;
           }
           }
@@ -141,21 +223,31 @@ static unsigned r2r_blocks(long long work)
      return (unsigned)b;
 }
 
-extern "C" int gb_r2r_pre(int prec, int kind, long long n, long long hm, const void *in, long long is, long long idist,
-                          void *buf, void *stream)
+extern "C" int gb_r2r_pre(int prec, int kind, long long n, long long V, const void *in, long long is,
+                          const gb_r2r_vec *vec, void *buf, void *stream)
 {
      cudaStream_t st = (cudaStream_t)stream;
-     const long long per = (kind == R2R_HC2R || kind == R2R_REDFT01 || kind == R2R_RODFT01) ? n / 2 + 1 : n;
-     if (prec == 4) k_r2r_pre<float><<<r2r_blocks(per * hm), 256, 0, st>>>(kind, n, hm, (const float *)in, is, idist, buf);
-     else k_r2r_pre<double><<<r2r_blocks(per * hm), 256, 0, st>>>(kind, n, hm, (const double *)in, is, idist, buf);
+     long long L;
+     const int core = gb_r2r_core(kind, n, &L);
+     const long long per = core == GB_R2R_CORE_C2R ? L / 2 + 1 : L;
+     if (vec->nv < 0 || vec->nv > GB_R2R_MAXV) return -1;
+     if (prec == 4)
+          k_r2r_pre<float><<<r2r_blocks(per * V), 256, 0, st>>>(kind, n, L, V, (const float *)in, is, *vec, buf);
+     else
+          k_r2r_pre<double><<<r2r_blocks(per * V), 256, 0, st>>>(kind, n, L, V, (const double *)in, is, *vec, buf);
      return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-extern "C" int gb_r2r_post(int prec, int kind, long long n, long long hm, const void *buf, void *out, long long os,
-                           long long odist, void *stream)
+extern "C" int gb_r2r_post(int prec, int kind, long long n, long long V, const void *buf, void *out, long long os,
+                           const gb_r2r_vec *vec, void *stream)
 {
      cudaStream_t st = (cudaStream_t)stream;
-     if (prec == 4) k_r2r_post<float><<<r2r_blocks(n * hm), 256, 0, st>>>(kind, n, hm, buf, (float *)out, os, odist);
-     else k_r2r_post<double><<<r2r_blocks(n * hm), 256, 0, st>>>(kind, n, hm, buf, (double *)out, os, odist);
+     long long L;
+     gb_r2r_core(kind, n, &L);
+     if (vec->nv < 0 || vec->nv > GB_R2R_MAXV) return -1;
+     if (prec == 4)
+          k_r2r_post<float><<<r2r_blocks(n * V), 256, 0, st>>>(kind, n, L, V, buf, (float *)out, os, *vec);
+     else
+          k_r2r_post<double><<<r2r_blocks(n * V), 256, 0, st>>>(kind, n, L, V, buf, (double *)out, os, *vec);
      return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

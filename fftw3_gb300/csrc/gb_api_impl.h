@@ -179,14 +179,48 @@ PFX(plan) PFX(plan_guru64_dft)(int rank, const PFX(iodim64) *dims, int howmany_r
 }
 
 /* api/plan-guru-split-dft.h:23-38: the forward DFT of ri + i ii into
- * ro + i io, strides in reals. */
-static PFX(plan) PFX(split_common)(int rank, const long long *dn, const long long *dis, const long long *dos,
-                                   int hrank, const long long *hn, const long long *his, const long long *hos,
-                                   R *ri, R *ii, R *ro, R *io_, unsigned flags)
+ * ro + i io, strides in reals (kind GB_PROB_DFT); r2c of ri into (ro, io)
+ * and c2r of (ri, ii) into ro (api/plan-guru-split-dft-r2c.h,
+ * api/plan-guru-split-dft-c2r.h). */
+static PFX(plan) PFX(split_common)(int kind, int rank, const long long *dn, const long long *dis,
+                                   const long long *dos, int hrank, const long long *hn, const long long *his,
+                                   const long long *hos, R *ri, R *ii, R *ro, R *io_, unsigned flags)
 {
      gb_dim d[GB_MAXRANK], v[GB_MAXRANK];
-     int i, even = 1;
+     int i, even = 1, ein = 1, eout = 1;
      if (rank < 0 || rank > GB_MAXRANK || hrank < 0 || hrank > GB_MAXRANK) return 0;
+     if (kind != GB_PROB_DFT) {
+          /* one complex side: interleaved (second array = first + 1, even
+           * strides) makes it an ordinary r2c / c2r plan */
+          if (rank < 1) return 0;
+          for (i = 0; i < rank; ++i) {
+               if (dn[i] <= 0) return 0;
+               if (dis[i] % 2) ein = 0;
+               if (dos[i] % 2) eout = 0;
+          }
+          for (i = 0; i < hrank; ++i) {
+               if (hn[i] < 0) return 0;
+               if (his[i] % 2) ein = 0;
+               if (hos[i] % 2) eout = 0;
+          }
+          if ((kind == GB_PROB_R2C && eout && io_ - ro == 1) || (kind == GB_PROB_C2R && ein && ii - ri == 1)) {
+               long long a[GB_MAXRANK], b[GB_MAXRANK], c[GB_MAXRANK], e[GB_MAXRANK];
+               PFX(plan) p;
+               for (i = 0; i < rank; ++i) {
+                    a[i] = kind == GB_PROB_C2R ? dis[i] / 2 : dis[i];
+                    b[i] = kind == GB_PROB_R2C ? dos[i] / 2 : dos[i];
+               }
+               for (i = 0; i < hrank; ++i) {
+                    c[i] = kind == GB_PROB_C2R ? his[i] / 2 : his[i];
+                    e[i] = kind == GB_PROB_R2C ? hos[i] / 2 : hos[i];
+               }
+               p = PFX(guru_common)(kind, rank, dn, a, b, hrank, hn, c, e, ri, ro,
+                                    kind == GB_PROB_R2C ? FFTW_FORWARD : FFTW_BACKWARD, flags);
+               if (p) p->view = 1;
+               return p;
+          }
+          goto general;
+     }
      for (i = 0; i < rank; ++i) {
           if (dn[i] <= 0) return 0;
           if (dis[i] % 2 || dos[i] % 2) even = 0;
@@ -207,6 +241,7 @@ static PFX(plan) PFX(split_common)(int rank, const long long *dn, const long lon
           if (p) p->view = swapped ? 2 : 1;
           return p;
      }
+general:
      for (i = 0; i < rank; ++i) { d[i].n = dn[i]; d[i].is = dis[i]; d[i].os = dos[i]; }
      for (i = 0; i < hrank; ++i) { v[i].n = hn[i]; v[i].is = his[i]; v[i].os = hos[i]; }
      {
@@ -217,7 +252,7 @@ static PFX(plan) PFX(split_common)(int rank, const long long *dn, const long lon
                return 0;
           }
           gb_lock();
-          g = gb_mksplit((int)sizeof(R), rank, d, hrank, v, ri, ii, ro, io_, flags);
+          g = gb_mksplit(kind, (int)sizeof(R), rank, d, hrank, v, ri, ii, ro, io_, flags);
           if (g && !(flags & FFTW_ESTIMATE) && !gb_dry_run()) gb_tune(g->split_inner, flags);
           gb_unlock();
           p = PFX(wrap)(g);
@@ -234,7 +269,8 @@ PFX(plan) PFX(plan_guru_split_dft)(int rank, const PFX(iodim) *dims, int howmany
           GB_UNPACK(dims, rank, dn, dis, dos);
           {
                GB_UNPACK(howmany_dims, howmany_rank, hn, his, hos);
-               return PFX(split_common)(rank, dn, dis, dos, howmany_rank, hn, his, hos, ri, ii, ro, io_, flags);
+               return PFX(split_common)(GB_PROB_DFT, rank, dn, dis, dos, howmany_rank, hn, his, hos, ri, ii, ro, io_,
+                                        flags);
           }
      }
 }
@@ -246,7 +282,8 @@ PFX(plan) PFX(plan_guru64_split_dft)(int rank, const PFX(iodim64) *dims, int how
           GB_UNPACK(dims, rank, dn, dis, dos);
           {
                GB_UNPACK(howmany_dims, howmany_rank, hn, his, hos);
-               return PFX(split_common)(rank, dn, dis, dos, howmany_rank, hn, his, hos, ri, ii, ro, io_, flags);
+               return PFX(split_common)(GB_PROB_DFT, rank, dn, dis, dos, howmany_rank, hn, his, hos, ri, ii, ro, io_,
+                                        flags);
           }
      }
 }
@@ -386,97 +423,130 @@ PFX(plan) PFX(plan_guru64_dft_c2r)(int rank, const PFX(iodim64) *dims, int howma
      }
 }
 
-#define GB_NULL_PLANNER(decl)                                                          \
-     decl                                                                              \
-     {                                                                                 \
-          gb_set_error("this planner is not provided by this library (r2r / split)");  \
-          return 0;                                                                    \
-     }
-GB_NULL_PLANNER(PFX(plan) PFX(plan_guru_split_dft_r2c)(int rank, const PFX(iodim) *dims, int howmany_rank,
-                const PFX(iodim) *howmany_dims, R *in, R *ro, R *io_, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_guru_split_dft_c2r)(int rank, const PFX(iodim) *dims, int howmany_rank,
-                const PFX(iodim) *howmany_dims, R *ri, R *ii, R *out, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_guru64_split_dft_r2c)(int rank, const PFX(iodim64) *dims, int howmany_rank,
-                const PFX(iodim64) *howmany_dims, R *in, R *ro, R *io_, unsigned flags))
-GB_NULL_PLANNER(PFX(plan) PFX(plan_guru64_split_dft_c2r)(int rank, const PFX(iodim64) *dims, int howmany_rank,
-                const PFX(iodim64) *howmany_dims, R *ri, R *ii, R *out, unsigned flags))
-/* r2r: rank 1 (plan_r2r_1d, plan_r2r / plan_many_r2r / guru of rank 1 with
- * at most one howmany dimension); multi-dimensional r2r returns NULL.
- * Strides and distances count reals (api/plan-many-r2r.c, api/plan-r2r.c). */
-static PFX(plan) PFX(r2r_common)(int kind, long long n, long long hm, long long is, long long idist, long long os,
-                                 long long odist, R *in, R *out, unsigned flags)
+/* split-array r2c / c2r (api/plan-guru-split-dft-r2c.h,
+ * api/plan-guru-split-dft-c2r.h; 64-bit variants api/plan-guru64-*) */
+#define GB_SPLIT_REAL(kind, a0, a1, a2, a3)                                                   \
+     do {                                                                                 \
+          if (rank < 0 || howmany_rank < 0) return 0;                                     \
+          {                                                                               \
+               GB_UNPACK(dims, rank, dn, dis, dos);                                       \
+               {                                                                          \
+                    GB_UNPACK(howmany_dims, howmany_rank, hn, his, hos);                  \
+                    return PFX(split_common)(kind, rank, dn, dis, dos, howmany_rank, hn, his, hos, a0, \
+                                             a1, a2, a3, flags);                          \
+               }                                                                          \
+          }                                                                               \
+     } while (0)
+PFX(plan) PFX(plan_guru_split_dft_r2c)(int rank, const PFX(iodim) *dims, int howmany_rank,
+                                       const PFX(iodim) *howmany_dims, R *in, R *ro, R *io_, unsigned flags)
+{
+     GB_SPLIT_REAL(GB_PROB_R2C, in, 0, ro, io_);
+}
+PFX(plan) PFX(plan_guru_split_dft_c2r)(int rank, const PFX(iodim) *dims, int howmany_rank,
+                                       const PFX(iodim) *howmany_dims, R *ri, R *ii, R *out, unsigned flags)
+{
+     GB_SPLIT_REAL(GB_PROB_C2R, ri, ii, out, 0);
+}
+PFX(plan) PFX(plan_guru64_split_dft_r2c)(int rank, const PFX(iodim64) *dims, int howmany_rank,
+                                         const PFX(iodim64) *howmany_dims, R *in, R *ro, R *io_, unsigned flags)
+{
+     GB_SPLIT_REAL(GB_PROB_R2C, in, 0, ro, io_);
+}
+PFX(plan) PFX(plan_guru64_split_dft_c2r)(int rank, const PFX(iodim64) *dims, int howmany_rank,
+                                         const PFX(iodim64) *howmany_dims, R *ri, R *ii, R *out, unsigned flags)
+{
+     GB_SPLIT_REAL(GB_PROB_C2R, ri, ii, out, 0);
+}
+/* r2r of any rank (rank 0: a copy) with any howmany rank (api/plan-many-r2r.c,
+ * api/plan-r2r.c, api/plan-r2r-1d/2d/3d.c, api/plan-guru-r2r.h); strides and
+ * distances count reals; one kind per transform dim. */
+static PFX(plan) PFX(r2r_common)(int rank, const gb_dim *dims, const int *kinds, int vrank, const gb_dim *vdims,
+                                 R *in, R *out, unsigned flags)
 {
      gb_plan *g;
      PFX(plan) p;
-     if (n <= 0 || hm < 0) return 0;
      if (!gb_dry_run() && !gb_cuda_ready()) {
           gb_set_error("no CUDA device: libfftw3_gb300 runs transforms on the GPU only");
           return 0;
      }
      gb_lock();
-     g = gb_mkr2r((int)sizeof(R), kind, n, hm, is, idist, os, odist, in, out, flags);
-     if (g && !(flags & FFTW_ESTIMATE) && !gb_dry_run()) gb_tune(g->r2r_inner, flags);
+     g = gb_mkr2r((int)sizeof(R), rank, dims, kinds, vrank, vdims, in, out, flags);
+     if (g && !(flags & FFTW_ESTIMATE) && !gb_dry_run()) gb_r2r_tune(g, flags);
      gb_unlock();
      p = PFX(wrap)(g);
      if (p) p->view = 4;
      return p;
 }
 
-static PFX(plan) PFX(r2r_multid)(void)
-{
-     gb_set_error("multi-dimensional r2r is not provided by this library (rank 1 only)");
-     return 0;
-}
-
 PFX(plan) PFX(plan_many_r2r)(int rank, const int *n, int howmany, R *in, const int *inembed, int istride, int idist,
                              R *out, const int *onembed, int ostride, int odist, const PFX(r2r_kind) *kind,
                              unsigned flags)
 {
-     (void)inembed; (void)onembed;
-     if (rank != 1) return rank > 1 ? PFX(r2r_multid)() : 0;
-     if (!n || !kind || n[0] <= 0 || howmany < 0) return 0;
-     return PFX(r2r_common)((int)kind[0], n[0], howmany, istride, idist, ostride, odist, in, out, flags);
+     gb_problem prb;
+     gb_dim v;
+     int k[GB_MAXRANK], d;
+     if (!PFX(kosher)(rank, n, howmany) || !kind) return 0;
+     if (rank > GB_MAXRANK) {
+          gb_set_error("r2r of rank %d is not provided by this library (rank 0..%d)", rank, GB_MAXRANK);
+          return 0;
+     }
+     memset(&prb, 0, sizeof prb);
+     PFX(rowmajor)(&prb, rank, n, inembed ? inembed : n, onembed ? onembed : n, istride, ostride);
+     for (d = 0; d < rank; ++d) k[d] = (int)kind[d];
+     v.n = howmany; v.is = idist; v.os = odist;
+     return PFX(r2r_common)(rank, prb.sz, k, 1, &v, in, out, flags);
 }
 PFX(plan) PFX(plan_r2r)(int rank, const int *n, R *in, R *out, const PFX(r2r_kind) *kind, unsigned flags)
 {
-     if (rank != 1) return rank > 1 ? PFX(r2r_multid)() : 0;
-     if (!n || !kind || n[0] <= 0) return 0;
-     return PFX(r2r_common)((int)kind[0], n[0], 1, 1, n[0], 1, n[0], in, out, flags);
+     return PFX(plan_many_r2r)(rank, n, 1, in, 0, 1, 0, out, 0, 1, 0, kind, flags);
 }
 PFX(plan) PFX(plan_r2r_1d)(int n, R *in, R *out, PFX(r2r_kind) kind, unsigned flags)
 {
-     if (n <= 0) return 0;
-     return PFX(r2r_common)((int)kind, n, 1, 1, n, 1, n, in, out, flags);
+     return PFX(plan_r2r)(1, &n, in, out, &kind, flags);
 }
 PFX(plan) PFX(plan_r2r_2d)(int n0, int n1, R *in, R *out, PFX(r2r_kind) kind0, PFX(r2r_kind) kind1, unsigned flags)
 {
-     (void)n0; (void)n1; (void)in; (void)out; (void)kind0; (void)kind1; (void)flags;
-     return PFX(r2r_multid)();
+     const int n[2] = {n0, n1};
+     const PFX(r2r_kind) k[2] = {kind0, kind1};
+     return PFX(plan_r2r)(2, n, in, out, k, flags);
 }
 PFX(plan) PFX(plan_r2r_3d)(int n0, int n1, int n2, R *in, R *out, PFX(r2r_kind) kind0, PFX(r2r_kind) kind1,
                            PFX(r2r_kind) kind2, unsigned flags)
 {
-     (void)n0; (void)n1; (void)n2; (void)in; (void)out; (void)kind0; (void)kind1; (void)kind2; (void)flags;
-     return PFX(r2r_multid)();
+     const int n[3] = {n0, n1, n2};
+     const PFX(r2r_kind) k[3] = {kind0, kind1, kind2};
+     return PFX(plan_r2r)(3, n, in, out, k, flags);
 }
+#define GB_R2R_GURU(dims, rank, howmany_dims, howmany_rank)                                 \
+     do {                                                                                    \
+          gb_dim dd_[GB_MAXRANK], vv_[GB_MAXRANK];                                           \
+          int kk_[GB_MAXRANK], q_;                                                           \
+          if (rank < 0 || rank > GB_MAXRANK || howmany_rank < 0 || howmany_rank > GB_MAXRANK) { \
+               gb_set_error("r2r of rank %d / howmany rank %d is not provided by this library", \
+                            rank, howmany_rank);                                             \
+               return 0;                                                                     \
+          }                                                                                  \
+          if ((rank > 0 && (!dims || !kind)) || (howmany_rank > 0 && !howmany_dims)) return 0; \
+          for (q_ = 0; q_ < rank; ++q_) {                                                    \
+               dd_[q_].n = (dims)[q_].n; dd_[q_].is = (dims)[q_].is; dd_[q_].os = (dims)[q_].os; \
+               kk_[q_] = (int)kind[q_];                                                      \
+          }                                                                                  \
+          for (q_ = 0; q_ < howmany_rank; ++q_) {                                            \
+               vv_[q_].n = (howmany_dims)[q_].n; vv_[q_].is = (howmany_dims)[q_].is;         \
+               vv_[q_].os = (howmany_dims)[q_].os;                                           \
+          }                                                                                  \
+          return PFX(r2r_common)(rank, dd_, kk_, howmany_rank, vv_, in, out, flags);         \
+     } while (0)
 PFX(plan) PFX(plan_guru_r2r)(int rank, const PFX(iodim) *dims, int howmany_rank, const PFX(iodim) *howmany_dims,
                              R *in, R *out, const PFX(r2r_kind) *kind, unsigned flags)
 {
-     if (rank != 1 || howmany_rank > 1 || howmany_rank < 0) return rank > 1 ? PFX(r2r_multid)() : 0;
-     if (!dims || !kind || dims[0].n <= 0) return 0;
-     return PFX(r2r_common)((int)kind[0], dims[0].n, howmany_rank ? howmany_dims[0].n : 1, dims[0].is,
-                            howmany_rank ? howmany_dims[0].is : 0, dims[0].os, howmany_rank ? howmany_dims[0].os : 0,
-                            in, out, flags);
+     GB_R2R_GURU(dims, rank, howmany_dims, howmany_rank);
 }
 PFX(plan) PFX(plan_guru64_r2r)(int rank, const PFX(iodim64) *dims, int howmany_rank,
                                const PFX(iodim64) *howmany_dims, R *in, R *out, const PFX(r2r_kind) *kind,
                                unsigned flags)
 {
-     if (rank != 1 || howmany_rank > 1 || howmany_rank < 0) return rank > 1 ? PFX(r2r_multid)() : 0;
-     if (!dims || !kind || dims[0].n <= 0) return 0;
-     return PFX(r2r_common)((int)kind[0], dims[0].n, howmany_rank ? howmany_dims[0].n : 1, dims[0].is,
-                            howmany_rank ? howmany_dims[0].is : 0, dims[0].os, howmany_rank ? howmany_dims[0].os : 0,
-                            in, out, flags);
+     GB_R2R_GURU(dims, rank, howmany_dims, howmany_rank);
 }
 
 /* ---------------------------------------------------------------- execute */
@@ -525,7 +595,7 @@ void PFX(execute_dft_c2r)(const PFX(plan) p, C *in, R *out) { PFX(run)(p, in, ou
 void PFX(execute_split_dft)(const PFX(plan) p, R *ri, R *ii, R *ro, R *io_)
 {
      if (!p) return;
-     if (p->view == 3) PFX(run_split)(p, ri, ii, ro, io_);
+     if (p->view == 3 && p->g->split_kind == GB_PROB_DFT) PFX(run_split)(p, ri, ii, ro, io_);
      else if (p->view == 1) PFX(run)(p, ri, ro, GB_PROB_DFT);
      else if (p->view == 2) PFX(run)(p, ii, io_, GB_PROB_DFT);
      else {
@@ -533,8 +603,27 @@ void PFX(execute_split_dft)(const PFX(plan) p, R *ri, R *ii, R *ro, R *io_)
           fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
      }
 }
-void PFX(execute_split_dft_r2c)(const PFX(plan) p, R *in, R *ro, R *io_) { (void)p; (void)in; (void)ro; (void)io_; }
-void PFX(execute_split_dft_c2r)(const PFX(plan) p, R *ri, R *ii, R *out) { (void)p; (void)ri; (void)ii; (void)out; }
+/* api/execute-split-dft-r2c.c, api/execute-split-dft-c2r.c */
+void PFX(execute_split_dft_r2c)(const PFX(plan) p, R *in, R *ro, R *io_)
+{
+     if (!p) return;
+     if (p->view == 3 && p->g->split_kind == GB_PROB_R2C) PFX(run_split)(p, in, 0, ro, io_);
+     else if (p->view == 1 && p->g->prb.kind == GB_PROB_R2C) PFX(run)(p, in, ro, GB_PROB_R2C);
+     else {
+          gb_set_error("execute_split_dft_r2c: the plan was not made by plan_guru_split_dft_r2c");
+          fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
+     }
+}
+void PFX(execute_split_dft_c2r)(const PFX(plan) p, R *ri, R *ii, R *out)
+{
+     if (!p) return;
+     if (p->view == 3 && p->g->split_kind == GB_PROB_C2R) PFX(run_split)(p, ri, ii, out, 0);
+     else if (p->view == 1 && p->g->prb.kind == GB_PROB_C2R) PFX(run)(p, ri, out, GB_PROB_C2R);
+     else {
+          gb_set_error("execute_split_dft_c2r: the plan was not made by plan_guru_split_dft_c2r");
+          fprintf(stderr, "[fftw_gb300] %s\n", gb_last_error());
+     }
+}
 /* api/execute-r2r.c: the plan's transform on new arrays of the same layout */
 void PFX(execute_r2r)(const PFX(plan) p, R *in, R *out)
 {

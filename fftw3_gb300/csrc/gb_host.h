@@ -48,6 +48,17 @@ typedef struct gb_step {
 
 #define GB_CHUNK_SLOTS 3
 
+/* one stage of an r2r plan: the r2r of one transform dim over all the
+ * other dims (vector loop vec) */
+typedef struct gb_r2r_axis {
+     int kind, core;            /* fftw_r2r_kind; GB_R2R_CORE_* */
+     long long n, L, V;         /* length, core length, transforms in the stage */
+     long long is, os;          /* strides along the dim (reals) */
+     int src_mid, dst_mid;      /* read from / write to r2r_mid instead of the caller's arrays */
+     gb_r2r_vec vec;
+     struct gb_plan *inner;     /* the core transform on r2r_buf[0] -> r2r_buf[1] */
+} gb_r2r_axis;
+
 struct gb_plan {
      int refcnt;
      gb_problem prb;
@@ -74,16 +85,18 @@ struct gb_plan {
       * [vector dims..., transform dims...] with strides in reals; the
       * transform runs as the forward c2c plan split_inner on dense
       * interleaved buffers, between a pack and an unpack kernel */
+     int split_kind;            /* GB_PROB_DFT, GB_PROB_R2C or GB_PROB_C2R */
      int split_nd;
      long long split_n[2 * GB_MAXRANK], split_is[2 * GB_MAXRANK], split_os[2 * GB_MAXRANK];
      void *split_arr[4];        /* ri, ii, ro, io at planning time */
      struct gb_plan *split_inner;
      void *split_buf[2];        /* dense complex input and output of split_inner */
-     /* 1D r2r (fftw_r2r_kind r2r_kind): a pre kernel, the real DFT r2r_inner
-      * on dense buffers, a post kernel */
-     int r2r_kind;
-     struct gb_plan *r2r_inner;
-     void *r2r_buf[2];
+     /* r2r problems: one stage per transform dim (a pre kernel, the core
+      * transform on dense buffers, a post kernel), last dim first */
+     int r2r_naxis;
+     struct gb_r2r_axis *r2r_ax;
+     void *r2r_buf[2];          /* dense core input and output */
+     void *r2r_mid;             /* dense real intermediate between stages (rank > 1) */
      void *stream;              /* cudaStream_t; 0 = legacy default stream */
      int async;                 /* 1: execute does not wait for completion */
      int in_align, out_align;   /* alignment of the planning arrays (bytes, capped at 16) */
@@ -120,12 +133,13 @@ int gb_tune(gb_plan *p, unsigned flags);
 
 /* execution (gb_exec.c) */
 int gb_execute(gb_plan *p, void *in, void *out);
-gb_plan *gb_mksplit(int prec, int rank, const gb_dim *dims, int vrank, const gb_dim *vdims, void *ri, void *ii,
-                    void *ro, void *io, unsigned flags);
-int gb_execute_split(gb_plan *p, void *ri, void *ii, void *ro, void *io);
-gb_plan *gb_mkr2r(int prec, int kind, long long n, long long hm, long long is, long long idist, long long os,
-                  long long odist, void *in, void *out, unsigned flags);
+gb_plan *gb_mksplit(int kind, int prec, int rank, const gb_dim *dims, int vrank, const gb_dim *vdims, void *ri,
+                    void *ii, void *ro, void *io, unsigned flags);
+int gb_execute_split(gb_plan *p, void *a0, void *a1, void *a2, void *a3);
+gb_plan *gb_mkr2r(int prec, int rank, const gb_dim *dims, const int *kinds, int vrank, const gb_dim *vdims, void *in,
+                  void *out, unsigned flags);
 int gb_execute_r2r(gb_plan *p, void *in, void *out);
+int gb_r2r_tune(gb_plan *p, unsigned flags);
 
 /* wisdom (gb_wisdom.c) */
 typedef struct gb_wisdom_entry {

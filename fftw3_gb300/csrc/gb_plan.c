@@ -572,6 +572,18 @@ static int use_rader(int prec, long long n, const gb_wisdom_entry *w)
      return e && !strcmp(e, "rader");
 }
 
+/* 1 when a c2c of length n runs only as the multi-pass convolution, which
+ * needs scratch of its own: a prime factor > 13 and too long for Rader or
+ * Bluestein in one CTA */
+static int c2c_needs_conv(int prec, long long n)
+{
+     gb_pass t;
+     gb_dim one = {1, 0, 0};
+     if (config_pass(&t, prec, GB_KIND_C2C, n, -1, 1, 1, 1, &one, 0, 0) >= 0) return 0;
+     if (use_rader(prec, n, 0) && config_pass(&t, prec, GB_KIND_RADER, n, -1, 1, 1, 1, &one, 0, 0) == 0) return 0;
+     return config_pass(&t, prec, GB_KIND_BLUESTEIN, n, -1, 1, 1, 1, &one, 0, 0) != 0;
+}
+
 /* Adds the steps of one batched 1D transform: length n along (is, os), batch
  * dims v (count nv), from buffer src to dst.  Chooses single-CTA kernels,
  * the in-CTA Bluestein, or the two-pass four-step decomposition. */
@@ -588,8 +600,8 @@ static gb_step *add_pointwise(builder *b, int pw, long long n, long long nfft, i
 {
      gb_plan *p = b->p;
      int prec = p->prb.prec, i;
-     long long L = (pw == GB_PW_HC2C_POST) ? nfft + 1 : (pw == GB_PW_CHIRP_OUT) ? n
-                 : (pw == GB_PW_HALF_COPY) ? n / 2 + 1 : nfft;
+     long long L = (pw == GB_PW_HC2C_POST) ? nfft + 1 : (pw == GB_PW_CHIRP_OUT || pw == GB_PW_CHIRP_OUT_REAL) ? n
+                 : (pw == GB_PW_HALF_COPY || pw == GB_PW_CHIRP_OUT_HALF) ? n / 2 + 1 : nfft;
      gb_step *s = new_step(b);
      gb_pass *P;
      if (!s) return 0;
@@ -914,11 +926,7 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
                if (os != 1) ok = 0;
                for (i = 0; i < nvk; ++i) if (v[i].os % 2) ok = 0;
           }
-          if (!ok || src == GB_BUF_SCRATCH || dst == GB_BUF_SCRATCH) {
-               gb_set_error("real length %lld beyond one CTA needs unit real stride", n);
-               b->err = 1;
-               return;
-          }
+          if (!ok || src == GB_BUF_SCRATCH || dst == GB_BUF_SCRATCH || c2c_needs_conv(prec, M)) goto conv;
           need_scratch(p, GB_BUF_SCRATCH, (size_t)(M * howmany) * csize(prec));
           if (kind == GB_KIND_R2C) {
                for (i = 0; i < nvk; ++i) { vp[i].n = v[i].n; vp[i].is = v[i].is / 2; }
@@ -962,6 +970,35 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           }
           return;
      }
+conv:
+     if ((kind == GB_KIND_R2C || kind == GB_KIND_C2R) && src != GB_BUF_SCRATCH && dst != GB_BUF_SCRATCH &&
+         src != GB_BUF_SCRATCH2 && dst != GB_BUF_SCRATCH2) {
+          /* a real length none of the paths above takes (odd beyond one CTA
+           * with a prime factor > 13, even with a half length that needs its
+           * own convolution, or non-unit real strides beyond one CTA):
+           * Bluestein's convolution read straight from the real array (r2c)
+           * or from the half spectrum extended by Hermitian symmetry (c2r),
+           * written back as the half spectrum or the real parts
+           * (dft/bluestein.c:82-128) */
+          long long nb = 1;
+          gb_dim vin[GB_MAXRANK + 2], vmid[GB_MAXRANK + 2], vout[GB_MAXRANK + 2];
+          while (nb < 2 * n - 1) nb <<= 1;
+          dense_dims(v, nvk, nb, vin, 1);
+          dense_dims(v, nvk, nb, vmid, 0);
+          for (i = 0; i < nvk; ++i) vmid[i].is = vmid[i].os = vin[i].os;
+          dense_dims(v, nvk, nb, vout, 0);
+          need_scratch(p, GB_BUF_SCRATCH, (size_t)(nb * howmany) * csize(prec));
+          if (!add_pointwise(b, kind == GB_KIND_R2C ? GB_PW_CHIRP_IN_REAL : GB_PW_CHIRP_IN_HERM, n, nb, sign, is, 1,
+                             nvk, vin, src, GB_BUF_SCRATCH))
+               return;
+          add_1d_mid(b, GB_KIND_C2C, nb, -1, 1, 1, nvk, vmid, GB_BUF_SCRATCH, GB_BUF_SCRATCH, GB_BUF_SCRATCH2);
+          if (!b->err) add_pointwise(b, GB_PW_SPEC_MUL, n, nb, sign, 1, 1, nvk, vmid, GB_BUF_SCRATCH, GB_BUF_SCRATCH);
+          add_1d_mid(b, GB_KIND_C2C, nb, 1, 1, 1, nvk, vmid, GB_BUF_SCRATCH, GB_BUF_SCRATCH, GB_BUF_SCRATCH2);
+          if (!b->err)
+               add_pointwise(b, kind == GB_KIND_R2C ? GB_PW_CHIRP_OUT_HALF : GB_PW_CHIRP_OUT_REAL, n, nb, sign, 1, os,
+                             nvk, vout, GB_BUF_SCRATCH, dst);
+          return;
+     }
      gb_set_error("length %lld is not supported for this transform kind", n);
      b->err = 1;
 }
@@ -976,9 +1013,14 @@ static void describe(gb_plan *p)
           const gb_pass *P = &p->step[i].pass;
           static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy", "rader", "pointwise"};
           static const char *mv[] = {"direct", "rows", "cols"};
+          static const char *pw[] = {"hc2c-post", "hc2c-pre", "chirp-in", "spec-mul", "chirp-out", "promote",
+                                     "half-copy", "herm-ext", "real-part", "chirp-in-real", "chirp-in-herm",
+                                     "chirp-out-half", "chirp-out-real"};
           off += snprintf(p->desc + off, sizeof p->desc - off,
-                          "\n  (pass %s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
-                          kk[P->kind], P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" :
+                          "\n  (pass %s%s%s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
+                          kk[P->kind], P->kind == GB_KIND_POINTWISE ? ":" : "",
+                          P->kind == GB_KIND_POINTWISE && P->pw >= 0 && P->pw <= GB_PW_CHIRP_OUT_REAL ? pw[P->pw] : "",
+                          P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" :
                           P->variant == GB_VAR_TMA_COLS ? "cols-tma" :
                           P->variant == GB_VAR_TC ? "tc-split-fp16" : "gen", P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
@@ -1146,8 +1188,13 @@ void gb_destroy(gb_plan *p)
           if (p->split_buf[i] && !gb_dry) cudaFree(p->split_buf[i]);
      }
      if (p->split_inner) gb_destroy(p->split_inner);
-     if (p->r2r_inner) gb_destroy(p->r2r_inner);
+     if (p->r2r_ax) {
+          for (i = 0; i < p->r2r_naxis; ++i)
+               if (p->r2r_ax[i].inner) gb_destroy(p->r2r_ax[i].inner);
+          free(p->r2r_ax);
+     }
      for (i = 0; i < 2; ++i)
           if (p->r2r_buf[i] && !gb_dry) cudaFree(p->r2r_buf[i]);
+     if (p->r2r_mid && !gb_dry) cudaFree(p->r2r_mid);
      free(p);
 }

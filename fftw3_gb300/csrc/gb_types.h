@@ -41,7 +41,11 @@ enum gb_pw {
      GB_PW_PROMOTE = 5,     /* odd r2c: n reals -> n complex with zero imaginary parts */
      GB_PW_HALF_COPY = 6,   /* odd r2c: first n/2+1 of n complex */
      GB_PW_HERM_EXT = 7,    /* odd c2r: n/2+1 complex -> n complex, X[n-k] = conj X[k] */
-     GB_PW_REAL_PART = 8    /* odd c2r: n complex -> n reals (real parts) */
+     GB_PW_REAL_PART = 8,   /* odd c2r: n complex -> n reals (real parts) */
+     GB_PW_CHIRP_IN_REAL = 9,    /* Bluestein r2c: n reals x conj(w), zero-padded to nfft */
+     GB_PW_CHIRP_IN_HERM = 10,   /* Bluestein c2r: n/2+1 complex extended by Hermitian symmetry, x conj(w) */
+     GB_PW_CHIRP_OUT_HALF = 11,  /* Bluestein r2c: conv conj(w), first n/2+1 */
+     GB_PW_CHIRP_OUT_REAL = 12   /* Bluestein c2r: real part of conv conj(w), first n */
 };
 
 /* How the transform is computed inside one CTA. */
@@ -149,7 +153,8 @@ int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul
 int gb_cols_tma_smem(int nfft, int tb);
 #define GB_SPLIT_MAXD 32   /* dims of a split-array problem: vector + transform dims */
 /* split-array pack (pack != 0: re/im strided -> dense complex buf) and
- * unpack (dense complex buf -> re/im strided); n/s: nd dims, strides in reals */
+ * unpack (dense complex buf -> re/im strided); n/s: nd dims, strides in
+ * reals; im == NULL copies one real array to or from dense reals */
 int gb_split_copy(int pack, int prec, int nd, const long long *n, const long long *s, long long total, void *re,
                   void *im, void *buf, void *stream);
 int gb_cols_tma_plan_ok(const gb_pass *p);
@@ -159,11 +164,48 @@ const char *gb_last_cuda_error(void);
 long long gb_launch_count(void);
 int gb_device_status(void);
 int *gb_device_status_ptr(void);
-/* 1D r2r pre- and post-processing around the real DFT (fft_r2r.cu) */
-int gb_r2r_pre(int prec, int kind, long long n, long long hm, const void *in, long long is, long long idist, void *buf,
-               void *stream);
-int gb_r2r_post(int prec, int kind, long long n, long long hm, const void *buf, void *out, long long os, long long odist,
-                void *stream);
+/* r2r transforms (fft_r2r.cu): every kind of length n runs as one core
+ * transform of length L between a pre and a post kernel.  The core is a
+ * real DFT (r2c or c2r) or, for REDFT11/RODFT11, a complex DFT. */
+enum { GB_R2R_CORE_R2C = 0, GB_R2R_CORE_C2R = 1, GB_R2R_CORE_C2C = 2 };
+#ifdef __CUDACC__
+#define GB_HD __host__ __device__
+#else
+#define GB_HD
+#endif
+/* kind: fftw_r2r_kind value; returns the core and sets *len = L */
+static inline GB_HD int gb_r2r_core(int kind, long long n, long long *len)
+{
+     switch (kind) {
+     case 1: case 4: case 8:            /* HC2R, REDFT01, RODFT01 */
+          *len = n;
+          return GB_R2R_CORE_C2R;
+     case 3:                            /* REDFT00: even extension, logical 2(n-1) */
+          *len = 2 * (n - 1);
+          return GB_R2R_CORE_R2C;
+     case 7:                            /* RODFT00: odd extension, logical 2(n+1) */
+          *len = 2 * (n + 1);
+          return GB_R2R_CORE_R2C;
+     case 6: case 10:                   /* REDFT11, RODFT11: n/2 complex (even n), 2n zero-padded (odd n) */
+          *len = (n & 1) ? 2 * n : n / 2;
+          return GB_R2R_CORE_C2C;
+     default:                           /* R2HC, DHT, REDFT10, RODFT10 */
+          *len = n;
+          return GB_R2R_CORE_R2C;
+     }
+}
+/* The vector loop of one r2r axis: nv dims (outermost first) with input and
+ * output strides in reals; row t of the dense core buffers is the vector
+ * index t in row-major order over these dims. */
+#define GB_R2R_MAXV 32
+typedef struct {
+     int nv;
+     long long n[GB_R2R_MAXV], is[GB_R2R_MAXV], os[GB_R2R_MAXV];
+} gb_r2r_vec;
+int gb_r2r_pre(int prec, int kind, long long n, long long V, const void *in, long long is, const gb_r2r_vec *vec,
+               void *buf, void *stream);
+int gb_r2r_post(int prec, int kind, long long n, long long V, const void *buf, void *out, long long os,
+                const gb_r2r_vec *vec, void *stream);
 
 #ifdef __cplusplus
 }

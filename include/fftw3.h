@@ -13,10 +13,12 @@
  *   plan_dft{,_1d,_2d,_3d}, plan_many_dft, plan_guru_dft, plan_guru64_dft,
  *   plan_dft_r2c{,_1d,_2d,_3d}, plan_many_dft_r2c, plan_guru{,64}_dft_r2c,
  *   plan_dft_c2r{,_1d,_2d,_3d}, plan_many_dft_c2r, plan_guru{,64}_dft_c2r,
- *   execute, execute_dft, execute_dft_r2c, execute_dft_c2r.
- * Present but returning NULL plans (not on the accelerated path): r2r
- * (plan_*r2r*) and the split-array (plan_guru*_split_*) planners; their
- * execute_* entry points do nothing on a NULL plan.
+ *   execute, execute_dft, execute_dft_r2c, execute_dft_c2r;
+ *   plan_guru{,64}_split_dft{,_r2c,_c2r}, execute_split_dft{,_r2c,_c2r}
+ *   (split real / imaginary arrays);
+ *   plan_r2r{,_1d,_2d,_3d}, plan_many_r2r, plan_guru{,64}_r2r, execute_r2r
+ *   (all eleven r2r kinds, any rank).
+ * Every execute_* entry point does nothing on a NULL plan.
  *
  * Pointer model: arrays may be device memory (cudaMalloc, managed) or host
  * memory (malloc, fftw_malloc).  Host arrays are staged through device

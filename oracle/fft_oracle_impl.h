@@ -585,8 +585,8 @@ void P(twiddle)(I m, I n, int sign, R *out2)
  * argument reduced exactly (cos/sin of 2 pi m / M with integer m, M), as the
  * reference's manual states them (doc/reference.texi:1923-2020 R2HC/HC2R,
  * 2022-2175 REDFT, 2176-2300 RODFT, and the DHT); kinds use the
- * fftw_r2r_kind values (api/fftw3.h:96-100).  Returns -1 for a kind not
- * restated here. */
+ * fftw_r2r_kind values (api/fftw3.h:96-100).  Returns -1 for a kind out of
+ * range and for a size-1 REDFT00 (not defined). */
 static T r2r_cos(I m, I M) { T c, s; m %= M; if (m < 0) m += M; cexp_t(m, M, &c, &s); return c; }
 static T r2r_sin(I m, I M) { T c, s; m %= M; if (m < 0) m += M; cexp_t(m, M, &c, &s); return s; }
 
@@ -614,6 +614,11 @@ int P(r2r)(int kind, I n, I howmany, const R *in, R *out)
                case 2: /* DHT: sum x_j (cos + sin)(2 pi j k / n) */
                     for (j = 0; j < n; ++j) acc += (T)x[j] * (r2r_cos(j * k, n) + r2r_sin(j * k, n));
                     break;
+               case 3: /* REDFT00: x_0 + (-1)^k x_{n-1} + 2 sum_{0<j<n-1} x_j cos(pi j k / (n-1)); n > 1 */
+                    if (n < 2) return -1;
+                    acc = (T)x[0] + ((k & 1) ? -(T)x[n - 1] : (T)x[n - 1]);
+                    for (j = 1; j + 1 < n; ++j) acc += 2 * (T)x[j] * r2r_cos(j * k, 2 * (n - 1));
+                    break;
                case 4: /* REDFT01: x_0 + 2 sum_{j>=1} x_j cos(pi j (2k+1) / 2n) */
                     acc = x[0];
                     for (j = 1; j < n; ++j) acc += 2 * (T)x[j] * r2r_cos(j * (2 * k + 1), 4 * n);
@@ -621,12 +626,21 @@ int P(r2r)(int kind, I n, I howmany, const R *in, R *out)
                case 5: /* REDFT10: 2 sum x_j cos(pi (2j+1) k / 2n) */
                     for (j = 0; j < n; ++j) acc += 2 * (T)x[j] * r2r_cos((2 * j + 1) * k, 4 * n);
                     break;
+               case 6: /* REDFT11: 2 sum x_j cos(pi (2j+1)(2k+1) / 4n) */
+                    for (j = 0; j < n; ++j) acc += 2 * (T)x[j] * r2r_cos((2 * j + 1) * (2 * k + 1), 8 * n);
+                    break;
+               case 7: /* RODFT00: 2 sum x_j sin(pi (j+1)(k+1) / (n+1)) */
+                    for (j = 0; j < n; ++j) acc += 2 * (T)x[j] * r2r_sin((j + 1) * (k + 1), 2 * (n + 1));
+                    break;
                case 8: /* RODFT01: (-1)^k x_{n-1} + 2 sum_{j<n-1} x_j sin(pi (j+1)(2k+1) / 2n) */
                     acc = (k & 1) ? -(T)x[n - 1] : (T)x[n - 1];
                     for (j = 0; j + 1 < n; ++j) acc += 2 * (T)x[j] * r2r_sin((j + 1) * (2 * k + 1), 4 * n);
                     break;
                case 9: /* RODFT10: 2 sum x_j sin(pi (2j+1)(k+1) / 2n) */
                     for (j = 0; j < n; ++j) acc += 2 * (T)x[j] * r2r_sin((2 * j + 1) * (k + 1), 4 * n);
+                    break;
+               case 10: /* RODFT11: 2 sum x_j sin(pi (2j+1)(2k+1) / 4n) */
+                    for (j = 0; j < n; ++j) acc += 2 * (T)x[j] * r2r_sin((2 * j + 1) * (2 * k + 1), 8 * n);
                     break;
                default:
                     return -1;

@@ -120,6 +120,20 @@ class Restatement:
         assert rc == 0, f"r2r kind {kind} is not restated"
         return y
 
+    def r2r_nd(self, x, shape, kinds, prec="d"):
+        """Multi-dimensional r2r of a row-major array of the given shape
+        (batched over any leading elements): the 1D r2r of kinds[d] along each
+        dim d, the separable product the reference defines."""
+        rt, _ = _PREC[prec]
+        r = len(shape)
+        a = _as(x, rt).reshape((-1,) + tuple(shape))
+        for d in range(r):
+            ax = 1 + d
+            b = np.ascontiguousarray(np.moveaxis(a, ax, -1))
+            y = self.r2r(b.ravel(), shape[d], kinds[d], prec).reshape(b.shape)
+            a = np.moveaxis(y, -1, ax)
+        return np.ascontiguousarray(a).ravel()
+
     def dft_method(self, x, sign=FFTW_FORWARD, method=1, prec="d"):
         """One 1D DFT with a named solver: 1 CT, 2 generic, 3 Rader, 4 Bluestein."""
         rt, ct = _PREC[prec]

@@ -60,15 +60,23 @@ def test_invalid_arguments_return_null(lib):
             assert not f(1, n, -1, 16, None, 1, 64, 32, None, 1, 64, -1, g.FFTW_ESTIMATE)
             assert not f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, 0, g.FFTW_ESTIMATE)   # sign must be +-1
             assert f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, -1, g.FFTW_ESTIMATE)
-            # r2r: rank 1 of the kinds built here; other kinds and rank > 1 return NULL
+            # r2r: every fftw_r2r_kind (api/fftw3.h:96-100), any rank; a kind
+            # out of range and a size-1 REDFT00 (not defined) return NULL
             f = getattr(lib, pfx + "plan_many_r2r")
             f.restype = ctypes.c_void_p
-            for kind, ok in ((0, True), (1, True), (2, True), (4, True), (5, True), (8, True), (9, True),
-                             (3, False), (6, False), (7, False), (10, False)):
+            for kind in range(11):
                 kinds = (ctypes.c_int * 2)(kind, kind)
-                assert bool(f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, kinds, 64)) == ok, kind
-            n2 = (ctypes.c_int * 2)(8, 8)
-            assert not f(2, n2, 1, 16, None, 1, 64, 32, None, 1, 64, (ctypes.c_int * 2)(5, 5), 64)
+                assert f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, kinds, 64), kind
+            assert not f(1, n, 1, 16, None, 1, 64, 32, None, 1, 64, (ctypes.c_int * 1)(11), 64)
+            one = (ctypes.c_int * 1)(1)
+            assert not f(1, one, 1, 16, None, 1, 1, 32, None, 1, 1, (ctypes.c_int * 1)(3), 64)
+            assert "REDFT00" in g.last_error()
+            assert f(1, one, 1, 16, None, 1, 1, 32, None, 1, 1, (ctypes.c_int * 1)(7), 64)
+            assert f(0, n, 5, 16, None, 1, 2, 32, None, 1, 3, (ctypes.c_int * 1)(0), 64)   # rank 0: a copy
+            n3 = (ctypes.c_int * 3)(6, 5, 8)
+            p = f(3, n3, 2, 16, None, 1, 240, 32, None, 1, 240, (ctypes.c_int * 3)(3, 10, 1), 64)
+            assert p
+            assert getattr(lib, pfx + "sprint_plan")(p).decode().count("(dim ") == 3
     finally:
         g.set_dry_run(False)
 

@@ -377,13 +377,17 @@ def test_c2c_bluestein_multipass(lib, torch_cuda, restatement, n, prec):
         assert rel_l2(y, oracle_c2c(restatement, x, [n], sign, prec)) <= TOL[prec]
 
 
-LARGE_REAL = [(1 << 16, "f"), (40000, "f"), (1 << 20, "f"), (1 << 15, "d"), (60000, "d")]
+LARGE_REAL = [(1 << 16, "f"), (40000, "f"), (1 << 20, "f"), (1 << 15, "d"), (60000, "d"),
+              (4099, "f"), (12297, "f"), (2049, "d"), (4099, "d"), (8198, "d")]
 
 
 @pytest.mark.parametrize("n,prec", LARGE_REAL)
 def test_r2c_c2r_multipass(lib, torch_cuda, restatement, n, prec):
-    """Even real lengths beyond one CTA: half-length c2c over the real array
-    as pairs plus an element-wise hc2c pass."""
+    """Real lengths beyond one CTA: even lengths as a half-length c2c over the
+    real array as pairs plus an element-wise hc2c pass; lengths with a prime
+    factor > 13 beyond one CTA (4099, 3 x 4099, and in double 2049, 4099,
+    2 x 4099) as Bluestein's convolution read from the real array (r2c) or
+    the Hermitian-extended half spectrum (c2r)."""
     import fftw3_gb300 as g
     torch = torch_cuda
     rng = np.random.default_rng(n + 7)
@@ -404,6 +408,36 @@ def test_r2c_c2r_multipass(lib, torch_cuda, restatement, n, prec):
     q.execute()
     ref = restatement.c2r(z.astype(np.clongdouble if prec == "d" else np.complex128), [n], op, nthreads=4)
     assert rel_l2(_host(ro), ref) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_r2c_c2r_strided_beyond_one_cta(lib, torch_cuda, restatement, prec):
+    """An even length beyond one CTA with a real stride of 2 (r2c input, c2r
+    output): not a complex array of pairs, so it runs as the convolution."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    n, hm = 40000, 2
+    nc = n // 2 + 1
+    rng = np.random.default_rng(77)
+    src = rng.standard_normal(2 * n * hm)
+    xi = _dev(torch, src.astype(RT[prec]))
+    yo = torch.empty(hm * nc, dtype=torch.complex64 if prec == "f" else torch.complex128, device="cuda")
+    p = g.plan_many_dft_r2c([n], hm, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE, prec, istride=2, idist=2 * n)
+    assert "pointwise" in p.describe()
+    p.execute()
+    op = "l" if prec == "d" else "d"
+    x = src.reshape(hm, 2 * n)[:, ::2].ravel()
+    ref = restatement.r2c(x.astype(np.longdouble if prec == "d" else np.float64), [n], op, nthreads=4)
+    assert rel_l2(_host(yo), ref) <= TOL[prec]
+    z = rng.standard_normal(nc * hm) + 1j * rng.standard_normal(nc * hm)
+    zi = _dev(torch, z.astype(CT[prec]))
+    ro = torch.zeros(hm * 2 * n, dtype=torch.float32 if prec == "f" else torch.float64, device="cuda")
+    q = g.plan_many_dft_c2r([n], hm, zi.data_ptr(), ro.data_ptr(), g.FFTW_ESTIMATE, prec, ostride=2, odist=2 * n)
+    q.execute()
+    ref = restatement.c2r(z.astype(np.clongdouble if prec == "d" else np.complex128), [n], op, nthreads=4)
+    out = _host(ro).reshape(hm, 2 * n)
+    assert rel_l2(out[:, ::2].ravel(), ref) <= TOL[prec]
+    assert np.all(out[:, 1::2] == 0)
 
 
 def test_c2r_multid_preserve_input_is_null(lib):

@@ -1,6 +1,8 @@
-"""1D r2r transforms (plan_r2r_1d, plan_many_r2r, execute_r2r) on the GPU
-against the oracle's defining sums (long double): float rel L2 <= 1e-6,
-double <= 1e-14; round trips of each kind with its unnormalized inverse."""
+"""r2r transforms (plan_r2r_1d/2d/3d, plan_many_r2r, plan_guru_r2r,
+execute_r2r) on the GPU against the oracle's defining sums (double for float
+results, long double for double results): float rel L2 <= 1e-6, double <=
+1e-14; round trips of each kind with its unnormalized inverse; multi-d r2r as
+the separable product of the 1D kinds."""
 import ctypes
 
 import numpy as np
@@ -10,8 +12,16 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-KINDS = {0: "R2HC", 1: "HC2R", 2: "DHT", 4: "REDFT01", 5: "REDFT10", 8: "RODFT01", 9: "RODFT10"}
-INVERSE = {0: 1, 1: 0, 2: 2, 4: 5, 5: 4, 8: 9, 9: 8}
+KINDS = {0: "R2HC", 1: "HC2R", 2: "DHT", 3: "REDFT00", 4: "REDFT01", 5: "REDFT10", 6: "REDFT11", 7: "RODFT00",
+         8: "RODFT01", 9: "RODFT10", 10: "RODFT11"}
+INVERSE = {0: 1, 1: 0, 2: 2, 3: 3, 4: 5, 5: 4, 6: 6, 7: 7, 8: 9, 9: 8, 10: 10}
+
+
+def logical(kind, n):
+    """The logical DFT size N: the inverse kind undoes a kind up to N."""
+    return {3: 2 * (n - 1), 7: 2 * (n + 1)}.get(kind, 2 * n if kind >= 4 else n)
+
+
 TOL = {"f": 1e-6, "d": 1e-14}
 RT = {"f": np.float32, "d": np.float64}
 
@@ -46,6 +56,8 @@ def run(lib, prec, p, inp, out):
 @pytest.mark.parametrize("kind", sorted(KINDS), ids=[KINDS[k] for k in sorted(KINDS)])
 @pytest.mark.parametrize("n", [1, 2, 5, 8, 17, 100, 1024])
 def test_r2r_device(lib, torch_cuda, restatement, prec, kind, n):
+    if kind == 3 and n == 1:
+        pytest.skip("a size-1 REDFT00 is not defined")
     torch = torch_cuda
     hm = 2
     rng = np.random.default_rng(n + 31 * kind)
@@ -62,8 +74,8 @@ def test_r2r_device(lib, torch_cuda, restatement, prec, kind, n):
 @pytest.mark.parametrize("kind", sorted(KINDS), ids=[KINDS[k] for k in sorted(KINDS)])
 def test_r2r_round_trip_and_layouts(lib, torch_cuda, restatement, kind):
     """Strided input (stride 2, distance 2n+1), host output; then the inverse
-    kind on device arrays gives back N x the input (N = n, or 2n for the
-    DCT/DST pairs)."""
+    kind on device arrays gives back N x the input (N the logical DFT size:
+    n for R2HC/HC2R/DHT, 2(n-1) for REDFT00, 2(n+1) for RODFT00, else 2n)."""
     torch = torch_cuda
     n, hm = 96, 4
     rng = np.random.default_rng(40 + kind)
@@ -79,7 +91,7 @@ def test_r2r_round_trip_and_layouts(lib, torch_cuda, restatement, kind):
     dz = torch.zeros_like(dy)
     q = plan_many(lib, "f", n, hm, dy.data_ptr(), dz.data_ptr(), INVERSE[kind])
     run(lib, "f", q, dy.data_ptr(), dz.data_ptr())
-    scale = 2 * n if kind in (4, 5, 8, 9) else n
+    scale = logical(kind, n)
     assert rel_l2(dz.cpu().numpy().astype(np.float64) / scale, x.ravel().astype(np.float64)) <= 2e-6
 
 
@@ -100,3 +112,106 @@ def test_r2r_1d_in_place_and_execute(lib, torch_cuda, restatement):
     torch.cuda.synchronize()
     ref = restatement.r2r(x.astype(np.float64), n, 5, "d")
     assert rel_l2(dx.cpu().numpy().astype(np.float64), ref) <= 1e-6
+
+
+def plan_r2r_nd(lib, prec, shape, kinds, inp, out):
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    f = getattr(lib, pfx + "plan_r2r")
+    f.restype = ctypes.c_void_p
+    r = len(shape)
+    p = f(r, (ctypes.c_int * r)(*shape), inp, out, (ctypes.c_int * r)(*kinds), 64)
+    assert p, lib.fftw_gb300_last_error()
+    return p
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("shape,kinds", [([12, 17], [5, 10]), ([9, 16], [3, 0]), ([6, 9, 10], [3, 2, 7]),
+                                         ([8, 5, 4], [6, 1, 9])])
+def test_r2r_multid_device(lib, torch_cuda, restatement, prec, shape, kinds):
+    """plan_r2r of rank 2 and 3 with a different kind per dim, device arrays."""
+    torch = torch_cuda
+    tot = int(np.prod(shape))
+    rng = np.random.default_rng(tot + sum(kinds))
+    x = rng.standard_normal(tot).astype(RT[prec])
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.zeros_like(dx)
+    p = plan_r2r_nd(lib, prec, shape, kinds, dx.data_ptr(), dy.data_ptr())
+    run(lib, prec, p, dx.data_ptr(), dy.data_ptr())
+    torch.cuda.synchronize()
+    op = "d" if prec == "f" else "l"
+    ref = restatement.r2r_nd(x.astype(np.float64 if prec == "f" else np.longdouble), shape, kinds, op)
+    assert rel_l2(dy.cpu().numpy().astype(np.float64), ref.astype(np.float64)) <= TOL[prec]
+
+
+def test_r2r_multid_many_host_strided(lib, restatement):
+    """plan_many_r2r rank 2 with howmany 3 on pageable host arrays: input
+    elements 2 reals apart (inembed pads the rows), output dense; then the
+    inverse kinds in place give back N0 N1 x the input."""
+    n0, n1, hm = 10, 14, 3
+    kinds, inv = [7, 4], [7, 5]
+    ie = [n0, 16]
+    idist = 2 * n0 * 16 + 5
+    rng = np.random.default_rng(50)
+    src = rng.standard_normal(idist * hm).astype(np.float32)
+    keep = src.copy()
+    x = np.stack([src[t * idist: t * idist + 2 * n0 * 16: 2].reshape(n0, 16)[:, :n1] for t in range(hm)])
+    y = np.full(n0 * n1 * hm, 3.0, dtype=np.float32)
+    f = lib.fftwf_plan_many_r2r
+    f.restype = ctypes.c_void_p
+    nn = (ctypes.c_int * 2)(n0, n1)
+    p = f(2, nn, hm, src.ctypes.data, (ctypes.c_int * 2)(*ie), 2, idist, y.ctypes.data, None, 1, n0 * n1,
+          (ctypes.c_int * 2)(*kinds), 64)
+    assert p, lib.fftw_gb300_last_error()
+    run(lib, "f", p, src.ctypes.data, y.ctypes.data)
+    assert np.array_equal(src, keep)
+    ref = restatement.r2r_nd(x.astype(np.float64).ravel(), [n0, n1], kinds, "d")
+    assert rel_l2(y.astype(np.float64), ref) <= 1e-6
+    q = f(2, nn, hm, y.ctypes.data, None, 1, n0 * n1, y.ctypes.data, None, 1, n0 * n1, (ctypes.c_int * 2)(*inv), 64)
+    assert q, lib.fftw_gb300_last_error()
+    run(lib, "f", q, y.ctypes.data, y.ctypes.data)
+    scale = logical(7, n0) * logical(4, n1)
+    assert rel_l2(y.astype(np.float64) / scale, x.ravel().astype(np.float64)) <= 2e-6
+
+
+def test_r2r_guru_rank2_in_place_device(lib, torch_cuda, restatement):
+    """plan_guru_r2r rank 2 (REDFT11 x R2HC) with one howmany dim, in place on a device array."""
+    torch = torch_cuda
+    n0, n1, hm = 16, 24, 2
+    rng = np.random.default_rng(51)
+    x = rng.standard_normal(n0 * n1 * hm)
+    dx = torch.from_numpy(x.copy()).cuda()
+
+    class IoDim(ctypes.Structure):
+        _fields_ = [("n", ctypes.c_int), ("is_", ctypes.c_int), ("os", ctypes.c_int)]
+    dims = (IoDim * 2)(IoDim(n0, n1, n1), IoDim(n1, 1, 1))
+    hdims = (IoDim * 1)(IoDim(hm, n0 * n1, n0 * n1))
+    f = lib.fftw_plan_guru_r2r
+    f.restype = ctypes.c_void_p
+    p = f(2, dims, 1, hdims, dx.data_ptr(), dx.data_ptr(), (ctypes.c_int * 2)(6, 0), 64)
+    assert p, lib.fftw_gb300_last_error()
+    run(lib, "d", p, dx.data_ptr(), dx.data_ptr())
+    torch.cuda.synchronize()
+    ref = restatement.r2r_nd(x.astype(np.longdouble), [n0, n1], [6, 0], "l")
+    assert rel_l2(dx.cpu().numpy(), ref.astype(np.float64)) <= 1e-14
+
+
+def test_r2r_rank0_copy(lib, torch_cuda):
+    """plan_guru_r2r of rank 0: a copy of the howmany elements (2D howmany
+    dims with strides 3 and 2 reals in, dense out), as in the reference."""
+    torch = torch_cuda
+    rng = np.random.default_rng(52)
+    src = rng.standard_normal(3 * 40 * 7).astype(np.float32)
+    ds = torch.from_numpy(src).cuda()
+    dd = torch.zeros(40 * 7, dtype=torch.float32, device="cuda")
+
+    class IoDim(ctypes.Structure):
+        _fields_ = [("n", ctypes.c_int), ("is_", ctypes.c_int), ("os", ctypes.c_int)]
+    hdims = (IoDim * 2)(IoDim(40, 21, 7), IoDim(7, 3, 1))
+    f = lib.fftwf_plan_guru_r2r
+    f.restype = ctypes.c_void_p
+    p = f(0, None, 2, hdims, ds.data_ptr(), dd.data_ptr(), None, 64)
+    assert p, lib.fftw_gb300_last_error()
+    run(lib, "f", p, ds.data_ptr(), dd.data_ptr())
+    torch.cuda.synchronize()
+    want = src.reshape(40, 21)[:, 0:21:3].ravel()
+    assert np.array_equal(dd.cpu().numpy(), want)

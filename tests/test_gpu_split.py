@@ -1,9 +1,11 @@
-"""Split-array DFTs (fftw[f]_plan_guru_split_dft / execute_split_dft):
-always the forward DFT of ri + i*ii into ro + i*io, strides counted in
-reals.  Checked against the oracle (float: rel L2 <= 1e-6 vs FP64; double:
-<= 1e-14 vs long double) for separate arrays (pack / c2c / unpack), arrays
-that interleave (an ordinary complex plan) or interleave swapped, host and
-device arrays, strided layouts, in place, and new-array execute."""
+"""Split-array transforms: fftw[f]_plan_guru_split_dft / execute_split_dft
+(always the forward DFT of ri + i*ii into ro + i*io) and the r2c / c2r forms
+plan_guru_split_dft_r2c / _c2r with execute_split_dft_r2c / _c2r, strides
+counted in reals.  Checked against the oracle (float: rel L2 <= 1e-6 vs FP64;
+double: <= 1e-14 vs long double) for separate arrays (copy / transform /
+copy), arrays that interleave (an ordinary complex, r2c or c2r plan) or
+interleave swapped, host and device arrays, strided layouts, in place, and
+new-array execute."""
 import numpy as np
 import pytest
 
@@ -128,3 +130,84 @@ def test_split_overlapping_spans_odd_stride(lib, restatement):
     assert rel_l2(y, oracle(restatement, x, [n], "f")) <= 1e-6
     assert np.all(out[2:3 * n:3] == 7.0) and out[-1] == 7.0      # gaps untouched
     assert np.array_equal(buf, keep)                              # input untouched
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_split_r2c_separate_host_arrays(lib, restatement, prec):
+    """plan_guru_split_dft_r2c, rank 2 with one howmany dim: real input on
+    pageable host memory, ro and io separate host arrays (last dim n/2+1)."""
+    import fftw3_gb300 as g
+    n0, n1, hm = 12, 20, 3
+    nc = n1 // 2 + 1
+    rng = np.random.default_rng(36)
+    x = rng.standard_normal(n0 * n1 * hm).astype(RT[prec])
+    ro = np.zeros(n0 * nc * hm, dtype=RT[prec])
+    io = np.zeros_like(ro)
+    p = g.plan_guru_split_dft_r2c([(n0, n1, nc), (n1, 1, 1)], [(hm, n0 * n1, n0 * nc)], x.ctypes.data,
+                                  ro.ctypes.data, io.ctypes.data, g.FFTW_ESTIMATE, prec)
+    assert "split-dft-r2c" in p.describe()
+    p.execute()
+    op = "l" if prec == "d" else "d"
+    ref = restatement.r2c(x.astype(np.longdouble if prec == "d" else np.float64), [n0, n1], op)
+    assert rel_l2(ro.astype(np.float64) + 1j * io.astype(np.float64), ref.astype(np.complex128)) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_split_c2r_strided_device_and_new_arrays(lib, torch_cuda, restatement, prec):
+    """plan_guru_split_dft_c2r: ri / ii elements 3 reals apart on the device,
+    dense real output; then execute_split_dft_c2r on new arrays."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    n, hm = 1000, 4
+    nc = n // 2 + 1
+    dist = 3 * nc + 1
+    rng = np.random.default_rng(37)
+    idx = (np.arange(hm)[:, None] * dist + np.arange(nc)[None, :] * 3).ravel()
+    p = None
+    for trial in range(2):
+        a = rng.standard_normal(dist * hm).astype(RT[prec])
+        b = rng.standard_normal(dist * hm).astype(RT[prec])
+        da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        out = torch.zeros(n * hm, dtype=da.dtype, device="cuda")
+        if p is None:
+            p = g.plan_guru_split_dft_c2r([(n, 3, 1)], [(hm, dist, n)], da.data_ptr(), db.data_ptr(),
+                                          out.data_ptr(), g.FFTW_ESTIMATE, prec)
+            assert "split-dft-c2r" in p.describe()
+            p.execute()
+        else:
+            p.execute_split_dft_c2r(da.data_ptr(), db.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        z = a[idx].astype(np.float64) + 1j * b[idx].astype(np.float64)
+        op = "l" if prec == "d" else "d"
+        ref = restatement.c2r(z.astype(np.clongdouble if prec == "d" else np.complex128), [n], op)
+        assert rel_l2(out.cpu().numpy().astype(np.float64), ref.astype(np.float64)) <= TOL[prec]
+        assert np.array_equal(da.cpu().numpy(), a)                 # input preserved
+
+
+def test_split_r2c_c2r_interleaved_views(lib, torch_cuda, restatement):
+    """io = ro + 1 (r2c) and ii = ri + 1 (c2r) with even strides: ordinary
+    r2c / c2r plans, run through execute_split_dft_r2c / _c2r."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    n, hm = 2048, 8
+    nc = n // 2 + 1
+    rng = np.random.default_rng(38)
+    x = rng.standard_normal(n * hm).astype(np.float32)
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.zeros(2 * nc * hm, dtype=torch.float32, device="cuda")
+    o = dy.data_ptr()
+    p = g.plan_guru_split_dft_r2c([(n, 1, 2)], [(hm, n, 2 * nc)], dx.data_ptr(), o, o + 4, g.FFTW_ESTIMATE, "f")
+    assert "split" not in p.describe()
+    p.execute_split_dft_r2c(dx.data_ptr(), o, o + 4)
+    torch.cuda.synchronize()
+    y = dy.cpu().numpy().reshape(hm * nc, 2).astype(np.float64)
+    ref = restatement.r2c(x.astype(np.float64), [n], "d")
+    assert rel_l2(y[:, 0] + 1j * y[:, 1], ref) <= 1e-6
+    dz = torch.zeros(n * hm, dtype=torch.float32, device="cuda")
+    q = g.plan_guru_split_dft_c2r([(n, 2, 1)], [(hm, 2 * nc, n)], o, o + 4, dz.data_ptr(), g.FFTW_ESTIMATE, "f")
+    assert "split" not in q.describe()
+    q.execute()
+    torch.cuda.synchronize()
+    zc = y[:, 0] + 1j * y[:, 1]
+    ref = restatement.c2r(zc, [n], "d")
+    assert rel_l2(dz.cpu().numpy().astype(np.float64), ref) <= 1e-6

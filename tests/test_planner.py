@@ -155,3 +155,58 @@ def test_split_array_plans(lib):
     r = g.plan_guru_split_dft([(12, 20, 1), (20, 1, 12)], [(3, 240, 240)], base, base + 8192, base + 16384,
                               base + 24576, prec="d")
     assert r.describe().startswith("(gb300-split-dft-f64")
+
+
+def test_split_real_plans(lib):
+    """plan_guru_split_dft_r2c/c2r: interleaved complex sides (io = ro + 1,
+    ii = ri + 1, even strides) become ordinary r2c / c2r plans; separate
+    arrays a copy / r2c or c2r / copy plan."""
+    base = 1 << 20
+    p = g.plan_guru_split_dft_r2c([(64, 1, 2)], [(10, 64, 66)], base, base + 8192, base + 8196, prec="f")
+    assert p.describe().startswith("(gb300-rdft2-r2c-f32")
+    q = g.plan_guru_split_dft_r2c([(64, 1, 1)], [(10, 64, 33)], base, base + 8192, base + 16384, prec="f")
+    assert q.describe().startswith("(gb300-split-dft-r2c-f32")
+    r = g.plan_guru_split_dft_c2r([(12, 9, 20), (16, 1, 1)], [], base, base + 8192, base + 16384, prec="d")
+    assert r.describe().startswith("(gb300-split-dft-c2r-f64")
+    t = g.plan_guru_split_dft_c2r([(64, 2, 1)], [(3, 66, 64)], base, base + 8, base + 16384, prec="d")
+    assert t.describe().startswith("(gb300-rdft2-c2r-f64")
+    with pytest.raises(RuntimeError):
+        g.plan_guru_split_dft_r2c([], [(3, 1, 1)], base, base + 8192, base + 16384, prec="f")
+
+
+@pytest.mark.parametrize("n,prec", [(4099, "f"), (12297, "f"), (1000003, "f"), (2049, "d"), (8198, "d")])
+def test_long_real_prime_lengths_run_as_convolution(n, prec):
+    """Real lengths with a prime factor > 13 beyond one CTA: Bluestein's
+    convolution straight from the real array (r2c) or from the
+    Hermitian-extended half spectrum (c2r), FFTs of a power of two >= 2n-1
+    in between."""
+    nb = 1 << (2 * n - 2).bit_length()
+    for make, pin, pout in ((g.plan_many_dft_r2c, "chirp-in-real", "chirp-out-half"),
+                            (g.plan_many_dft_c2r, "chirp-in-herm", "chirp-out-real")):
+        p = make([n], 2, 1 << 20, 1 << 30, prec=prec)
+        lines = p.describe().splitlines()
+        assert f"pointwise:{pin} n={n} nfft={nb} " in lines[1]
+        assert f"pointwise:{pout} n={n} " in lines[-1]
+        assert sum("pointwise:spec-mul" in x for x in lines) == 1
+
+
+def test_strided_long_real_runs_as_convolution():
+    p = g.plan_many_dft_r2c([40000], 2, 1 << 20, 1 << 30, prec="f", istride=2, idist=80000)
+    lines = p.describe().splitlines()
+    assert "pointwise:chirp-in-real" in lines[1] and "pointwise:chirp-out-half" in lines[-1]
+
+
+def test_r2r_stages_per_dim():
+    """A rank-3 r2r plan is one stage per dim, last dim first: a c2r core for
+    HC2R (8), a complex DFT of 2n for odd-length RODFT11 (5), an r2c of
+    2(n-1) for REDFT00 (6)."""
+    lib = g.load()
+    f = lib.fftwf_plan_many_r2r
+    f.restype = ctypes.c_void_p
+    p = f(3, (ctypes.c_int * 3)(6, 5, 8), 2, 1 << 20, None, 1, 240, 1 << 30, None, 1, 240,
+          (ctypes.c_int * 3)(3, 10, 1), 64)
+    assert p
+    d = lib.fftwf_sprint_plan(p).decode()
+    i2, i1, i0 = d.index("(dim 2 kind 1"), d.index("(dim 1 kind 10"), d.index("(dim 0 kind 3")
+    assert i2 < i1 < i0
+    assert "rdft2-c2r" in d[i2:i1] and "n=10" in d[i1:i0] and "r2c n=10" in d[i0:]

@@ -24,22 +24,26 @@ def test_help_and_version(lib, prec):
 
 
 def test_rejects_bad_sizes_and_options(lib):
-    r = tool("f", "-e", "-n", "kof1024")
-    assert r.returncode == 1 and "cannot parse size kof1024" in r.stderr
+    # r2r (type k) sizes take no direction and a kind after each dim
+    for bad in ("kof1024", "koe12x16", "kx10e10", "ko10e12", "cof", "cxf64"):
+        r = tool("f", "-e", "-n", bad)
+        assert r.returncode == 1 and f"cannot parse size {bad}" in r.stderr, bad
     r = tool("f", "--bogus")
     assert r.returncode == 1 and "unknown option" in r.stderr
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the message given without a GPU")
 def test_without_gpu_reports_each_size(lib):
-    r = tool("f", "-e", "-n", "cof64")
-    assert r.returncode == 1 and "cannot plan cof64" in r.stderr
+    for size in ("cof64", "ko10e10x16o11", "ki64", "ki32hx8e00"):
+        r = tool("f", "-e", "-n", size)
+        assert r.returncode == 1 and f"cannot plan {size}" in r.stderr, size
 
 
 @pytest.mark.gpu
 def test_tuned_wisdom_round_trip(lib, tmp_path):
     out = tmp_path / "w.txt"
-    r = tool("f", "-m", "-n", "-o", str(out), "cof4096", "cib1024", "rof2048", "cof64x64", timeout=600)
+    r = tool("f", "-m", "-n", "-o", str(out), "cof4096", "cib1024", "rof2048", "cof64x64", "ko96e10x100o11",
+             timeout=600)
     assert r.returncode == 0, r.stderr
     text = out.read_text()
     assert text.startswith("(fftw-3.3.10-gb300 fftwf_wisdom") and '"c2c p4 n4096"' in text
