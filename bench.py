@@ -49,7 +49,9 @@ WORKLOADS = {
     "c2c1m": ("c2c", [1 << 20], 64, "f", False),
     "c3d512": ("c2c", [512, 512, 512], 1, "f", True),
     "r2c2d8192": ("r2c", [8192, 8192], 1, "f", False),
+    "r2r4096": ("r2r", [4096], 65536, "f", False),     # REDFT10 (DCT-II)
 }
+R2R_KIND = 5   # fftw_r2r_kind REDFT10 of the r2r workloads
 METRIC = "FFT Gflop/s (5N log2N/t) & HBM %peak: split-FP16 TC vs FP32, rel err<=1e-6"
 
 
@@ -97,7 +99,7 @@ def uneven_lengths(rng, count, max_pow2=16, max_smooth=60000, max_prime=4093):
 def flops_per_step(kind, shape, howmany):
     n = math.prod(shape)
     f = 5.0 * n * math.log2(n) * howmany
-    return f / 2 if kind in ("r2c", "c2r") else f
+    return f / 2 if kind in ("r2c", "c2r", "r2r") else f
 
 
 def bytes_per_step(kind, shape, howmany, prec):
@@ -105,6 +107,8 @@ def bytes_per_step(kind, shape, howmany, prec):
     cs = 8 if prec == "f" else 16
     if kind == "c2c":
         return 2 * n * cs * howmany
+    if kind == "r2r":
+        return n * cs * howmany
     nc = n // shape[-1] * (shape[-1] // 2 + 1)
     return (n * cs // 2 + nc * cs) * howmany
 
@@ -312,6 +316,11 @@ def run_ours(args):
         xin = torch.randn(howmany * n, dtype=cdt, device="cuda", generator=gen)
         yout = xin if inplace else torch.empty_like(xin)
         p = g.plan_many_dft(shape, howmany, xin.data_ptr(), yout.data_ptr(), -1, g.FFTW_ESTIMATE, prec)
+    elif kind == "r2r":
+        xin = torch.randn(howmany * n, dtype=rdt, device="cuda", generator=gen)
+        yout = torch.empty_like(xin)
+        p = g.plan_many_r2r(shape, howmany, xin.data_ptr(), yout.data_ptr(), [R2R_KIND] * len(shape),
+                            g.FFTW_ESTIMATE, prec)
     else:
         xin = torch.randn(howmany * n, dtype=rdt, device="cuda", generator=gen)
         yout = torch.empty(howmany * nc, dtype=cdt, device="cuda")
@@ -323,6 +332,8 @@ def run_ours(args):
     def step():
         if kind == "c2c":
             p.execute_dft(xin.data_ptr(), yout.data_ptr())
+        elif kind == "r2r":
+            p.execute_r2r(xin.data_ptr(), yout.data_ptr())
         else:
             p.execute_dft_r2c(xin.data_ptr(), yout.data_ptr())
 
@@ -360,6 +371,14 @@ def run_ours(args):
         torch.cuda.synchronize()
         err = float(torch.linalg.vector_norm(xin / n - x0) / torch.linalg.vector_norm(x0))
         k = 0
+    elif kind == "r2r":
+        k = min(k, 8)   # the oracle evaluates the defining sum, O(n^2) per transform
+        xs = xin[: k * n].cpu().numpy()
+        step()
+        torch.cuda.synchronize()
+        ref = Restatement().r2r(xs.astype(np.float64 if prec == "f" else np.longdouble), n, R2R_KIND,
+                                "d" if prec == "f" else "l")
+        err = rel_l2(yout[: k * n].cpu().numpy(), ref)
     elif kind == "c2c":
         xs = xin[: k * n].cpu().numpy()
         step()
@@ -397,7 +416,7 @@ def run_ours(args):
         e2e = run_e2e(lib, g, kind, shape, howmany, prec, inplace, args)
 
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu and kind != "r2r":
         cpu = cpu_sample(args.workload, os.cpu_count() or 1, budget_s=12.0, prefer_ref=True)
 
     if rank == 0:
@@ -406,7 +425,8 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if prec == "f" else "f64", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: fftw{'f' if prec == 'f' else ''}_plan_many_dft{'_r2c' if kind == 'r2c' else ''} "
+            "config": {"workload": f"{args.workload}: fftw{'f' if prec == 'f' else ''}_plan_many_"
+                                   f"{'r2r REDFT10' if kind == 'r2r' else 'dft_r2c' if kind == 'r2c' else 'dft'} "
                                    f"{'x'.join(map(str, shape))} x {howmany}, {'in place' if inplace else 'out of place'}, FFTW_ESTIMATE",
                        "inputs": "N(0,1) from torch.Generator seed 1234+rank; batch larger than L2 (no flush needed)",
                        "form": "plain FP32 CUDA-core" if prec == "f" else "FP64",
@@ -566,7 +586,7 @@ def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
     cs = 8 if prec == "f" else 16
     nc = n // shape[-1] * (shape[-1] // 2 + 1)
     in_bytes = howmany * n * (cs if kind == "c2c" else cs // 2)
-    out_bytes = howmany * (n if kind == "c2c" else nc) * cs
+    out_bytes = howmany * n * cs // 2 if kind == "r2r" else howmany * (n if kind == "c2c" else nc) * cs
     pfx = "fftwf_" if prec == "f" else "fftw_"
     hin = getattr(lib, pfx + "malloc")(in_bytes)
     hout = hin if inplace else getattr(lib, pfx + "malloc")(out_bytes)
@@ -576,6 +596,9 @@ def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
     if kind == "c2c":
         p = g.plan_many_dft(shape, howmany, hin, hout, -1, g.FFTW_ESTIMATE, prec)
         ex = lambda: p.execute_dft(hin, hout)
+    elif kind == "r2r":
+        p = g.plan_many_r2r(shape, howmany, hin, hout, [R2R_KIND] * len(shape), g.FFTW_ESTIMATE, prec)
+        ex = lambda: p.execute_r2r(hin, hout)
     else:
         p = g.plan_many_dft_r2c(shape, howmany, hin, hout, g.FFTW_ESTIMATE, prec)
         ex = lambda: p.execute_dft_r2c(hin, hout)
@@ -600,7 +623,7 @@ def run_e2e(lib, g, kind, shape, howmany, prec, inplace, args):
     return {"value": round(v, 2), "unit": "Gflop/s", "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": out_bytes,
             "ms_per_step": round(dt * 1e3, 3), "ms_min": round(min(each) * 1e3, 3), "ms_max": round(max(each) * 1e3, 3),
             "path": path,
-            "timer": "host wall clock around fftwf_execute_dft (synchronous)"}
+            "timer": "host wall clock around the execute call (synchronous)"}
 
 
 def main():

@@ -71,6 +71,7 @@ def _sigs(lib, pfx):
     f("plan_guru_dft_r2c", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, cu])
     f("plan_guru_dft_c2r", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, cu])
     f("plan_many_r2r", vp, [ci, ip, ci, vp, ip, ci, ci, vp, ip, ci, ci, vp, cu])
+    f("execute_r2r", None, [vp, vp, vp])
     f("plan_guru_split_dft", vp, [ci, ctypes.POINTER(IODim), ci, ctypes.POINTER(IODim), vp, vp, vp, vp, cu])
     f("plan_guru64_split_dft", vp, [ci, ctypes.POINTER(IODim64), ci, ctypes.POINTER(IODim64), vp, vp, vp, vp, cu])
     f("execute_split_dft", None, [vp, vp, vp, vp, vp])
@@ -178,6 +179,9 @@ class Plan:
     def execute_dft_c2r(self, i, o):
         self._f("execute_dft_c2r")(self.ptr, i, o)
 
+    def execute_r2r(self, i, o):
+        self._f("execute_r2r")(self.ptr, i, o)
+
     def execute_split_dft(self, ri, ii, ro, io):
         self._f("execute_split_dft")(self.ptr, ri, ii, ro, io)
 
@@ -283,6 +287,21 @@ def plan_guru_split_dft(dims, howmany_dims, ri, ii, ro, io, flags=FFTW_ESTIMATE,
     d = (IODim * max(1, len(dims)))(*[IODim(*x) for x in dims])
     h = (IODim * max(1, len(howmany_dims)))(*[IODim(*x) for x in howmany_dims])
     p = getattr(lib, pfx + "plan_guru_split_dft")(len(dims), d, len(howmany_dims), h, ri, ii, ro, io, flags)
+    return Plan(p, prec)
+
+
+def plan_many_r2r(n, howmany, inp, out, kinds, flags=FFTW_ESTIMATE, prec="f", inembed=None, istride=1,
+                  idist=None, onembed=None, ostride=1, odist=None) -> Plan:
+    """r2r of rank len(n), one fftw_r2r_kind value per dim; strides in reals."""
+    lib = load()
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    tot = 1
+    for d in n:
+        tot *= d
+    k = (ctypes.c_int * len(kinds))(*kinds)
+    p = getattr(lib, pfx + "plan_many_r2r")(len(n), _iarr(n), howmany, inp, _iarr(inembed), istride,
+                                            tot if idist is None else idist, out, _iarr(onembed), ostride,
+                                            tot if odist is None else odist, k, flags)
     return Plan(p, prec)
 
 

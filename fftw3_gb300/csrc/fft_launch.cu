@@ -178,6 +178,8 @@ static unsigned long long gb_launches = 0;
 
 extern "C" long long gb_launch_count(void) { return (long long)__atomic_load_n(&gb_launches, __ATOMIC_RELAXED); }
 
+extern "C" void gb_count_launch(void) { __atomic_add_fetch(&gb_launches, 1ull, __ATOMIC_RELAXED); }
+
 extern "C" const char *gb_last_cuda_error(void) { return gb_errbuf; }
 
 static int gb_check(cudaError_t e, const char *what)

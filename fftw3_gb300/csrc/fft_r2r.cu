@@ -4,8 +4,14 @@
  * buffers between these two kernels; gb_r2r.c holds the algorithms with the
  * reference definitions.  Each thread handles one element of one transform
  * of the batch; the batch is a vector loop of up to GB_R2R_MAXV dims with
- * strides in reals.  Twiddles exp(+-i pi m / 2n) and exp(-i pi m / 4n) come
- * from the FP64 octant-reduced cexp rounded once.
+ * strides in reals.  The twiddles come from a per-stage table built once at
+ * plan time (k_r2r_table: the FP64 octant-reduced cexp rounded once), so the
+ * pre and post kernels do no FP64 work:
+ *   REDFT01/10, RODFT01/10:   w[q] = exp(-i pi q / 2n), q < n
+ *   REDFT11/RODFT11, even n:  w[m] = exp(-i pi (4m+1) / 4n), m < n/2;
+ *                             w[n/2 + p] = exp(-i pi p / n), p < n/2
+ *   REDFT11/RODFT11, odd n:   w[m] = exp(-i pi m / 2n), m < n;
+ *                             w[n + k] = exp(-i pi (2k+1) / 4n), k < n
  *
  * Core buffers per transform (row t of the batch):
  *   r2c core: pre writes L reals, post reads L/2+1 complex
@@ -41,6 +47,25 @@ __device__ __forceinline__ C half_spec(const C *V, long long n, long long k)
      return mk<C>(z.x, -z.y);
 }
 
+/* twiddle table entry i of a stage (layout in the file comment) */
+template <typename C>
+__device__ __forceinline__ C r2r_table_entry(int kind, long long n, long long i)
+{
+     if (kind == R2R_REDFT11 || kind == R2R_RODFT11) {
+          if (!(n & 1)) return i < n / 2 ? r2r_twiddle<C>(4 * i + 1, 8 * n, -1) : r2r_twiddle<C>(i - n / 2, 2 * n, -1);
+          return i < n ? r2r_twiddle<C>(i, 4 * n, -1) : r2r_twiddle<C>(2 * (i - n) + 1, 8 * n, -1);
+     }
+     return r2r_twiddle<C>(i, 4 * n, -1);
+}
+
+template <typename C>
+__global__ void k_r2r_table(int kind, long long n, long long len, C *tab)
+{
+     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len;
+          i += (long long)gridDim.x * blockDim.x)
+          tab[i] = r2r_table_entry<C>(kind, n, i);
+}
+
 /* element offset (reals) of vector index t on the input (out = 0) or output side */
 __device__ __forceinline__ long long vec_offset(const gb_r2r_vec &v, long long t, int out)
 {
@@ -54,17 +79,34 @@ __device__ __forceinline__ long long vec_offset(const gb_r2r_vec &v, long long t
      return off;
 }
 
+/* row and column of element g of a batch of rows of length per (32-bit
+ * division when the batch fits) */
+__device__ __forceinline__ void r2r_split(long long g, long long per, bool small, long long *t, long long *m)
+{
+     if (small) {
+          const unsigned q = (unsigned)g / (unsigned)per;
+          *t = q;
+          *m = (long long)((unsigned)g - q * (unsigned)per);
+     } else {
+          *t = g / per;
+          *m = g - *t * per;
+     }
+}
+
 template <typename R>
 __global__ void k_r2r_pre(int kind, long long n, long long L, long long V, const R *__restrict__ in, long long is,
-                          const gb_r2r_vec vec, void *__restrict__ buf)
+                          const gb_r2r_vec vec, void *__restrict__ buf, const void *__restrict__ twv)
 {
      typedef typename cplx_of<R>::T C;
+     const C *tw = (const C *)twv;
      long long Lc;
      const int core = gb_r2r_core(kind, n, &Lc);
      const long long per = core == GB_R2R_CORE_C2R ? L / 2 + 1 : L;
+     const bool small = per * V < (1LL << 32);
      for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < per * V;
           g += (long long)gridDim.x * blockDim.x) {
-          const long long t = g / per, m = g - t * per;
+          long long t, m;
+          r2r_split(g, per, small, &t, &m);
           const R *x = in + vec_offset(vec, t, 0);
           switch (kind) {
           case R2R_R2HC:
@@ -108,7 +150,7 @@ __global__ void k_r2r_pre(int kind, long long n, long long L, long long V, const
                const bool rev = (kind == R2R_RODFT01);
                const R a = x[(rev ? n - 1 - m : m) * is];
                const R b = (m == 0) ? (R)0 : x[(rev ? m - 1 : n - m) * is];
-               const C w = r2r_twiddle<C>(m, 4 * n, 1);
+               const C w0 = __ldg(tw + m), w = mk<C>(w0.x, -w0.y);   /* exp(i pi m / 2n) */
                /* (a - i b) * w */
                ((C *)buf)[g] = mk<C>(a * w.x + b * w.y, a * w.y - b * w.x);
                break;
@@ -122,11 +164,11 @@ __global__ void k_r2r_pre(int kind, long long n, long long L, long long V, const
                if (!(n & 1)) {
                     const long long ja = 2 * m, jb = n - 1 - 2 * m;
                     const R a = x[(rev ? jb : ja) * is], b = x[(rev ? ja : jb) * is];
-                    const C w = r2r_twiddle<C>(4 * m + 1, 8 * n, -1);
+                    const C w = __ldg(tw + m);
                     z = mk<C>(a * w.x - b * w.y, a * w.y + b * w.x);
                } else if (m < n) {
                     const R a = x[(rev ? n - 1 - m : m) * is];
-                    const C w = r2r_twiddle<C>(m, 4 * n, -1);
+                    const C w = __ldg(tw + m);
                     z = mk<C>(a * w.x, a * w.y);
                } else {
                     z = mk<C>((R)0, (R)0);
@@ -140,15 +182,18 @@ __global__ void k_r2r_pre(int kind, long long n, long long L, long long V, const
 
 template <typename R>
 __global__ void k_r2r_post(int kind, long long n, long long L, long long V, const void *__restrict__ buf,
-                           R *__restrict__ out, long long os, const gb_r2r_vec vec)
+                           R *__restrict__ out, long long os, const gb_r2r_vec vec, const void *__restrict__ twv)
 {
      typedef typename cplx_of<R>::T C;
+     const C *tw = (const C *)twv;
      long long Lc;
      const int core = gb_r2r_core(kind, n, &Lc);
      const long long rowc = core == GB_R2R_CORE_R2C ? L / 2 + 1 : L;   /* complex row length */
+     const bool small = n * V < (1LL << 32);
      for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n * V;
           g += (long long)gridDim.x * blockDim.x) {
-          const long long t = g / n, k = g - t * n;
+          long long t, k;
+          r2r_split(g, n, small, &t, &k);
           R *y = out + vec_offset(vec, t, 1);
           const C *Z = (const C *)buf + t * rowc;
           const R *v = (const R *)buf + t * L;
@@ -167,7 +212,7 @@ __global__ void k_r2r_post(int kind, long long n, long long L, long long V, cons
                /* DCT-II_q = 2 Re(exp(-i pi q / 2n) V_q); DST-II_k = DCT-II_{n-1-k}
                 * of the sign-alternated input */
                const long long q = (kind == R2R_RODFT10) ? n - 1 - k : k;
-               const C z = half_spec(Z, n, q), w = r2r_twiddle<C>(q, 4 * n, -1);
+               const C z = half_spec(Z, n, q), w = __ldg(tw + q);
                r = 2 * (w.x * z.x - w.y * z.y);
                break;
           }
@@ -197,10 +242,10 @@ __global__ void k_r2r_post(int kind, long long n, long long L, long long V, cons
                 * RODFT11_k = (-1)^k REDFT11_k of x reversed. */
                if (!(n & 1)) {
                     const long long p = (k & 1) ? (n - 1 - k) >> 1 : k >> 1;
-                    const C z = Z[p], w = r2r_twiddle<C>(p, 2 * n, -1);
+                    const C z = Z[p], w = __ldg(tw + n / 2 + p);
                     r = (k & 1) ? -2 * (z.x * w.y + z.y * w.x) : 2 * (z.x * w.x - z.y * w.y);
                } else {
-                    const C z = Z[k], w = r2r_twiddle<C>(2 * k + 1, 8 * n, -1);
+                    const C z = Z[k], w = __ldg(tw + n + k);
                     r = 2 * (z.x * w.x - z.y * w.y);
                }
                if (kind == R2R_RODFT11 && (k & 1)) r = -r;
@@ -223,8 +268,28 @@ static unsigned r2r_blocks(long long work)
      return (unsigned)b;
 }
 
+/* twiddle-table length of a stage (0: the kind uses none) */
+extern "C" long long gb_r2r_table_len(int kind, long long n)
+{
+     switch (kind) {
+     case R2R_REDFT01: case R2R_REDFT10: case R2R_RODFT01: case R2R_RODFT10: return n;
+     case R2R_REDFT11: case R2R_RODFT11: return (n & 1) ? 2 * n : n;
+     default: return 0;
+     }
+}
+
+extern "C" int gb_r2r_table(int prec, int kind, long long n, void *tab, void *stream)
+{
+     cudaStream_t st = (cudaStream_t)stream;
+     const long long len = gb_r2r_table_len(kind, n);
+     if (len <= 0) return 0;
+     if (prec == 4) k_r2r_table<float2><<<r2r_blocks(len), 256, 0, st>>>(kind, n, len, (float2 *)tab);
+     else k_r2r_table<double2><<<r2r_blocks(len), 256, 0, st>>>(kind, n, len, (double2 *)tab);
+     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 extern "C" int gb_r2r_pre(int prec, int kind, long long n, long long V, const void *in, long long is,
-                          const gb_r2r_vec *vec, void *buf, void *stream)
+                          const gb_r2r_vec *vec, void *buf, const void *tw, void *stream)
 {
      cudaStream_t st = (cudaStream_t)stream;
      long long L;
@@ -232,22 +297,25 @@ extern "C" int gb_r2r_pre(int prec, int kind, long long n, long long V, const vo
      const long long per = core == GB_R2R_CORE_C2R ? L / 2 + 1 : L;
      if (vec->nv < 0 || vec->nv > GB_R2R_MAXV) return -1;
      if (prec == 4)
-          k_r2r_pre<float><<<r2r_blocks(per * V), 256, 0, st>>>(kind, n, L, V, (const float *)in, is, *vec, buf);
+          k_r2r_pre<float><<<r2r_blocks(per * V), 256, 0, st>>>(kind, n, L, V, (const float *)in, is, *vec, buf, tw);
      else
-          k_r2r_pre<double><<<r2r_blocks(per * V), 256, 0, st>>>(kind, n, L, V, (const double *)in, is, *vec, buf);
+          k_r2r_pre<double><<<r2r_blocks(per * V), 256, 0, st>>>(kind, n, L, V, (const double *)in, is, *vec, buf,
+                                                                  tw);
+     gb_count_launch();
      return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 extern "C" int gb_r2r_post(int prec, int kind, long long n, long long V, const void *buf, void *out, long long os,
-                           const gb_r2r_vec *vec, void *stream)
+                           const gb_r2r_vec *vec, const void *tw, void *stream)
 {
      cudaStream_t st = (cudaStream_t)stream;
      long long L;
      gb_r2r_core(kind, n, &L);
      if (vec->nv < 0 || vec->nv > GB_R2R_MAXV) return -1;
      if (prec == 4)
-          k_r2r_post<float><<<r2r_blocks(n * V), 256, 0, st>>>(kind, n, L, V, buf, (float *)out, os, *vec);
+          k_r2r_post<float><<<r2r_blocks(n * V), 256, 0, st>>>(kind, n, L, V, buf, (float *)out, os, *vec, tw);
      else
-          k_r2r_post<double><<<r2r_blocks(n * V), 256, 0, st>>>(kind, n, L, V, buf, (double *)out, os, *vec);
+          k_r2r_post<double><<<r2r_blocks(n * V), 256, 0, st>>>(kind, n, L, V, buf, (double *)out, os, *vec, tw);
+     gb_count_launch();
      return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -56,6 +56,7 @@ typedef struct gb_r2r_axis {
      long long is, os;          /* strides along the dim (reals) */
      int src_mid, dst_mid;      /* read from / write to r2r_mid instead of the caller's arrays */
      gb_r2r_vec vec;
+     void *tw;                  /* device twiddle table of the stage (NULL: none) */
      struct gb_plan *inner;     /* the core transform on r2r_buf[0] -> r2r_buf[1] */
 } gb_r2r_axis;
 

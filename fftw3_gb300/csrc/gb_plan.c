@@ -1189,8 +1189,10 @@ void gb_destroy(gb_plan *p)
      }
      if (p->split_inner) gb_destroy(p->split_inner);
      if (p->r2r_ax) {
-          for (i = 0; i < p->r2r_naxis; ++i)
+          for (i = 0; i < p->r2r_naxis; ++i) {
                if (p->r2r_ax[i].inner) gb_destroy(p->r2r_ax[i].inner);
+               if (p->r2r_ax[i].tw && !gb_dry) cudaFree(p->r2r_ax[i].tw);
+          }
           free(p->r2r_ax);
      }
      for (i = 0; i < 2; ++i)

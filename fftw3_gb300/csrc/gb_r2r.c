@@ -186,6 +186,17 @@ gb_plan *gb_mkr2r(int prec, int rank, const gb_dim *dims, const int *kinds, int 
                gb_destroy(p);
                return 0;
           }
+          if (gb_r2r_table_len(a->kind, a->n) > 0 && !gb_dry_run()) {
+               /* the stage's twiddles, once, on the legacy stream before any execute */
+               const size_t tb = (size_t)gb_r2r_table_len(a->kind, a->n) * 2 * (size_t)prec;
+               if (cudaMalloc(&a->tw, tb) != cudaSuccess || gb_r2r_table(prec, a->kind, a->n, a->tw, 0) ||
+                   cudaStreamSynchronize(0) != cudaSuccess) {
+                    cudaGetLastError();
+                    gb_set_error("r2r twiddle table (%zu bytes) failed", tb);
+                    gb_destroy(p);
+                    return 0;
+               }
+          }
           for (s = 0; s < a->inner->nstep && p->nstep < GB_MAXPASS; ++s) p->step[p->nstep++] = a->inner->step[s];
           p->add += a->inner->add; p->mul += a->inner->mul; p->fma += a->inner->fma;
           if (len < (int)sizeof p->desc)
@@ -275,11 +286,11 @@ int gb_execute_r2r(gb_plan *p, void *in, void *out)
           gb_r2r_axis *a = &p->r2r_ax[i];
           const void *src = a->src_mid ? p->r2r_mid : din;
           void *dst = a->dst_mid ? p->r2r_mid : dout;
-          if (gb_r2r_pre(prec, a->kind, a->n, a->V, src, a->is, &a->vec, p->r2r_buf[0], st)) goto done;
+          if (gb_r2r_pre(prec, a->kind, a->n, a->V, src, a->is, &a->vec, p->r2r_buf[0], a->tw, st)) goto done;
           a->inner->stream = p->stream;
           a->inner->async = 1;
           if (gb_execute(a->inner, p->r2r_buf[0], p->r2r_buf[1])) goto done;
-          if (gb_r2r_post(prec, a->kind, a->n, a->V, p->r2r_buf[1], dst, a->os, &a->vec, st)) goto done;
+          if (gb_r2r_post(prec, a->kind, a->n, a->V, p->r2r_buf[1], dst, a->os, &a->vec, a->tw, st)) goto done;
      }
      if (sout && cudaMemcpyAsync((char *)out + olo * prec, sout, ob, cudaMemcpyDefault, st) != cudaSuccess) goto done;
      if ((sin_ || sout || !p->async) && cudaStreamSynchronize(st) != cudaSuccess) goto done;

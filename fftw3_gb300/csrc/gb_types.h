@@ -162,6 +162,7 @@ int gb_chirp(void *dst, int prec, long long n, int sign, void *stream);
 int gb_device_max_smem(void);
 const char *gb_last_cuda_error(void);
 long long gb_launch_count(void);
+void gb_count_launch(void);   /* one more kernel launched outside gb_launch_pass */
 int gb_device_status(void);
 int *gb_device_status_ptr(void);
 /* r2r transforms (fft_r2r.cu): every kind of length n runs as one core
@@ -202,10 +203,12 @@ typedef struct {
      int nv;
      long long n[GB_R2R_MAXV], is[GB_R2R_MAXV], os[GB_R2R_MAXV];
 } gb_r2r_vec;
+long long gb_r2r_table_len(int kind, long long n);
+int gb_r2r_table(int prec, int kind, long long n, void *tab, void *stream);
 int gb_r2r_pre(int prec, int kind, long long n, long long V, const void *in, long long is, const gb_r2r_vec *vec,
-               void *buf, void *stream);
+               void *buf, const void *tw, void *stream);
 int gb_r2r_post(int prec, int kind, long long n, long long V, const void *buf, void *out, long long os,
-                const gb_r2r_vec *vec, void *stream);
+                const gb_r2r_vec *vec, const void *tw, void *stream);
 
 #ifdef __cplusplus
 }

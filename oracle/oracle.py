@@ -171,6 +171,9 @@ class Reference:
                 f = getattr(lib, pfx + nm)
                 f.restype = vp
                 f.argtypes = [ci, ip, ci, vp, vp, ci, ci, vp, vp, ci, ci, cu]
+            f = getattr(lib, pfx + "plan_many_r2r")
+            f.restype = vp
+            f.argtypes = [ci, ip, ci, vp, vp, ci, ci, vp, vp, ci, ci, ip, cu]
             getattr(lib, pfx + "execute").argtypes = [vp]
             getattr(lib, pfx + "destroy_plan").argtypes = [vp]
             getattr(lib, pfx + "plan_with_nthreads").argtypes = [ci]
@@ -194,6 +197,25 @@ class Reference:
                                       y.ctypes.data, None, 1, tot, sign, flags)
         if not p:
             raise RuntimeError(f"reference could not plan c2c {shape}")
+        self._fn("execute")(p)
+        self._fn("destroy_plan")(p)
+        return y
+
+    def r2r(self, x, n, kind, flags=FFTW_ESTIMATE | FFTW_ALLOW_LARGE_GENERIC):
+        """Batched 1D r2r of length n through the reference's own r2r planner.
+        The codelet-free build plans odd lengths of every kind but REDFT00 and
+        RODFT00 (whose logical sizes 2(n-1), 2(n+1) are even); None when the
+        planner returns NULL."""
+        rt, _ = _PREC[self.prec]
+        x = np.array(x, dtype=rt).ravel()
+        howmany = x.size // int(n)
+        y = np.zeros(x.size, dtype=rt)
+        nn = (ctypes.c_int * 1)(int(n))
+        kk = (ctypes.c_int * 1)(int(kind))
+        p = self._fn("plan_many_r2r")(1, nn, howmany, x.ctypes.data, None, 1, int(n), y.ctypes.data, None, 1,
+                                      int(n), kk, flags)
+        if not p:
+            return None
         self._fn("execute")(p)
         self._fn("destroy_plan")(p)
         return y

@@ -1,7 +1,12 @@
 """The oracle's r2r restatement against the defining sums of the reference
-manual, evaluated independently here with numpy in float64 (CPU only)."""
+manual, evaluated independently here with numpy in float64, and against the
+reference's own r2r planner (oracle/_ref, built from the reference sources
+where they are present) for the lengths its codelet-free build can plan
+(CPU only)."""
 import numpy as np
 import pytest
+
+from oracle.oracle import Reference, ref_available
 
 KINDS = {0: "R2HC", 1: "HC2R", 2: "DHT", 3: "REDFT00", 4: "REDFT01", 5: "REDFT10", 6: "REDFT11", 7: "RODFT00",
          8: "RODFT01", 9: "RODFT10", 10: "RODFT11"}
@@ -68,3 +73,39 @@ def test_r2r_nd_oracle_is_separable(restatement):
     m1 = np.stack([definition(7, e) for e in np.eye(n1)], axis=1)
     ref = np.einsum("ia,bj,tab->tij", m0, m1.T, x)
     assert np.abs(y - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.skipif(not ref_available(), reason="the reference build (oracle/_ref) is not on this machine")
+@pytest.mark.parametrize("kind", [k for k in sorted(KINDS) if k not in (3, 7)], ids=lambda k: KINDS[k])
+@pytest.mark.parametrize("n", [1, 3, 5, 7, 9, 15, 21, 105])
+def test_r2r_oracle_matches_reference(restatement, kind, n):
+    """Pins the restatement to the reference itself: odd lengths of the nine
+    kinds its codelet-free build plans (REDFT00 / RODFT00 have even logical
+    sizes, which that build cannot plan)."""
+    rng = np.random.default_rng(1000 + 16 * n + kind)
+    x = rng.standard_normal(4 * n)
+    ref = Reference("d").r2r(x, n, kind)
+    assert ref is not None, "the reference planner returned NULL"
+    y = restatement.r2r(x, n, kind, "l").astype(np.float64)
+    assert np.abs(y - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.skipif(not ref_available(), reason="the reference build (oracle/_ref) is not on this machine")
+@pytest.mark.parametrize("kind", [3, 7], ids=lambda k: KINDS[k])
+@pytest.mark.parametrize("n", [2, 3, 8, 17, 100])
+def test_r2r_oracle_dct1_dst1_match_reference_dft(restatement, kind, n):
+    """REDFT00 / RODFT00 pinned through the reference's complex DFT of the
+    even / odd extension (logical sizes 2(n-1) / 2(n+1)): DCT-I is the real
+    part of bins 0..n-1, DST-I minus the imaginary part of bins 1..n."""
+    rng = np.random.default_rng(2000 + 16 * n + kind)
+    x = rng.standard_normal((3, n))
+    if kind == 3:
+        ext = np.concatenate([x, x[:, -2:0:-1]], axis=1)
+    else:
+        z = np.zeros((3, 1))
+        ext = np.concatenate([z, x, z, -x[:, ::-1]], axis=1)
+    N = ext.shape[1]
+    full = Reference("d").c2c(ext.astype(np.complex128).ravel(), [N]).reshape(3, N)
+    ref = full[:, :n].real if kind == 3 else -full[:, 1:n + 1].imag
+    y = restatement.r2r(x.ravel(), n, kind, "l").astype(np.float64).reshape(3, n)
+    assert np.abs(y - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max())
