@@ -343,15 +343,18 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.barrier()
     l0 = g.launch_count()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # one event between consecutive steps: the total over K steps is the
+    # reported time; the per-step spread (min, median) is reported beside it
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
+        evs[0].record(stream)
+        for i in range(args.steps):
             step()
-        ev1.record(stream)
+            evs[i + 1].record(stream)
         torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
+    ms = evs[0].elapsed_time(evs[-1])
+    per_step = sorted(evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps))
     launches = g.launch_count() - l0
     fl = flops_per_step(kind, shape, howmany)
     ms, value = aggregate(ms, ws, fl * args.steps, "cuda")
@@ -423,6 +426,7 @@ def run_ours(args):
         out = {
             "metric": METRIC, "value": round(value, 2), "unit": "Gflop/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+            "ms_step_min": round(per_step[0], 4), "ms_step_median": round(statistics.median(per_step), 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if prec == "f" else "f64", "data": "synthetic",
             "config": {"workload": f"{args.workload}: fftw{'f' if prec == 'f' else ''}_plan_many_"
