@@ -1,5 +1,5 @@
 /* Configuration header for compiling the reference FFTW sources into the
- * test-only oracle library (oracle/_ref).  Written for this build: it states
+ * test-only oracle library (oracle/_ref).  Written for this repository: it states
  * the platform facts the reference's sources query (libm long-double trig,
  * posix_memalign, pthreads, gettimeofday) for Linux/gcc on x86_64 or aarch64.
  * Precision is chosen on the command line with -DFFTW_SINGLE / -DFFTW_LDOUBLE
