@@ -109,3 +109,31 @@ def test_r2r_oracle_dct1_dst1_match_reference_dft(restatement, kind, n):
     ref = full[:, :n].real if kind == 3 else -full[:, 1:n + 1].imag
     y = restatement.r2r(x.ravel(), n, kind, "l").astype(np.float64).reshape(3, n)
     assert np.abs(y - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max())
+
+
+def _golden_r2r():
+    import json
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_r2r.npz"))
+    out = []
+    for m in json.loads(bytes(z["meta"]).decode()):
+        k = m["key"]
+        yl = z[k + "_yl_hi"].astype(np.longdouble) + z[k + "_yl_lo"].astype(np.longdouble)
+        out.append(dict(m, x=z[k + "_x"], yd=z[k + "_yd"], yl=yl))
+    return out
+
+
+GOLDEN_R2R = _golden_r2r()
+
+
+@pytest.mark.parametrize("case", GOLDEN_R2R, ids=[f"{KINDS[c['kind']]}-n{c['n']}" for c in GOLDEN_R2R])
+def test_r2r_oracle_matches_reference_golden(restatement, case):
+    """The restatement against the reference's own r2r outputs committed in
+    tests/golden/golden_r2r.npz (gen_golden_r2r.py): double vs the reference's
+    double, long double vs its long double."""
+    x, n, kind = case["x"], case["n"], case["kind"]
+    yd = restatement.r2r(x, n, kind, "d")
+    yl = restatement.r2r(x.astype(np.longdouble), n, kind, "l")
+    scale = max(1.0, float(np.abs(case["yd"]).max()))
+    assert np.abs(yd - case["yd"]).max() <= 1e-14 * scale
+    assert float(np.abs(yl - case["yl"]).max()) <= 1e-17 * scale
