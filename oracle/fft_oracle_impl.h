@@ -650,3 +650,205 @@ int P(r2r)(int kind, I n, I howmany, const R *in, R *out)
      }
      return 0;
 }
+
+/* The same r2r kinds in O(n log n).  DCT/DST-II and -III run as one real
+ * DFT of n (r2r_makhoul), DCT/DST-IV of even n as one complex DFT of n/2
+ * (r2r_dct4_half); every other kind is the real DFT (this file's r2c / c2r
+ * restatement) of a symmetric extension of its input, as the reference's
+ * manual defines the REDFT / RODFT kinds: DFTs of real data with even / odd
+ * symmetry (doc/reference.texi:1923-2300; DCT-I / DST-I as in the
+ * reference's redft00e-r2hc-pad.c and rodft00e-r2hc-pad.c).  Extensions and
+ * the bins read back:
+ *   R2HC / DHT   r2c of n;  HC2R  c2r of the half spectrum
+ *   REDFT00      x even about 0 and n-1: length 2(n-1), Re of bins 0..n-1
+ *   RODFT00      x odd about 0 and n+1:  length 2(n+1), -Im of bins 1..n
+ *   REDFT10      x_j at odd sample 2j+1 of length 4n, even: Re of bins 0..n-1
+ *   RODFT10      the same, odd:                            -Im of bins 1..n
+ *   REDFT01      x_j at sample j of length 4n, even:       Re of odd bins 2k+1
+ *   RODFT01      x_j at sample j+1, odd (x_{n-1} halved at n): -Im of odd bins
+ *   REDFT11      x_j at odd sample 2j+1 of length 8n, even: Re of odd bins 2k+1
+ *   RODFT11      the same, odd:                             -Im of odd bins
+ * Used by the tests at sizes the defining sums cannot reach and as the
+ * host-side timing of r2r.  Returns -1 for a kind out of range or a size-1
+ * REDFT00. */
+/* DCT-II / DST-II (REDFT10 / RODFT10) and DCT-III / DST-III (REDFT01 /
+ * RODFT01) through one real DFT of length n, Makhoul's reduction, the
+ * reduction the reference's reodft010e-r2hc.c:42-83 states (it cites the
+ * same paper): DCT-II of x is 2 Re(exp(-i pi k / 2n) V_k) with V the DFT of
+ * (x_0, x_2, ..., x_3, x_1); DCT-III is its inverse; the DST forms are the
+ * DCT forms of the sign-alternated (II) or reversed (III) data. */
+static void r2r_makhoul(int kind, I n, I howmany, const R *in, R *out, int nthreads)
+{
+     const I nc = n / 2 + 1;
+     R *v = (R *)malloc(sizeof(R) * (size_t)(howmany * n));
+     C *V = (C *)malloc(sizeof(C) * (size_t)(howmany * nc));
+     T *wc = (T *)malloc(sizeof(T) * (size_t)n), *ws = (T *)malloc(sizeof(T) * (size_t)n);
+     I t, j, k;
+     int Ni = (int)n;
+     for (k = 0; k < n; ++k) cexp_t(k, 4 * n, &wc[k], &ws[k]);   /* cos, sin of pi k / 2n */
+     if (kind == 5 || kind == 9) {
+          for (t = 0; t < howmany; ++t)
+               for (j = 0; j < n; ++j) {
+                    R a = in[t * n + j];
+                    if (kind == 9 && (j & 1)) a = -a;
+                    v[t * n + ((j & 1) ? n - 1 - (j >> 1) : (j >> 1))] = a;
+               }
+          P(r2c)(1, &Ni, howmany, v, V, nthreads);
+          for (t = 0; t < howmany; ++t)
+               for (k = 0; k < n; ++k) {
+                    const I q = kind == 9 ? n - 1 - k : k;
+                    const I h = (2 * q <= n) ? q : n - q;
+                    const T zr = V[t * nc + h].re, zi = (2 * q <= n) ? (T)V[t * nc + h].im : -(T)V[t * nc + h].im;
+                    /* exp(-i pi q / 2n) = wc - i ws */
+                    out[t * n + k] = (R)(2 * (wc[q] * zr + ws[q] * zi));
+               }
+     } else {
+          for (t = 0; t < howmany; ++t)
+               for (k = 0; k < nc; ++k) {
+                    const R *x = in + t * n;
+                    const T a = kind == 8 ? (T)x[n - 1 - k] : (T)x[k];
+                    const T b = k == 0 ? 0 : (kind == 8 ? (T)x[k - 1] : (T)x[n - k]);
+                    /* exp(i pi k / 2n) = wc + i ws */
+                    V[t * nc + k].re = (R)(a * wc[k] + b * ws[k]);
+                    V[t * nc + k].im = (R)(a * ws[k] - b * wc[k]);
+               }
+          P(c2r)(1, &Ni, howmany, V, v, nthreads);
+          for (t = 0; t < howmany; ++t)
+               for (k = 0; k < n; ++k) {
+                    R r = v[t * n + ((k & 1) ? n - 1 - (k >> 1) : (k >> 1))];
+                    if (kind == 8 && (k & 1)) r = -r;
+                    out[t * n + k] = r;
+               }
+     }
+     free(v);
+     free(V);
+     free(wc);
+     free(ws);
+}
+
+/* DCT-IV / DST-IV (REDFT11 / RODFT11) of even n through one complex DFT of
+ * n/2, the half-length reduction (the reference's reodft11e-radix2.c
+ * splits the same transform into two halves of n/2): z_m = (x_{2m} +
+ * i x_{n-1-2m}) exp(-i pi (4m+1) / 4n), u_p = Z_p exp(-i pi p / n),
+ * y_{2p} = 2 Re u_p, y_{n-1-2p} = -2 Im u_p; DST-IV is (-1)^k DCT-IV of x
+ * reversed. */
+static void r2r_dct4_half(int kind, I n, I howmany, const R *in, R *out, int nthreads)
+{
+     const I M = n / 2;
+     C *z = (C *)malloc(sizeof(C) * (size_t)(howmany * M));
+     C *Z = (C *)malloc(sizeof(C) * (size_t)(howmany * M));
+     T *w = (T *)malloc(sizeof(T) * (size_t)(4 * M));   /* pre (c, s), post (c, s) per index */
+     I t, m, p;
+     int Mi = (int)M;
+     for (m = 0; m < M; ++m) {
+          cexp_t(4 * m + 1, 8 * n, &w[4 * m], &w[4 * m + 1]);   /* pi (4m+1) / 4n */
+          cexp_t(m, 2 * n, &w[4 * m + 2], &w[4 * m + 3]);       /* pi m / n */
+     }
+     for (t = 0; t < howmany; ++t)
+          for (m = 0; m < M; ++m) {
+               const R *x = in + t * n;
+               const I ja = 2 * m, jb = n - 1 - 2 * m;
+               const T a = kind == 10 ? (T)x[jb] : (T)x[ja], b = kind == 10 ? (T)x[ja] : (T)x[jb];
+               const T c = w[4 * m], s_ = w[4 * m + 1];   /* exp(-i pi (4m+1) / 4n) = c - i s_ */
+               z[t * M + m].re = (R)(a * c + b * s_);
+               z[t * M + m].im = (R)(b * c - a * s_);
+          }
+     P(c2c)(1, &Mi, howmany, z, Z, -1, nthreads);
+     for (t = 0; t < howmany; ++t)
+          for (p = 0; p < M; ++p) {
+               const T zr = Z[t * M + p].re, zi = Z[t * M + p].im;
+               const T c = w[4 * p + 2], s_ = w[4 * p + 3];   /* exp(-i pi p / n) = c - i s_ */
+               T ur, ui;
+               R ye, yo;
+               ur = zr * c + zi * s_;
+               ui = zi * c - zr * s_;
+               ye = (R)(2 * ur);
+               yo = (R)(-2 * ui);
+               /* y_{2p} (even index) and y_{n-1-2p} (odd index: DST-IV flips its sign) */
+               out[t * n + 2 * p] = ye;
+               out[t * n + n - 1 - 2 * p] = kind == 10 ? -yo : yo;
+          }
+     free(z);
+     free(Z);
+     free(w);
+}
+
+int P(r2r_fast)(int kind, I n, I howmany, const R *in, R *out, int nthreads)
+{
+     I N, nc, t, j, k;
+     int Ni;
+     R *ext;
+     C *spec;
+     if (kind < 0 || kind > 10 || (kind == 3 && n < 2)) return -1;
+     if (kind == 4 || kind == 5 || kind == 8 || kind == 9) {
+          r2r_makhoul(kind, n, howmany, in, out, nthreads);
+          return 0;
+     }
+     if ((kind == 6 || kind == 10) && n % 2 == 0) {
+          r2r_dct4_half(kind, n, howmany, in, out, nthreads);
+          return 0;
+     }
+     if (kind == 1) {
+          /* HC2R: the halfcomplex array as the half spectrum, then c2r */
+          nc = n / 2 + 1;
+          spec = (C *)malloc(sizeof(C) * (size_t)(howmany * nc));
+          for (t = 0; t < howmany; ++t)
+               for (k = 0; k < nc; ++k) {
+                    spec[t * nc + k].re = in[t * n + k];
+                    spec[t * nc + k].im = (k == 0 || 2 * k == n) ? 0 : in[t * n + n - k];
+               }
+          Ni = (int)n;
+          P(c2r)(1, &Ni, howmany, spec, out, nthreads);
+          free(spec);
+          return 0;
+     }
+     N = (kind == 0 || kind == 2) ? n : kind == 3 ? 2 * (n - 1) : kind == 7 ? 2 * (n + 1)
+         : (kind == 6 || kind == 10) ? 8 * n : 4 * n;
+     nc = N / 2 + 1;
+     ext = (R *)calloc((size_t)(howmany * N), sizeof(R));
+     spec = (C *)malloc(sizeof(C) * (size_t)(howmany * nc));
+     for (t = 0; t < howmany; ++t) {
+          const R *x = in + t * n;
+          R *e = ext + t * N;
+          for (j = 0; j < n; ++j) {
+               switch (kind) {
+               case 0: case 2: e[j] = x[j]; break;
+               case 3: e[j] = x[j]; if (j > 0 && j < n - 1) e[N - j] = x[j]; break;
+               case 7: e[j + 1] = x[j]; e[N - 1 - j] = -x[j]; break;
+               case 5: e[2 * j + 1] = x[j]; e[N - 2 * j - 1] = x[j]; break;
+               case 9: e[2 * j + 1] = x[j]; e[N - 2 * j - 1] = -x[j]; break;
+               case 4: e[j] = x[j]; if (j > 0) e[N - j] = x[j]; break;
+               case 8:
+                    if (j + 1 < n) { e[j + 1] = x[j]; e[N - j - 1] = -x[j]; }
+                    else { e[n] = x[j] / 2; e[3 * n] = -x[j] / 2; }
+                    break;
+               case 6: e[2 * j + 1] = x[j]; e[N - 2 * j - 1] = x[j]; break;
+               default: e[2 * j + 1] = x[j]; e[N - 2 * j - 1] = -x[j]; break;   /* 10 */
+               }
+          }
+     }
+     Ni = (int)N;
+     P(r2c)(1, &Ni, howmany, ext, spec, nthreads);
+     for (t = 0; t < howmany; ++t) {
+          const C *Y = spec + t * nc;
+          R *y = out + t * n;
+          for (k = 0; k < n; ++k) {
+               switch (kind) {
+               case 0: y[k] = (2 * k <= n) ? Y[k].re : Y[n - k].im; break;
+               case 2: {
+                    const I h = (2 * k <= n) ? k : n - k;
+                    const T im = (2 * k <= n) ? (T)Y[h].im : -(T)Y[h].im;
+                    y[k] = (R)((T)Y[h].re - im);
+                    break;
+               }
+               case 3: case 5: y[k] = Y[k].re; break;
+               case 7: case 9: y[k] = -Y[k + 1].im; break;
+               case 4: case 6: y[k] = Y[2 * k + 1].re; break;
+               default: y[k] = -Y[2 * k + 1].im; break;                         /* 8, 10 */
+               }
+          }
+     }
+     free(ext);
+     free(spec);
+     return 0;
+}

@@ -72,6 +72,8 @@ class Restatement:
                 getattr(lib, f"orc_{p}_dft_method").argtypes = [I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
                 getattr(lib, f"orc_{p}_twiddle").argtypes = [I, I, ctypes.c_int, ctypes.c_void_p]
                 getattr(lib, f"orc_{p}_r2r").argtypes = [ctypes.c_int, I, I, ctypes.c_void_p, ctypes.c_void_p]
+                getattr(lib, f"orc_{p}_r2r_fast").argtypes = [ctypes.c_int, I, I, ctypes.c_void_p, ctypes.c_void_p,
+                                                              ctypes.c_int]
             Restatement._lib = lib
         self.lib = Restatement._lib
 
@@ -118,6 +120,17 @@ class Restatement:
         y = np.empty(x.size, dtype=rt)
         rc = getattr(self.lib, f"orc_{prec}_r2r")(int(kind), int(n), x.size // int(n), x.ctypes.data, y.ctypes.data)
         assert rc == 0, f"r2r kind {kind} is not restated"
+        return y
+
+    def r2r_fast(self, x, n, kind, prec="d", nthreads=1):
+        """Batched 1D r2r of length n in O(n log n): the real DFT of the
+        kind's symmetric extension (same results as r2r, for large n)."""
+        rt, _ = _PREC[prec]
+        x = _as(x, rt)
+        y = np.empty(x.size, dtype=rt)
+        rc = getattr(self.lib, f"orc_{prec}_r2r_fast")(int(kind), int(n), x.size // int(n), x.ctypes.data,
+                                                       y.ctypes.data, int(nthreads))
+        assert rc == 0, f"r2r kind {kind} of size {n} is not defined"
         return y
 
     def r2r_nd(self, x, shape, kinds, prec="d"):

@@ -137,3 +137,20 @@ def test_r2r_oracle_matches_reference_golden(restatement, case):
     scale = max(1.0, float(np.abs(case["yd"]).max()))
     assert np.abs(yd - case["yd"]).max() <= 1e-14 * scale
     assert float(np.abs(yl - case["yl"]).max()) <= 1e-17 * scale
+
+
+@pytest.mark.parametrize("kind", sorted(KINDS), ids=[KINDS[k] for k in sorted(KINDS)])
+def test_r2r_fast_oracle_matches_defining_sums(restatement, kind):
+    """The O(n log n) restatement (real DFT of the symmetric extension)
+    against the defining sums, and against the reference's golden outputs."""
+    for n in (1, 2, 3, 4, 7, 16, 33, 100, 257):
+        if kind == 3 and n == 1:
+            continue
+        x = np.random.default_rng(3000 + 16 * n + kind).standard_normal(3 * n)
+        ref = restatement.r2r(x.astype(np.longdouble), n, kind, "l").astype(np.float64)
+        y = restatement.r2r_fast(x, n, kind, "d")
+        assert np.abs(y - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max()), n
+    for case in GOLDEN_R2R:
+        if case["kind"] == kind:
+            y = restatement.r2r_fast(case["x"], case["n"], kind, "d")
+            assert np.abs(y - case["yd"]).max() <= 1e-14 * max(1.0, float(np.abs(case["yd"]).max()))
