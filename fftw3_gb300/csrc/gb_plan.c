@@ -1025,8 +1025,9 @@ static void describe(gb_plan *p)
                           P->variant == GB_VAR_TC ? "tc-split-fp16" : "gen", P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
                           P->vn[0], P->post_N ? " +twiddle" : "");
+          if (off >= (int)sizeof p->desc) off = (int)sizeof p->desc - 1;   /* truncated */
      }
-     snprintf(p->desc + off, sizeof p->desc - off, ")");
+     if (off < (int)sizeof p->desc - 1) snprintf(p->desc + off, sizeof p->desc - off, ")");
 }
 
 /* Build the steps of a problem.  Returns NULL (with gb_last_error set) when

@@ -210,3 +210,13 @@ def test_r2r_stages_per_dim():
     i2, i1, i0 = d.index("(dim 2 kind 1"), d.index("(dim 1 kind 10"), d.index("(dim 0 kind 3")
     assert i2 < i1 < i0
     assert "rdft2-c2r" in d[i2:i1] and "n=10" in d[i1:i0] and "r2c n=10" in d[i0:]
+
+
+def test_long_description_is_truncated_not_overflowed():
+    """A plan with many passes (3D r2c whose axes all run as multi-pass
+    convolutions) describes itself within the fixed description buffer."""
+    p = g.plan_many_dft_r2c([4099, 2049, 17], 1, 1 << 20, 1 << 36, prec="d", istride=2,
+                            idist=2 * 4099 * 2049 * 17)
+    d = p.describe()
+    assert d.startswith("(gb300-rdft2-r2c-f64") and len(d) <= 1023
+    assert len(p.passes()) > 6
