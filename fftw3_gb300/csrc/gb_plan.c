@@ -1113,8 +1113,10 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
           }
      } else {
           /* multi-dimensional c2r works in place on its input; like the
-           * reference, no input-preserving algorithm exists for it */
-          if (r > 1 && (flags & FFTW_PRESERVE_INPUT)) {
+           * reference, no input-preserving algorithm exists for it out of
+           * place, while an in-place problem overwrites its input anyway
+           * (rdft/rank-geq2-rdft2.c:118-124) */
+          if (r > 1 && (flags & FFTW_PRESERVE_INPUT) && prb->in != prb->out) {
                gb_set_error("multi-dimensional c2r cannot preserve its input");
                free(p);
                return 0;

@@ -45,6 +45,19 @@ def build(ref: bool = False) -> None:
                         "REF=" + os.environ.get("FFTW_REF_SRC", "/root/reference")], check=True)
 
 
+def harness() -> str | None:
+    """Build the reference's own benchmark harness (tests/bench.c +
+    libbench2) against this library's fftw3.h and libfftw3_gb300.so, where
+    the reference sources exist; returns the executable's path, else None.
+    The executable answers `--can-do <problem>` from this library's planner
+    in dry-run mode (oracle/ref/harness_shim.c)."""
+    src = os.environ.get("FFTW_REF_SRC", "/root/reference")
+    if not os.path.isfile(os.path.join(src, "tests", "bench.c")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "harness", "REF=" + src], check=True)
+    return os.path.join(REFDIR, "bench_gb300")
+
+
 def ref_available() -> bool:
     return all(os.path.exists(os.path.join(REFDIR, f"libfftw3_ref{p}.so")) for p in ("", "f", "l"))
 

@@ -220,3 +220,14 @@ def test_long_description_is_truncated_not_overflowed():
     d = p.describe()
     assert d.startswith("(gb300-rdft2-r2c-f64") and len(d) <= 1023
     assert len(p.passes()) > 6
+
+
+def test_c2r_multid_preserve_input_in_place(lib):
+    """The reference plans an in-place multi-dimensional c2r under
+    FFTW_PRESERVE_INPUT (the input is overwritten by definition,
+    rdft/rank-geq2-rdft2.c:118-124); out of place it returns NULL."""
+    f = lib.fftwf_plan_dft_c2r_2d
+    f.restype = ctypes.c_void_p
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint]
+    assert f(64, 64, 1 << 20, 1 << 20, g.FFTW_ESTIMATE | g.FFTW_PRESERVE_INPUT)
+    assert not f(64, 64, 1 << 20, 1 << 30, g.FFTW_ESTIMATE | g.FFTW_PRESERVE_INPUT)
