@@ -34,7 +34,7 @@ def _worker(rank, ws, port, out):
 def test_two_rank_aggregate_max_time_and_total_work():
     ws = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:   # no fork of a process that may hold threads
         out = m.dict()
         mp.spawn(_worker, args=(ws, port, out), nprocs=ws, join=True)
         res = dict(out)
