@@ -45,15 +45,22 @@ def build(ref: bool = False) -> None:
                         "REF=" + os.environ.get("FFTW_REF_SRC", "/root/reference")], check=True)
 
 
+def ref_source(rel: str) -> str | None:
+    """Path of a file of the reference checkout (FFTW_REF_SRC), or None
+    where the reference sources are absent."""
+    path = os.path.join(os.environ.get("FFTW_REF_SRC", "/root/reference"), rel)
+    return path if os.path.isfile(path) else None
+
+
 def harness() -> str | None:
     """Build the reference's own benchmark harness (tests/bench.c +
     libbench2) against this library's fftw3.h and libfftw3_gb300.so, where
     the reference sources exist; returns the executable's path, else None.
     The executable answers `--can-do <problem>` from this library's planner
     in dry-run mode (oracle/ref/harness_shim.c)."""
-    src = os.environ.get("FFTW_REF_SRC", "/root/reference")
-    if not os.path.isfile(os.path.join(src, "tests", "bench.c")):
+    if ref_source(os.path.join("tests", "bench.c")) is None:
         return None
+    src = os.environ.get("FFTW_REF_SRC", "/root/reference")
     subprocess.run(["make", "-s", "-C", HERE, "harness", "REF=" + src], check=True)
     return os.path.join(REFDIR, "bench_gb300")
 

@@ -107,3 +107,18 @@ def test_threads_api(lib):
     assert lib.fftwf_planner_nthreads() == 8
     lib.fftwf_plan_with_nthreads(1)
     lib.fftw_cleanup_threads()
+
+
+def test_header_declares_exactly_the_reference_api():
+    """include/fftw3.h declares the same function and data names as the
+    reference's FFTW_DEFINE_API list (api/fftw3.h:127-466), no more, no less."""
+    from oracle.oracle import ref_source
+    path = ref_source(os.path.join("api", "fftw3.h"))
+    if path is None:
+        pytest.skip("the reference sources are not on this machine")
+    ref = open(path).read()
+    body = ref[ref.index("#define FFTW_DEFINE_API"):ref.index("FFTW_DEFINE_API(FFTW_MANGLE_DOUBLE")]
+    want = set(re.findall(r"X\((\w+)\)\s*[\(\[]", body))
+    ours = open(os.path.join(ROOT, "include", "fftw3.h")).read()
+    have = set(re.findall(r"PFX##(\w+)\s*[\(\[]", ours))
+    assert len(want) > 70 and want == have, (sorted(want - have), sorted(have - want))
