@@ -19,7 +19,7 @@
  * so nothing is allocated when it runs.  The array's size is the limit:
  * n * howmany <= FFTWF_GB300_NOALLOC_MAX_POINTS (2^21 complex floats,
  * 16 MiB), and every GPU the entry point runs on holds the array (16 MiB +
- * 33 KiB) until the process exits.
+ * 48.25 KiB of status word and twiddle tables) until the process exits.
  *
  * Set-up: the first call on each device, with that device current, looks up
  * the array's device address (cudaGetSymbolAddress), which can load this
@@ -47,9 +47,27 @@ namespace {
 
 constexpr long long kMaxPoints = FFTWF_GB300_NOALLOC_MAX_POINTS;
 constexpr int kStatusWords = 32;     /* 256 bytes: the status word, padded so the tables start aligned */
-constexpr int kTableWords = 4096;    /* n1 + n2 + S + ceil(n/S) <= 1024 + 2048 + 2048 + 1024 for n <= 2^21 */
 constexpr int kMinLog = 12, kMaxLog = 21;
 constexpr int kMaxDevices = 64;
+
+/* Table entries one call of length 2^L needs: n1 + n2 + S + ceil(n / S),
+ * with n1 = 2^(L/2), n2 = n / n1 and S the least power of two whose square
+ * reaches n (the same split the entry point uses). */
+constexpr long long table_words(int L)
+{
+     return (1LL << (L / 2)) + (1LL << (L - L / 2)) + (1LL << ((L + 1) / 2)) +
+            ((1LL << L) + (1LL << ((L + 1) / 2)) - 1) / (1LL << ((L + 1) / 2));
+}
+constexpr long long max_table_words(int L)
+{
+     return L > kMaxLog ? 0 : (table_words(L) > max_table_words(L + 1) ? table_words(L) : max_table_words(L + 1));
+}
+/* 6144 entries (at n = 2^21: 1024 + 2048 + 2048 + 1024), rounded up to a
+ * multiple of 32 so the scratch that follows stays 256-byte aligned */
+constexpr int kTableWords = (int)((max_table_words(kMinLog) + 31) / 32 * 32);
+static_assert(table_words(21) == 6144 && table_words(20) == 4096 && table_words(12) == 256,
+              "table layout of the four-step split");
+static_assert(kTableWords >= max_table_words(kMinLog), "tables must not reach into the scratch region");
 
 }  // namespace
 
@@ -180,6 +198,10 @@ extern "C" int fftwf_gb300_dft_1d_noalloc(int n, int howmany, const fftwf_comple
      long long S = 1;
      int lS = 0;
      while (S * S < n) { S <<= 1; ++lS; }
+     if (n1 + n2 + S + (n + S - 1) / S > kTableWords) {
+          gb_set_error("fftwf_gb300_dft_1d_noalloc: internal: tables of n = %d exceed the fixed table region", n);
+          return -1;
+     }
      float2 *status = area, *tw1 = area + kStatusWords, *tw2 = tw1 + n1, *lo = tw2 + n2, *hi = lo + S;
      float2 *mid = area + kStatusWords + kTableWords;
 

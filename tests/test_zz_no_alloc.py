@@ -91,3 +91,23 @@ def test_noalloc_in_place_and_limits(lib, torch_cuda):
     assert lib.fftwf_gb300_dft_1d_noalloc(1 << 22, 0, x.data_ptr(), x.data_ptr(), -1, st) == -1
     assert lib.fftw_gb300_launch_count() == before
     assert MAX_POINTS == n * hm
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_noalloc_every_length(lib, torch_cuda, sign):
+    """Every length the entry point accepts, one transform each (n = 2^21
+    uses the largest twiddle tables, right below the scratch region), and
+    2^19 with several transforms; each call follows the previous one on the
+    same stream, so every call meets the array as its predecessor left it."""
+    torch = torch_cuda
+    cases = [(1 << L, 1) for L in range(12, 22)] + [(1 << 19, 4)]
+    xs = [_input(torch, n, hm, 300 + 7 * i + (sign > 0)) for i, (n, hm) in enumerate(cases)]
+    ys = [torch.empty_like(x) for x in xs]
+    for (n, hm), x, y in zip(cases, xs, ys):
+        _noalloc(lib, torch, x, y, n, hm, sign)
+    torch.cuda.synchronize()
+    for (n, hm), x, y in zip(cases, xs, ys):
+        ref = _planned(torch, x, n, hm, sign)
+        err = rel_l2(y.cpu().numpy(), ref)
+        assert err <= TOL, f"n={n} howmany={hm} sign={sign}: rel L2 {err:.3e}"
+
