@@ -126,6 +126,8 @@ def load(path: str | None = None):
     lib.fftw_gb300_failures.restype = ci
     lib.fftw_gb300_set_dry_run.argtypes = [ci]
     lib.fftw_gb300_launch_count.restype = ctypes.c_longlong
+    lib.fftw_gb300_fp64_fma_gflops.restype = ctypes.c_double
+    lib.fftw_gb300_fp64_fma_gflops.argtypes = []
     lib.fftwf_gb300_dft_1d_noalloc.restype = ci
     lib.fftwf_gb300_dft_1d_noalloc.argtypes = [ci, ci, vp, vp, ci, vp]
     _lib = lib

@@ -350,8 +350,37 @@ __device__ __forceinline__ void reg_gather(C (&x)[reg_e(N)], int tid, const C *s
      }
 }
 
-template <typename C, int N, int DIR, int NS>
-__device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, const C *__restrict__ tw)
+/* Barriers of the stage exchanges: the whole CTA, or one of two groups of
+ * threads of a CTA that runs independent groups (named barriers 1 and 2,
+ * immediate ids so the kernel reserves three barriers, not sixteen). */
+struct cta_sync {
+     __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct group_sync {
+     unsigned id, n;   /* id 1 or 2; n threads, a multiple of 32 */
+     __device__ __forceinline__ void operator()() const
+     {
+          if (id == 1) asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory");
+          else asm volatile("bar.sync 2, %0;" ::"r"(n) : "memory");
+     }
+};
+
+/* AND of v over the n threads of named barrier id (1 or 2; a barrier as well) */
+__device__ __forceinline__ bool group_and(unsigned id, unsigned n, bool v)
+{
+     unsigned r;
+     if (id == 1)
+          asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}"
+                       : "=r"(r) : "r"((unsigned)v), "r"(n) : "memory");
+     else
+          asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 2, %2, p;\n selp.u32 %0, 1, 0, q;\n}"
+                       : "=r"(r) : "r"((unsigned)v), "r"(n) : "memory");
+     return r != 0;
+}
+
+template <typename C, int N, int DIR, int NS, typename S = cta_sync>
+__device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, const C *__restrict__ tw,
+                                           const S &sync = S())
 {
      constexpr int E = reg_e(N);
      constexpr int T = N / E;
@@ -390,10 +419,10 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
           }
      }
      if constexpr (!LAST) {
-          __syncthreads();
+          sync();
           reg_gather<C, N>(x, tid, smt);
-          __syncthreads();
-          reg_stages<C, N, DIR, NS * RAD>(x, tid, smt, tw);
+          sync();
+          reg_stages<C, N, DIR, NS * RAD, S>(x, tid, smt, tw, sync);
      }
 }
 
@@ -594,11 +623,22 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
 
 /* ======================================================================
  * k_reg_tma: persistent variant of k_reg for unit-stride c2c and r2c
- * batches whose transforms start on 16-byte boundaries.  Each CTA walks its tiles with a
- * two-slot pipeline: while the tile in one shared-memory slot is being
- * transformed, the TMA engine copies the next tile into the other slot
- * (cp.async.bulk, completion tracked by an mbarrier), so HBM reads overlap
- * the arithmetic.  Results are stored straight from registers.
+ * batches whose transforms start on 16-byte boundaries.
+ *
+ * A CTA runs G independent compute groups (tma_threads(nfft) threads each,
+ * synchronised by their own named barrier) over G + 1 shared-memory
+ * buffers of one tile each.  The CTA's tiles are i = 0, 1, 2, ... (global
+ * tile blockIdx.x + i * gridDim.x); tile i is transformed by group i mod G
+ * in buffer i mod (G + 1).  The TMA engine copies each tile into its buffer
+ * (cp.async.bulk, completion on the buffer's mbarrier): the first G + 1
+ * tiles at start, and tile i + G + 1 as soon as the group that transformed
+ * tile i has last read that buffer.  So while every group transforms a
+ * tile, one more tile is on its way, and a group finds its next tile
+ * already resident.  Results are stored straight from registers.
+ * One group per CTA (two buffers) leaves each thread 85 registers and puts
+ * three CTAs of 256 threads on an SM; two groups (float only: 64 registers a
+ * thread) put two CTAs of 2 x 256 threads on an SM, four transforms of 4096
+ * in flight against three.  The planner picks the count per length.
  * ==================================================================== */
 
 __host__ __device__ constexpr int tma_sms(int nfft) { return reg_sms(nfft); }
@@ -622,13 +662,23 @@ __device__ __forceinline__ void tma_issue(const gb_pass &P, const void *in, long
      }
 }
 
-/* threads per CTA of k_reg_tma: 256, or one transform's T when larger */
+/* threads of one compute group of k_reg_tma: 256, or one transform's T when larger */
 __host__ __device__ constexpr int tma_threads(int nfft) { return (nfft / reg_e(nfft)) > 256 ? (nfft / reg_e(nfft)) : 256; }
+
+/* most compute groups per CTA of k_reg_tma (complex element size csize) */
+__host__ __device__ constexpr int tma_max_groups(int csize) { return csize == 8 ? 2 : 1; }
+
+/* CTAs per SM the register budget is sized for: 64 registers a thread for
+ * two groups, 85 for one group of 256 threads */
+__host__ __device__ constexpr int tma_minblocks(int nfft, int G)
+{
+     return G * tma_threads(nfft) >= 1024 ? 1 : G == 2 ? 2 : (tma_threads(nfft) > 256 ? 1 : 3);
+}
 
 #define GB_WAIT_NS 2000000000ull   /* bound on any wait for a copy: 2 s */
 
-template <typename C, int LOGN, int DIR, int KIND>
-__global__ void __launch_bounds__(tma_threads(1 << LOGN), tma_threads(1 << LOGN) > 256 ? 1 : 3)
+template <typename C, int LOGN, int DIR, int KIND, int G>
+__global__ void __launch_bounds__(G * tma_threads(1 << LOGN), tma_minblocks(1 << LOGN, G))
 k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
 {
      typedef typename real_of<C>::T R;
@@ -636,62 +686,83 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
      constexpr int E = reg_e(N);
      constexpr int T = N / E;
      constexpr int SMS = tma_sms(N);
+     constexpr int NB = G + 1;
      extern __shared__ __align__(128) unsigned char gb_smem[];
-     __shared__ __align__(8) unsigned long long bar[2];
-     C *const buf0 = (C *)gb_smem;
-     C *const buf1 = buf0 + P.tb * SMS;
-     const int tl = threadIdx.x / T;
-     const int tid = threadIdx.x - tl * T;
+     __shared__ __align__(8) unsigned long long full[NB];
+     __shared__ int issued[NB], consumed[NB];
+     const int GT = P.threads;                /* threads of one group */
+     const int g = (int)threadIdx.x / GT;
+     const int gtid = (int)threadIdx.x - g * GT;
+     const int tl = gtid / T;
+     const int tid = gtid - tl * T;
+     const int tile_elems = P.tb * SMS;
+     C *const base = (C *)gb_smem;
      const C *__restrict__ tw = (const C *)P.tw;
+     const group_sync gs = {(unsigned)(1 + g), (unsigned)GT};
+     const long long stride = gridDim.x;
 
      if (threadIdx.x == 0) {
-          mbar_init(&bar[0], 1);
-          mbar_init(&bar[1], 1);
+#pragma unroll
+          for (int b = 0; b < NB; ++b) {
+               mbar_init(&full[b], 1);
+               issued[b] = 0;
+               consumed[b] = 0;
+          }
           mbar_fence_init();
      }
      __syncthreads();
-     const long long stride = gridDim.x;
-     long long blk = blockIdx.x;
-     if (threadIdx.x == 0 && blk < P.nblocks) tma_issue<C, N, KIND>(P, in, blk, buf0, &bar[0]);
-     unsigned parity = 0;   /* bit b: parity of the next phase of bar[b] */
-
-     for (int it = 0; blk < P.nblocks; blk += stride, ++it) {
-          const int b = it & 1;
-          C *const cur = b ? buf1 : buf0;
-          const long long nxt = blk + stride;
-          const bool issued = nxt < P.nblocks;
-          if (threadIdx.x == 0 && issued) {
-               fence_proxy_async_smem();
-               tma_issue<C, N, KIND>(P, in, nxt, b ? buf0 : buf1, &bar[b ^ 1]);
-          }
-          const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u, GB_WAIT_NS);
-          if (!__syncthreads_and(ok)) {
-               /* the copy never completed: report, drain the other slot, leave */
-               if (threadIdx.x == 0) {
-                    if (issued) mbar_wait(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u, GB_WAIT_NS);
-                    if (P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
+     if (threadIdx.x == 0) {
+#pragma unroll
+          for (int b = 0; b < NB; ++b) {
+               const long long blk = blockIdx.x + b * stride;
+               if (blk < P.nblocks) {
+                    tma_issue<C, N, KIND>(P, in, blk, base + b * tile_elems, &full[b]);
+                    issued[b] = 1;
                }
-               return;
           }
-          parity ^= 1u << b;
+     }
 
+     for (int i = g;; i += G) {
+          const long long blk = blockIdx.x + (long long)i * stride;
+          if (blk >= P.nblocks) break;
+          const int b = i % NB;
+          const unsigned parity = (unsigned)((i / NB) & 1);
+          C *const cur = base + b * tile_elems;
+          if (!group_and(gs.id, gs.n, mbar_wait(&full[b], parity, GB_WAIT_NS))) {
+               /* the copy never completed: report and leave (the copies still
+                * in flight are drained below) */
+               if (gtid == 0 && P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
+               break;
+          }
+          if (gtid == 0) atomicAdd(&consumed[b], 1);
+          C x[E];
+          {
+               const C *s0 = cur + tl * SMS + tid;
+#pragma unroll
+               for (int e = 0; e < E; ++e) x[e] = s0[T * e];
+          }
+          gs();
+          reg_stages<C, N, DIR, 1, group_sync>(x, tid, cur + tl * SMS, tw, gs);
+          /* (the tile's indices are formed after the stages, which need every
+           * register they can get) */
+          C *smt = cur + tl * SMS;
+          /* the tile of buffer b after this one: issued by this group once it
+           * has last read the buffer */
+          const long long nxt = blk + NB * stride;
           const tile_t tile = tile_of(P, blk);
           const long long v = tile.v0 + tl;
           const bool valid = v < P.vn[0];
           const long long bo = tile.bo + v * P.vos[0];
-          C *smt = cur + tl * SMS;
-          C x[E];
-#pragma unroll
-          for (int e = 0; e < E; ++e) x[e] = smt[tid + T * e];
-          __syncthreads();
-          reg_stages<C, N, DIR, 1>(x, tid, smt, tw);
           if constexpr (KIND == GB_KIND_R2C) {
                /* hc2c post-pass (rdft/ct-hc2c.c:197-210):
                 * X[k] = (Z[k] + conj Z[N-k])/2 + W_2N^k (Z[k] - conj Z[N-k])/(2i) */
 #pragma unroll
                for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
-               __syncthreads();
+               gs();
+               /* each output straight to HBM as it is formed (no array of
+                * results held across the loop) */
                const C *__restrict__ th = (const C *)P.tw_half;
+               C *o = (C *)out + bo + tid;
 #pragma unroll
                for (int e = 0; e < E; ++e) {
                     const int k = tid + T * e;
@@ -699,17 +770,26 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
                     bq.y = -bq.y;
                     const C ev = cscale(cadd(a, bq), (R)0.5), dd = csub(a, bq);
                     const C od = mk<C>(dd.y * (R)0.5, -dd.x * (R)0.5);
-                    x[e] = cadd(ev, cmul(__ldg(th + k), od));
+                    if (valid) o[T * e] = cadd(ev, cmul(__ldg(th + k), od));
                }
-               const C z0 = smt[pad_for(N, 0)];
-               if (valid) {
-                    C *o = (C *)out + bo + tid;
-#pragma unroll
-                    for (int e = 0; e < E; ++e) o[T * e] = x[e];
-                    if (tid == 0) o[N] = mk<C>(z0.x - z0.y, 0);
+               if (valid && tid == 0) {
+                    const C z0 = smt[pad_for(N, 0)];
+                    o[N] = mk<C>(z0.x - z0.y, 0);
                }
-               __syncthreads();   /* the slot is the next bulk copy's target */
+               gs();   /* the buffer is the next bulk copy's target */
+               if (gtid == 0 && nxt < P.nblocks) {
+                    fence_proxy_async_smem();
+                    tma_issue<C, N, KIND>(P, in, nxt, cur, &full[b]);
+                    atomicAdd(&issued[b], 1);
+               }
           } else {
+               /* every thread of the group is past the barrier that follows
+                * the last read of the buffer (inside the stages) */
+               if (gtid == 0 && nxt < P.nblocks) {
+                    fence_proxy_async_smem();
+                    tma_issue<C, N, KIND>(P, in, nxt, cur, &full[b]);
+                    atomicAdd(&issued[b], 1);
+               }
                if (P.post_N) {
                     apply_post_twiddles<C, E, T>(P, P.post_vdim ? tile.vpost : v, tid, x);
                }
@@ -720,6 +800,14 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
                     for (int e = 0; e < E; ++e) o[T * e] = x[e];
                }
           }
+     }
+     /* a group that gave up may leave copies in flight: wait (bounded) for
+      * each before the CTA's shared memory is released */
+     __syncthreads();
+     if (threadIdx.x == 0) {
+#pragma unroll
+          for (int b = 0; b < NB; ++b)
+               if (issued[b] > consumed[b]) mbar_wait(&full[b], (unsigned)((issued[b] - 1) & 1), GB_WAIT_NS);
      }
 }
 

@@ -14,12 +14,13 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
+#include <pthread.h>
 #include "fft_kernels.cuh"
 
 extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir);
 extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
-extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir);
-extern "C" const void *gb_tma_kernel_d(int logn, int kind, int dir);
+extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir, int groups);
+extern "C" const void *gb_tma_kernel_d(int logn, int kind, int dir, int groups);
 extern "C" const void *gb_tc_kernel(int nfft, int dir);
 extern "C" const void *gb_cols_tma_kernel(int logn, int dir);
 extern "C" int gb_tc_smem(int nfft);
@@ -309,11 +310,19 @@ static const void *pick_kernel(const gb_pass *p)
           while ((1 << logn) < p->nfft) ++logn;
           if (p->variant == GB_VAR_TMA)
                return (p->kind == GB_KIND_C2C || p->kind == GB_KIND_R2C)
-                           ? (p->prec == 4 ? gb_tma_kernel_f(logn, p->kind, p->sign) : gb_tma_kernel_d(logn, p->kind, p->sign))
+                           ? (p->prec == 4 ? gb_tma_kernel_f(logn, p->kind, p->sign, p->groups)
+                                           : gb_tma_kernel_d(logn, p->kind, p->sign, p->groups))
                            : 0;
           return p->prec == 4 ? gb_reg_kernel_f(logn, p->kind, p->sign) : gb_reg_kernel_d(logn, p->kind, p->sign);
      }
      return p->prec == 4 ? (const void *)k_gen<float2> : (const void *)k_gen<double2>;
+}
+
+/* Threads of one CTA: a k_reg_tma CTA runs p->groups groups of p->threads
+ * threads. */
+static int cta_threads(const gb_pass *p)
+{
+     return p->variant == GB_VAR_TMA ? p->groups * p->threads : p->threads;
 }
 
 /* Number of CTAs launched for a pass: all tiles, capped; kernels stride over
@@ -326,7 +335,7 @@ static unsigned grid_of(const gb_pass *p, const void *fn)
           int dev = 0, sms = 0, per = 0;
           cudaGetDevice(&dev);
           cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-          const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, p->threads, (size_t)p->smem);
+          const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, cta_threads(p), (size_t)p->smem);
           if (gb_trace)
                fprintf(stderr, "[fftw_gb300] occupancy of variant %d: %d CTAs/SM (%s)\n", p->variant, per, cudaGetErrorString(e));
           if (e != cudaSuccess) {
@@ -346,25 +355,55 @@ static unsigned grid_of(const gb_pass *p, const void *fn)
      return (unsigned)g;
 }
 
-/* One device word where kernels report a bounded wait that gave up. */
-static int *gb_status_word = 0;
+/* One word per device where that device's kernels report a bounded wait
+ * that gave up (a kernel may only write its own device's word: another
+ * device's memory is not reachable without peer access). */
+#define GB_MAX_DEVICES 64
+static int *gb_status_word[GB_MAX_DEVICES];
+static pthread_mutex_t gb_status_mtx = PTHREAD_MUTEX_INITIALIZER;
 
-extern "C" int *gb_device_status_ptr(void)
+static int current_device(void)
 {
-     if (!gb_status_word) {
-          if (cudaMalloc((void **)&gb_status_word, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return 0; }
-          cudaMemset(gb_status_word, 0, sizeof(int));
+     int dev = -1;
+     if (cudaGetDevice(&dev) != cudaSuccess) {
+          cudaGetLastError();
+          return -1;
      }
-     return gb_status_word;
+     return (dev >= 0 && dev < GB_MAX_DEVICES) ? dev : -1;
 }
 
-/* Read and clear the device status word (0 = no kernel reported a problem). */
+/* The current device's status word, allocated (and cleared) on first use. */
+extern "C" int *gb_device_status_ptr(void)
+{
+     const int dev = current_device();
+     int *w;
+     if (dev < 0) return 0;
+     w = __atomic_load_n(&gb_status_word[dev], __ATOMIC_ACQUIRE);
+     if (w) return w;
+     pthread_mutex_lock(&gb_status_mtx);
+     w = gb_status_word[dev];
+     if (!w) {
+          if (cudaMalloc((void **)&w, sizeof(int)) != cudaSuccess || cudaMemset(w, 0, sizeof(int)) != cudaSuccess) {
+               cudaGetLastError();
+               w = 0;
+          } else {
+               __atomic_store_n(&gb_status_word[dev], w, __ATOMIC_RELEASE);
+          }
+     }
+     pthread_mutex_unlock(&gb_status_mtx);
+     return w;
+}
+
+/* Read and clear the current device's status word (0 = no kernel on this
+ * device reported a problem since the last read). */
 extern "C" int gb_device_status(void)
 {
+     const int dev = current_device();
      int v = 0, z = 0;
-     if (!gb_status_word) return 0;
-     if (cudaMemcpy(&v, gb_status_word, sizeof v, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
-     cudaMemcpy(gb_status_word, &z, sizeof z, cudaMemcpyHostToDevice);
+     int *w = dev >= 0 ? __atomic_load_n(&gb_status_word[dev], __ATOMIC_ACQUIRE) : 0;
+     if (!w) return 0;
+     if (cudaMemcpy(&v, w, sizeof v, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+     cudaMemcpy(w, &z, sizeof z, cudaMemcpyHostToDevice);
      return v;
 }
 
@@ -481,11 +520,13 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->post_N && (p->post_lS < 0 || (1LL << p->post_lS) != p->post_S || p->post_S * p->post_S < p->post_N))
                bad = "four-step twiddle table split is inconsistent";
           else if (p->variant == GB_VAR_REG && p->smem < p->tb * reg_sms(p->nfft) * 2 * p->prec) bad = "shared memory too small for the tile";
-          else if (p->variant == GB_VAR_TMA && (p->threads > tma_threads(p->nfft) || p->is != 1 || p->os != 1 ||
+          else if (p->variant == GB_VAR_TMA && (p->threads > tma_threads(p->nfft) || p->threads % 32 || p->is != 1 || p->os != 1 ||
                                                 (p->kind != GB_KIND_C2C && p->kind != GB_KIND_R2C) ||
                                                 (p->kind == GB_KIND_R2C && p->n != 2 * p->nfft) ||
-                                                p->smem < 2 * p->tb * tma_sms(p->nfft) * 2 * p->prec))
-               bad = "persistent bulk-copy pass needs unit-stride c2c/r2c in and out and two smem slots";
+                                                p->groups < 1 || p->groups > gb_tma_max_groups(p->prec) ||
+                                                p->groups * p->threads > 1024 ||
+                                                p->smem < (p->groups + 1) * p->tb * tma_sms(p->nfft) * 2 * p->prec))
+               bad = "persistent bulk-copy pass needs unit-stride c2c/r2c in and out and one smem buffer per group and one more";
           else if (p->variant == GB_VAR_TMA && ((uintptr_t)in % 16 != 0)) bad = "bulk copies need a 16-byte aligned input";
           else if (p->variant == GB_VAR_TMA_COLS && !cols_tma_ok(p, in))
                bad = "tensor-map column pass needs f32 c2c column tiles of 2..128 columns, 16..2048 points, even positive "
@@ -534,8 +575,8 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
      const unsigned grid = grid_of(p, fn);
      if (gb_trace)
           fprintf(stderr, "[fftw_gb300] launch kind %d variant %d nfft %d tb %d: grid %u x %d threads, %d B smem\n",
-                  p->kind, p->variant, p->nfft, p->tb, grid, p->threads, p->smem);
-     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(p->threads), args, (size_t)pv.smem, (cudaStream_t)stream);
+                  p->kind, p->variant, p->nfft, p->tb, grid, cta_threads(p), p->smem);
+     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(cta_threads(p)), args, (size_t)pv.smem, (cudaStream_t)stream);
      __atomic_add_fetch(&gb_launches, 1ull, __ATOMIC_RELAXED);
      return gb_check(e, "kernel launch");
 }

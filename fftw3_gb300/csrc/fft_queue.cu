@@ -3,9 +3,10 @@
  * device) claim items from a device queue with one atomic each and run them
  * with the shared-memory tile body of k_gen.  Items of one long transform
  * are ordered column tiles first, row tiles last; a row tile waits for its
- * transform's column tiles on a device counter.  Every wait is bounded (2 s
- * of wall time); a wait that gives up writes GB_STATUS_QUEUE_TIMEOUT to the
- * status word and the item is skipped, so the kernel always finishes.
+ * transform's column tiles on a device counter.  Every wait is bounded
+ * (wait_ns of wall time, 2 s unless the set says otherwise); a wait that
+ * gives up writes GB_STATUS_QUEUE_TIMEOUT to the status word and the item is
+ * skipped, so the kernel always finishes.
  *
  * This is the GB300 replacement for running many independent plans one
  * after another (the reference's only way to execute a set of transforms):
@@ -31,7 +32,7 @@ __device__ __forceinline__ void red_release_add(int *p, int v)
 
 template <typename C, int THREADS>
 __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_queue(const gb_qitem *__restrict__ items, int nitems, int *head,
-                                                int *ctrs, int *status)
+                                                int *ctrs, int *status, unsigned long long wait_ns)
 {
      extern __shared__ __align__(16) unsigned char gb_smem[];
      __shared__ __align__(16) gb_qitem it;
@@ -50,7 +51,7 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_queue(const
                     const int *c = ctrs + it.wait_ctr;
                     unsigned long long t0 = globaltimer_ns();
                     while (ld_acquire(c) < it.wait_target) {
-                         if (globaltimer_ns() - t0 > 2000000000ull) {
+                         if (globaltimer_ns() - t0 > wait_ns) {
                               go = 0;
                               if (status) atomicExch(status, GB_STATUS_QUEUE_TIMEOUT);
                               break;
@@ -109,11 +110,11 @@ extern "C" int gb_queue_grid(int prec, int threads, int smem)
 }
 
 extern "C" int gb_launch_queue(const gb_qitem *items, int nitems, int *head, int *ctrs, int prec, int threads,
-                               int smem, int grid, void *stream)
+                               int smem, int grid, unsigned long long wait_ns, void *stream)
 {
      const void *fn = queue_kernel(prec, threads);
      int *status = gb_device_status_ptr();
-     void *args[5] = {(void *)&items, (void *)&nitems, (void *)&head, (void *)&ctrs, (void *)&status};
+     void *args[6] = {(void *)&items, (void *)&nitems, (void *)&head, (void *)&ctrs, (void *)&status, (void *)&wait_ns};
      if (smem > 48 * 1024 && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
           return -1;
      return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, (size_t)smem, (cudaStream_t)stream) == cudaSuccess ? 0 : -1;

@@ -3,4 +3,7 @@
 #define GB_MAXLOG 14
 #include "fft_reg_inst.cuh"
 extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir) { return gb::reg_lookup<0>(logn, kind, dir); }
-extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir) { return gb::tma_lookup<6>(logn, kind, dir); }
+extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir, int groups)
+{
+     return gb::tma_lookup<6>(logn, kind, dir, groups);
+}

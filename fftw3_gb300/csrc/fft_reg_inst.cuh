@@ -16,23 +16,24 @@ static const void *reg_pick(int kind, int dir)
      return 0;
 }
 
-template <int L>
+template <int L, int G>
 static const void *tma_pick(int kind, int dir)
 {
-     if constexpr (L < 6 || L > 13) return 0;
+     if constexpr (L < 6 || L > 13 || G > tma_max_groups(sizeof(GB_CT))) return 0;
      else {
-          if (kind == GB_KIND_R2C) return (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_R2C>;
-          return dir < 0 ? (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_C2C> : (const void *)k_reg_tma<GB_CT, L, 1, GB_KIND_C2C>;
+          if (kind == GB_KIND_R2C) return (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_R2C, G>;
+          return dir < 0 ? (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_C2C, G>
+                         : (const void *)k_reg_tma<GB_CT, L, 1, GB_KIND_C2C, G>;
      }
 }
 
 template <int L>
-static const void *tma_lookup(int logn, int kind, int dir)
+static const void *tma_lookup(int logn, int kind, int dir, int groups)
 {
      if constexpr (L > 13) return 0;
      else {
-          if (logn == L) return tma_pick<L>(kind, dir);
-          return tma_lookup<L + 1>(logn, kind, dir);
+          if (logn == L) return groups == 2 ? tma_pick<L, 2>(kind, dir) : groups == 1 ? tma_pick<L, 1>(kind, dir) : 0;
+          return tma_lookup<L + 1>(logn, kind, dir, groups);
      }
 }
 

@@ -157,6 +157,14 @@ GB_EXT(fftwf_, fftwf_plan)
           gb_set_info((const gb_set *)s, nitems, ntransforms, nlong, grid, smem);      \
           return 0;                                                                    \
      }                                                                                 \
+     int PFX_##gb300_set_wait_limit(SET s, double seconds)                             \
+     {                                                                                 \
+          return s ? gb_set_wait_limit((gb_set *)s, seconds) : -1;                     \
+     }                                                                                 \
+     int PFX_##gb300_set_test_stall(SET s, int on)                                     \
+     {                                                                                 \
+          return s ? gb_set_test_stall((gb_set *)s, on) : -1;                          \
+     }                                                                                 \
      void PFX_##gb300_destroy_set(SET s)                                               \
      {                                                                                 \
           gb_lock();                                                                   \

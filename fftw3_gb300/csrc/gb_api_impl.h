@@ -35,20 +35,25 @@ static PFX(plan) PFX(wrap)(gb_plan *g)
 static PFX(plan) PFX(mk)(gb_problem *prb, unsigned flags)
 {
      gb_plan *g;
-     if (flags & FFTW_WISDOM_ONLY) {
-          /* the reference returns NULL when wisdom has no entry
-           * (api/apiplan.c:102-107); wisdom here keys passes by length */
-          char key[128];
-          long long n = prb->rank > 0 ? prb->sz[prb->rank - 1].n : 1;
-          snprintf(key, sizeof key, "c2c p%d n%lld", prb->prec, n);
-          if (!gb_wisdom_lookup(key)) {
-               gb_set_error("FFTW_WISDOM_ONLY: no wisdom for this problem");
-               return 0;
-          }
-     }
+     char key[256];
+     gb_problem_key(prb, key, sizeof key);
      gb_lock();
+     if ((flags & FFTW_WISDOM_ONLY) && !gb_wisdom_lookup(key)) {
+          /* the reference returns NULL when wisdom has no entry for the
+           * problem (api/apiplan.c:102-107); the entry is the whole problem's
+           * key, recorded when a problem of this exact shape was tuned */
+          gb_unlock();
+          gb_set_error("FFTW_WISDOM_ONLY: no wisdom for this problem");
+          return 0;
+     }
      g = gb_mkplan(prb, flags);
-     if (g && !(flags & FFTW_ESTIMATE) && !gb_dry_run()) gb_tune(g, flags);
+     if (g && !(flags & (FFTW_ESTIMATE | FFTW_WISDOM_ONLY)) && !gb_dry_run() && gb_tune(g, flags) == 0) {
+          gb_wisdom_entry e;
+          memset(&e, 0, sizeof e);
+          snprintf(e.key, sizeof e.key, "%s", key);
+          e.variant = -2;   /* a tuned problem, no pass choice of its own */
+          gb_wisdom_store(&e);
+     }
      gb_unlock();
      return PFX(wrap)(g);
 }

@@ -77,6 +77,11 @@ static void *mapped_host(const void *ptr)
 static int ensure(void **buf, size_t *have, size_t need)
 {
      if (*have >= need) return 0;
+     /* an earlier call's copies may still be queued on the old buffer */
+     if (*buf && cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("staging: %s", cudaGetErrorString(cudaGetLastError()));
+          return -1;
+     }
      if (*buf) cudaFree(*buf);
      *buf = 0;
      *have = 0;
@@ -270,7 +275,11 @@ cuerr:
      return -1;
 }
 
-int gb_execute(gb_plan *p, void *in, void *out)
+/* One execute with the plan's lock held.  *sync_after = 1 asks the caller
+ * to wait for the plan's stream once the lock is released (a synchronous
+ * execute on device arrays): the next call may enqueue meanwhile, since the
+ * stream orders it after this one. */
+static int execute_locked(gb_plan *p, void *in, void *out, int *sync_after)
 {
      const gb_problem *prb = &p->prb;
      long long cin, cout;
@@ -375,11 +384,30 @@ int gb_execute(gb_plan *p, void *in, void *out)
                               device_accessible(out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st) != cudaSuccess)
                goto cuerr;
      }
-     if (stage_i || stage_o || direct_host || !p->async) {
+     if (stage_i || stage_o || direct_host) {
           if (cudaStreamSynchronize(st) != cudaSuccess) goto cuerr;
+     } else if (!p->async) {
+          *sync_after = 1;
      }
      return 0;
 cuerr:
      gb_set_error("CUDA error during execute: %s", cudaGetErrorString(cudaGetLastError()));
      return -1;
+}
+
+/* Executes from several host threads on one plan are safe: each takes the
+ * plan's lock while it enqueues (and, for host arrays, until its copies
+ * are back), so the device sees the calls one after another on the plan's
+ * stream and no two share the plan's scratch or staging buffers. */
+int gb_execute(gb_plan *p, void *in, void *out)
+{
+     int sync_after = 0, r;
+     pthread_mutex_lock(&p->exec_mtx);
+     r = execute_locked(p, in, out, &sync_after);
+     pthread_mutex_unlock(&p->exec_mtx);
+     if (r == 0 && sync_after && cudaStreamSynchronize((cudaStream_t)p->stream) != cudaSuccess) {
+          gb_set_error("CUDA error during execute: %s", cudaGetErrorString(cudaGetLastError()));
+          return -1;
+     }
+     return r;
 }

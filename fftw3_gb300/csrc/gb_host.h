@@ -62,6 +62,12 @@ typedef struct gb_r2r_axis {
 
 struct gb_plan {
      int refcnt;
+     /* held while one execute enqueues its work: calls on the same plan from
+      * several host threads reach the device one whole call after another,
+      * so the plan-owned scratch, staging buffers and chunk slots are never
+      * shared by two calls in flight (api/execute.c may run concurrently on
+      * one plan, doc/threads.texi:243-247) */
+     pthread_mutex_t exec_mtx;
      gb_problem prb;
      unsigned flags;
      int nstep;
@@ -110,6 +116,8 @@ typedef struct gb_plan gb_plan;
 
 /* planner / problem (gb_plan.c) */
 gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags);
+gb_plan *gb_plan_alloc(void);   /* zeroed plan with refcnt 1 and its execute lock */
+void gb_problem_key(const gb_problem *prb, char *key, size_t cap);   /* wisdom key of a whole problem */
 void gb_destroy(gb_plan *p);
 int gb_dry_run(void);
 void gb_set_dry_run(int on);
@@ -169,6 +177,8 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags);
 int gb_execute_set(gb_set *S);
 void gb_set_stream_of_set(gb_set *S, void *stream, int async);
 void gb_set_info(const gb_set *S, int *nitems, int *ntransforms, int *nlong, int *grid, int *smem);
+int gb_set_wait_limit(gb_set *S, double seconds);
+int gb_set_test_stall(gb_set *S, int on);
 void gb_destroy_set(gb_set *S);
 
 /* launch layer (fft_launch.cu) */

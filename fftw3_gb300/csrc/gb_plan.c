@@ -424,15 +424,28 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                const int ein = kind == GB_KIND_R2C ? prec : csize(prec);   /* bytes per input element */
                for (i = 0; i < nv; ++i)
                     if ((P->vis[i] * ein) % 16) ok = 0;
+               /* compute groups per CTA: two (four transforms in flight per SM
+                * over three buffers a CTA) where one transform needs 512 threads
+                * (nfft 8192), else one; FFTW_GB300_TMA_GROUPS overrides.  One
+                * buffer per group and one more; keep two CTAs of two groups or
+                * three of one group per SM */
+               const char *genv = getenv("FFTW_GB300_TMA_GROUPS");
+               int groups = (nfft >= 8192 && prec == 4) ? 2 : 1;
+               if (genv && (atoi(genv) == 1 || atoi(genv) == 2)) groups = atoi(genv);
+               if (groups > gb_tma_max_groups(prec)) groups = gb_tma_max_groups(prec);
+               const int nbuf = groups + 1;
+               const long long cap = groups == 2 ? 113 * 1024 : 76 * 1024;
                if (tbt < 1) tbt = 1;
-               while (tbt > 1 && (tbt >> 1) >= v[0].n) tbt >>= 1;
-               sm2 = 2LL * tbt * tma_sms((int)nfft) * csize(prec);
-               while (tbt > 1 && sm2 > 76 * 1024) {   /* keep >= 3 CTAs per SM */
+               /* a group is whole warps (its named barrier counts threads in warps) */
+               while (tbt > 1 && (tbt >> 1) >= v[0].n && (tbt >> 1) * T >= 32) tbt >>= 1;
+               sm2 = (long long)nbuf * tbt * tma_sms((int)nfft) * csize(prec);
+               while (tbt > 1 && sm2 > cap && (tbt >> 1) * T >= 32) {
                     tbt >>= 1;
-                    sm2 = 2LL * tbt * tma_sms((int)nfft) * csize(prec);
+                    sm2 = (long long)nbuf * tbt * tma_sms((int)nfft) * csize(prec);
                }
                if (ok && sm2 <= smax) {
                     P->variant = GB_VAR_TMA;
+                    P->groups = groups;
                     P->tb = tbt;
                     P->threads = tbt * T;
                     P->smem = (int)sm2;
@@ -1030,6 +1043,38 @@ static void describe(gb_plan *p)
      if (off < (int)sizeof p->desc - 1) snprintf(p->desc + off, sizeof p->desc - off, ")");
 }
 
+/* Wisdom key of a whole problem (the reference keys wisdom by the md5 of
+ * the problem, kernel/planner.c:651-703): kind, precision, direction, every
+ * transform and vector dimension with its strides, in-place-ness and the
+ * arrays' alignment, folded into a 64-bit FNV-1a hash. */
+void gb_problem_key(const gb_problem *prb, char *key, size_t cap)
+{
+     unsigned long long h = 1469598103934665603ULL;
+     long long f[8 + 6 * GB_MAXRANK];
+     int k = 0, i, j;
+     f[k++] = prb->kind; f[k++] = prb->prec; f[k++] = prb->sign; f[k++] = prb->rank; f[k++] = prb->vrank;
+     for (i = 0; i < prb->rank; ++i) { f[k++] = prb->sz[i].n; f[k++] = prb->sz[i].is; f[k++] = prb->sz[i].os; }
+     for (i = 0; i < prb->vrank; ++i) { f[k++] = prb->vec[i].n; f[k++] = prb->vec[i].is; f[k++] = prb->vec[i].os; }
+     f[k++] = prb->in == prb->out;
+     f[k++] = (long long)((size_t)prb->in % 16);
+     f[k++] = (long long)((size_t)prb->out % 16);
+     for (i = 0; i < k; ++i)
+          for (j = 0; j < 8; ++j) {
+               h ^= (unsigned long long)(f[i] >> (8 * j)) & 0xffULL;
+               h *= 1099511628211ULL;
+          }
+     snprintf(key, cap, "prob p%d k%d r%d %016llx", prb->prec, prb->kind, prb->rank, h);
+}
+
+gb_plan *gb_plan_alloc(void)
+{
+     gb_plan *p = (gb_plan *)calloc(1, sizeof *p);
+     if (!p) return 0;
+     p->refcnt = 1;
+     pthread_mutex_init(&p->exec_mtx, 0);
+     return p;
+}
+
 /* Build the steps of a problem.  Returns NULL (with gb_last_error set) when
  * the problem is invalid or not supported. */
 gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
@@ -1041,8 +1086,11 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
           gb_set_error("no CUDA device: libfftw3_gb300 runs transforms on the GPU only");
           return 0;
      }
-     p = (gb_plan *)calloc(1, sizeof *p);
-     p->refcnt = 1;
+     p = gb_plan_alloc();
+     if (!p) {
+          gb_set_error("out of host memory");
+          return 0;
+     }
      p->prb = *prb;
      p->flags = flags;
      b.p = p; b.err = 0;
@@ -1118,6 +1166,7 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
            * (rdft/rank-geq2-rdft2.c:118-124) */
           if (r > 1 && (flags & FFTW_PRESERVE_INPUT) && prb->in != prb->out) {
                gb_set_error("multi-dimensional c2r cannot preserve its input");
+               pthread_mutex_destroy(&p->exec_mtx);
                free(p);
                return 0;
           }
@@ -1144,6 +1193,7 @@ gb_plan *gb_mkplan(const gb_problem *prb, unsigned flags)
      }
 built:
      if (b.err) {
+          pthread_mutex_destroy(&p->exec_mtx);
           free(p);
           return 0;
      }
@@ -1151,6 +1201,7 @@ built:
           if (cudaMalloc(&p->scratch2, p->scratch2_bytes) != cudaSuccess) {
                cudaGetLastError();
                gb_set_error("cudaMalloc(%zu) for plan scratch failed", p->scratch2_bytes);
+               pthread_mutex_destroy(&p->exec_mtx);
                free(p);
                return 0;
           }
@@ -1159,6 +1210,7 @@ built:
           if (cudaMalloc(&p->scratch, p->scratch_bytes) != cudaSuccess) {
                cudaGetLastError();
                gb_set_error("cudaMalloc(%zu) for plan scratch failed", p->scratch_bytes);
+               pthread_mutex_destroy(&p->exec_mtx);
                free(p);
                return 0;
           }
@@ -1201,5 +1253,6 @@ void gb_destroy(gb_plan *p)
      for (i = 0; i < 2; ++i)
           if (p->r2r_buf[i] && !gb_dry) cudaFree(p->r2r_buf[i]);
      if (p->r2r_mid && !gb_dry) cudaFree(p->r2r_mid);
+     pthread_mutex_destroy(&p->exec_mtx);
      free(p);
 }

@@ -93,9 +93,8 @@ gb_plan *gb_mkr2r(int prec, int rank, const gb_dim *dims, const int *kinds, int 
           }
      }
      for (d = 0; d < vrank; ++d) if (vdims[d].n < 0) return 0;
-     p = (gb_plan *)calloc(1, sizeof *p);
+     p = gb_plan_alloc();
      if (!p) return 0;
-     p->refcnt = 1;
      p->flags = flags;
      p->prb.kind = GB_PROB_R2R;
      p->prb.prec = prec;
@@ -242,7 +241,20 @@ static void r2r_span(const gb_problem *q, int out, long long *lo, long long *hi)
      }
 }
 
+static int execute_r2r_locked(gb_plan *p, void *in, void *out);
+
+/* One call at a time per plan (its core buffers and intermediate are
+ * plan-owned); calls from several host threads queue up on the plan's lock. */
 int gb_execute_r2r(gb_plan *p, void *in, void *out)
+{
+     int r;
+     pthread_mutex_lock(&p->exec_mtx);
+     r = execute_r2r_locked(p, in, out);
+     pthread_mutex_unlock(&p->exec_mtx);
+     return r;
+}
+
+static int execute_r2r_locked(gb_plan *p, void *in, void *out)
 {
      const int prec = p->prb.prec;
      cudaStream_t st = (cudaStream_t)p->stream;

@@ -24,6 +24,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <stddef.h>
 #include <cuda_runtime_api.h>
 #include "gb_host.h"
 
@@ -47,8 +48,13 @@ struct gb_set {
      cudaGraph_t graph;
      cudaGraphExec_t gexec;
      int nsingle_items, nlong, ntransforms;
+     unsigned long long wait_ns;    /* bound on a row tile's wait for its column tiles */
+     int stall_item;                /* item whose wait target the test hook raised (-1: none) */
+     int stall_target;              /* its true target */
 };
 typedef struct gb_set gb_set;
+
+static void drop_graph(gb_set *S);
 
 static int is_prime_ll(long long n)
 {
@@ -308,6 +314,8 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
      S->nsingle_items = nm;
      S->nlong = nctr;
      S->ntransforms = nx;
+     S->wait_ns = 2000000000ull;
+     S->stall_item = -1;
      S->scratch_bytes = (size_t)scratch_elems * cs;
      S->grid = S->nsmall ? gb_queue_grid(prec, S->threads, S->smem) : 1;
      S->grid_l = S->nlarge ? gb_queue_grid(prec, S->threads_l, S->smem_l) : 1;
@@ -382,10 +390,10 @@ static int build_graph(gb_set *S)
           cudaMemsetAsync(S->d_head, 0, 2 * sizeof(int), st);
           if (S->nctr) cudaMemsetAsync(S->d_ctrs, 0, sizeof(int) * (size_t)S->nctr, st);
           if (S->nlarge && gb_launch_queue(S->d_items + S->nsmall, S->nlarge, S->d_head + 1, S->d_ctrs, S->prec,
-                                           S->threads_l, S->smem_l, S->grid_l, st))
+                                           S->threads_l, S->smem_l, S->grid_l, S->wait_ns, st))
                rc = -1;
           if (S->nsmall && gb_launch_queue(S->d_items, S->nsmall, S->d_head, S->d_ctrs, S->prec, S->threads,
-                                           S->smem, S->grid, st))
+                                           S->smem, S->grid, S->wait_ns, st))
                rc = -1;
           if (cudaStreamEndCapture(st, &S->graph) != cudaSuccess) rc = -1;
      }
@@ -415,14 +423,69 @@ int gb_execute_set(gb_set *S)
 
 void gb_set_stream_of_set(gb_set *S, void *stream, int async)
 {
-     if (S->stream != stream && S->gexec) {
+     if (S->stream != stream) drop_graph(S);
+     S->stream = stream;
+     S->async = async;
+}
+
+static void drop_graph(gb_set *S)
+{
+     if (S->gexec) {
           cudaGraphExecDestroy(S->gexec);
           cudaGraphDestroy(S->graph);
           S->gexec = 0;
           S->graph = 0;
      }
-     S->stream = stream;
-     S->async = async;
+}
+
+/* Bound on the device-side wait of a row tile (the graph is re-captured
+ * with the new limit on the next execute). */
+int gb_set_wait_limit(gb_set *S, double seconds)
+{
+     if (!(seconds > 0) || seconds > 60) {
+          gb_set_error("plan set: wait limit must be in (0, 60] seconds");
+          return -1;
+     }
+     S->wait_ns = (unsigned long long)(seconds * 1e9);
+     drop_graph(S);
+     return 0;
+}
+
+/* Test hook for the bounded waits: on != 0 raises the wait target of the
+ * set's first row tile one above what its column tiles will reach, so its
+ * wait runs out on the next execute (GB_STATUS_QUEUE_TIMEOUT, the tile is
+ * skipped); on == 0 puts the true target back.  Returns -1 when the set has
+ * no row tile.  Only the device copy of the item changes. */
+int gb_set_test_stall(gb_set *S, int on)
+{
+     const size_t off = offsetof(gb_qitem, wait_target);
+     int i, v;
+     if (on && S->stall_item < 0) {
+          for (i = 0; i < S->nsmall && S->stall_item < 0; ++i) {
+               gb_qitem it;
+               if (cudaMemcpy(&it, S->d_items + i, sizeof it, cudaMemcpyDeviceToHost) != cudaSuccess) goto cuerr;
+               if (it.wait_ctr >= 0) {
+                    S->stall_item = i;
+                    S->stall_target = it.wait_target;
+               }
+          }
+          if (S->stall_item < 0) {
+               gb_set_error("plan set: no row tile waits on a counter");
+               return -1;
+          }
+          v = S->stall_target + 1;
+          if (cudaMemcpy((char *)(S->d_items + S->stall_item) + off, &v, sizeof v, cudaMemcpyHostToDevice) != cudaSuccess)
+               goto cuerr;
+     } else if (!on && S->stall_item >= 0) {
+          v = S->stall_target;
+          if (cudaMemcpy((char *)(S->d_items + S->stall_item) + off, &v, sizeof v, cudaMemcpyHostToDevice) != cudaSuccess)
+               goto cuerr;
+          S->stall_item = -1;
+     }
+     return 0;
+cuerr:
+     gb_set_error("plan set: %s", cudaGetErrorString(cudaGetLastError()));
+     return -1;
 }
 
 void gb_set_info(const gb_set *S, int *nitems, int *ntransforms, int *nlong, int *grid, int *smem)

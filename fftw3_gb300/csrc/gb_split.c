@@ -77,9 +77,8 @@ gb_plan *gb_mksplit(int kind, int prec, int rank, const gb_dim *dims, int vrank,
           din *= vdims[d].n;
           dout *= vdims[d].n;
      }
-     p = (gb_plan *)calloc(1, sizeof *p);
+     p = gb_plan_alloc();
      if (!p) return 0;
-     p->refcnt = 1;
      p->flags = flags;
      p->split_kind = kind;
      p->prb.kind = kind;
@@ -213,7 +212,20 @@ static void split_pair_close(split_pair *sp)
 
 /* c2c: (ri, ii) -> (ro, io); r2c: a0 = real input -> (a2, a3) = (ro, io);
  * c2r: (a0, a1) = (ri, ii) -> a2 = real output */
+static int execute_split_locked(gb_plan *p, void *a0, void *a1, void *a2, void *a3);
+
+/* One call at a time per plan (its dense buffers are plan-owned); calls from
+ * several host threads on one plan queue up on the plan's lock. */
 int gb_execute_split(gb_plan *p, void *a0, void *a1, void *a2, void *a3)
+{
+     int r;
+     pthread_mutex_lock(&p->exec_mtx);
+     r = execute_split_locked(p, a0, a1, a2, a3);
+     pthread_mutex_unlock(&p->exec_mtx);
+     return r;
+}
+
+static int execute_split_locked(gb_plan *p, void *a0, void *a1, void *a2, void *a3)
 {
      const int es = p->prb.prec, kind = p->split_kind;
      cudaStream_t st = (cudaStream_t)p->stream;

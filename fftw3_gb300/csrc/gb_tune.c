@@ -152,6 +152,10 @@ int gb_tune(gb_plan *p, unsigned flags)
           if (q) {
                gb_plan keep = *p;
                *p = *q;
+               /* the plan keeps its own (unlocked: tuning runs before the
+                * plan is returned) execute lock */
+               p->exec_mtx = keep.exec_mtx;
+               pthread_mutex_destroy(&q->exec_mtx);
                p->refcnt = keep.refcnt;
                p->stream = keep.stream;
                p->async = keep.async;

@@ -72,7 +72,8 @@ typedef struct gb_pass {
      int nfft;          /* length of the complex FFT run by the kernel */
      int variant;       /* enum gb_variant */
      int tb;            /* transforms per CTA (along vector dimension 0) */
-     int threads;       /* threads per CTA */
+     int threads;       /* threads per CTA (per compute group for GB_VAR_TMA) */
+     int groups;        /* GB_VAR_TMA: compute groups per CTA (1 or 2), each over its own tile buffer */
      int smem;          /* dynamic shared memory bytes */
      int load_mode;     /* enum gb_move */
      int store_mode;    /* enum gb_move */
@@ -142,11 +143,16 @@ static inline int gb_pad_mult(int nfft)
      return (r == 16 && nfft >= 256) ? 2 : 1;
 }
 static inline int gb_reg_sms(int nfft) { return (nfft + gb_pad_mult(nfft) * (nfft >> 4) + 3) & ~1; }
+/* Most compute groups a k_reg_tma CTA can run (prec: bytes per real): two
+ * for float (64 registers a thread), one for double, whose 16 elements a
+ * thread already fill 64 registers.  A CTA of g groups of gb_pass.threads
+ * threads has g + 1 shared-memory tile buffers. */
+static inline int gb_tma_max_groups(int prec) { return prec == 4 ? 2 : 1; }
 
 /* Launchers implemented in the .cu files (plain C ABI). */
 int gb_launch_pass(const gb_pass *p, const void *in, void *out, void *stream);
 int gb_launch_queue(const gb_qitem *items, int nitems, int *head, int *ctrs, int prec, int threads, int smem,
-                    int grid, void *stream);
+                    int grid, unsigned long long wait_ns, void *stream);
 int gb_queue_grid(int prec, int threads, int smem);
 int gb_pass_configure(gb_pass *p, int max_smem_optin);
 int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream);

@@ -38,6 +38,10 @@ extern int fftw_gb300_device_status(void);
  * (IEEE half, row-major, device memory) and D 128 x 32 (float, device);
  * ks in 1..6.  Returns 0 on success. */
 extern int fftw_gb300_tc_selftest(const void *A, const void *B, float *D, int ks);
+/* FP64 fused multiply-add rate of the current GPU in GFLOP/s (two flops per
+ * FMA), measured with CUDA events: the roofline of double-precision passes,
+ * which this part's few FP64 units bound before HBM does.  0 on error. */
+extern double fftw_gb300_fp64_fma_gflops(void);
 
 /* No counterpart in the reference: a batched f32 1D c2c DFT that allocates
  * no device memory, for callers that cannot call cudaMalloc (device memory
@@ -45,7 +49,7 @@ extern int fftw_gb300_tc_selftest(const void *A, const void *B, float *D, int ks
  * implicit synchronisation).  It runs the two-pass (four-step) kernels of
  * a long 1D plan with their scratch and twiddle tables in one fixed device
  * array of the library, which every GPU it runs on holds until exit
- * (16 MiB + 33 KiB).  howmany contiguous transforms of length n at distance
+ * (16 MiB + 48.25 KiB).  howmany contiguous transforms of length n at distance
  * n; in and out are device arrays (they may be the same); n is a power of
  * two from 2^12 to 2^21 and n * howmany <= FFTWF_GB300_NOALLOC_MAX_POINTS,
  * else it returns -1 without launching.  Enqueues on cuda_stream and
@@ -73,6 +77,13 @@ extern int PFX##gb300_execute_set(PFX##gb300_set s);                            
 extern int PFX##gb300_set_stream_set(PFX##gb300_set s, void *cuda_stream, int async); \
 extern int PFX##gb300_set_info(PFX##gb300_set s, int *nitems, int *ntransforms,       \
                                int *nlong, int *grid, int *smem);                     \
+/* Bound (seconds, default 2) on a row tile's device-side wait for the      \
+ * column tiles of its transform; a wait that runs out skips the tile and   \
+ * sets device status 2.  Test hook: set_test_stall(s, 1) makes the first   \
+ * row tile wait for one column tile more than exist (its wait runs out on  \
+ * every execute), set_test_stall(s, 0) undoes it.                          */\
+extern int PFX##gb300_set_wait_limit(PFX##gb300_set s, double seconds);               \
+extern int PFX##gb300_set_test_stall(PFX##gb300_set s, int on);                       \
 extern void PFX##gb300_destroy_set(PFX##gb300_set s);
 
 GB_FFTW_EXT_DECLARE(fftw_)

@@ -37,19 +37,33 @@ FFTW_ESTIMATE = 1 << 6
 FFTW_ALLOW_LARGE_GENERIC = 1 << 13
 
 
+def ref_root() -> str | None:
+    """The reference FFTW checkout: the directory FFTW_REF_SRC names, else a
+    checkout named ``reference`` beside this repository; None where neither
+    exists (the reference is then only present through the committed
+    fixtures under tests/golden/)."""
+    env = os.environ.get("FFTW_REF_SRC")
+    cands = [env] if env else [os.path.join(os.path.dirname(HERE), os.pardir, "reference")]
+    for c in cands:
+        if c and os.path.isfile(os.path.join(c, "api", "fftw3.h")):
+            return os.path.realpath(c)
+    return None
+
+
 def build(ref: bool = False) -> None:
     """Compile the restatement (and, if asked and possible, the reference)."""
     subprocess.run(["make", "-s", "-C", HERE, "restate"], check=True)
-    if ref and os.path.isdir(os.environ.get("FFTW_REF_SRC", "/root/reference")):
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref",
-                        "REF=" + os.environ.get("FFTW_REF_SRC", "/root/reference")], check=True)
+    src = ref_root()
+    if ref and src:
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + src], check=True)
 
 
 def ref_source(rel: str) -> str | None:
-    """Path of a file of the reference checkout (FFTW_REF_SRC), or None
-    where the reference sources are absent."""
-    path = os.path.join(os.environ.get("FFTW_REF_SRC", "/root/reference"), rel)
-    return path if os.path.isfile(path) else None
+    """Path of a file of the reference checkout, or None where the
+    reference sources are absent."""
+    src = ref_root()
+    path = os.path.join(src, rel) if src else None
+    return path if path and os.path.isfile(path) else None
 
 
 def harness() -> str | None:
@@ -60,8 +74,7 @@ def harness() -> str | None:
     in dry-run mode (oracle/ref/harness_shim.c)."""
     if ref_source(os.path.join("tests", "bench.c")) is None:
         return None
-    src = os.environ.get("FFTW_REF_SRC", "/root/reference")
-    subprocess.run(["make", "-s", "-C", HERE, "harness", "REF=" + src], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "harness", "REF=" + ref_root()], check=True)
     return os.path.join(REFDIR, "bench_gb300")
 
 

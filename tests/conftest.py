@@ -52,6 +52,16 @@ def golden_cases():
     return out
 
 
+def rel_l2_f(y, ref):
+    """rel_l2 in double precision: for float results, whose errors (~1e-7)
+    double arithmetic resolves exactly enough, on arrays too large for the
+    long-double sum (software quad precision on some hosts)."""
+    y = np.asarray(y).ravel().astype(np.complex128)
+    ref = np.asarray(ref).ravel().astype(np.complex128)
+    den = np.linalg.norm(ref)
+    return float(np.linalg.norm(y - ref) / den) if den > 0 else float(np.linalg.norm(y))
+
+
 def rel_l2(y, ref):
     y = np.asarray(y).ravel()
     ref = np.asarray(ref).ravel()

@@ -196,6 +196,32 @@ def test_c2c_inplace_3d(lib, torch_cuda, restatement):
     assert rel_l2(back, x) <= 1e-6
 
 
+def test_c2c_inplace_3d_256_forward(lib, torch_cuda, restatement):
+    """plan_dft_3d 256^3 in place: the forward transform of the whole array
+    against the oracle (the round trip alone cannot see errors that cancel
+    between the two directions), then backward / N back to the input."""
+    import fftw3_gb300 as g
+    torch = torch_cuda
+    shape = [256, 256, 256]
+    tot = int(np.prod(shape))
+    rng = np.random.default_rng(256)
+    x = (rng.uniform(-1, 1, tot) + 1j * rng.uniform(-1, 1, tot)).astype(np.complex64)
+    a = _dev(torch, x)
+    lib_ = g.load()
+    pf = g.Plan(lib_.fftwf_plan_dft_3d(*shape, a.data_ptr(), a.data_ptr(), -1, g.FFTW_ESTIMATE), "f")
+    pb = g.Plan(lib_.fftwf_plan_dft_3d(*shape, a.data_ptr(), a.data_ptr(), 1, g.FFTW_ESTIMATE), "f")
+    assert len(pf.passes()) == 3
+    pf.execute()
+    yf = _host(a).astype(np.complex128)
+    ref = restatement.c2c(x.astype(np.complex128), shape, -1, "d", nthreads=8)
+    err = float(np.linalg.norm(yf - ref.ravel()) / np.linalg.norm(ref))
+    assert err <= 1e-6, f"forward rel L2 {err:.3e}"
+    del yf, ref
+    pb.execute()
+    back = _host(a) / tot
+    assert rel_l2(back, x) <= 1e-6
+
+
 def test_strided_embedded(lib, torch_cuda, restatement):
     """plan_many_dft with istride/idist/inembed/onembed (the advanced layout)."""
     import fftw3_gb300 as g

@@ -8,7 +8,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import rel_l2
+from conftest import rel_l2, rel_l2_f
 
 pytestmark = pytest.mark.gpu
 
@@ -42,7 +42,7 @@ def _check(restatement, xin, yout, offs, lengths, prec, sign, sample=None):
         a, b = int(offs[i]), int(offs[i + 1])
         xo = x[a:b].astype(np.clongdouble if prec == "d" else np.complex128)
         ref = restatement.c2c(xo, [b - a], sign, "l" if prec == "d" else "d")
-        e = rel_l2(y[a:b], ref)
+        e = (rel_l2_f if prec == "f" else rel_l2)(y[a:b], ref)
         worst = max(worst, e)
         assert e <= tol, f"transform {i} (n={b - a}): rel L2 {e:.3e}"
     return worst
@@ -138,3 +138,61 @@ def test_planset_first_use_in_fresh_process(lib):
         "print(rc, err); sys.exit(0 if rc == 0 and err < 1e-6 else 1)\n" % ROOT)
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_planset_bounded_wait_runs_out(lib, torch_cuda_set, restatement):
+    """A row tile whose column tiles never all arrive: its wait gives up after
+    the set's limit (5 ms here), the tile is skipped, the launch finishes and
+    the device status reads 2 (GB_STATUS_QUEUE_TIMEOUT); nothing traps or
+    hangs, and the next execute of the unchanged set is correct."""
+    torch = torch_cuda_set
+    lengths = [65536, 32768, 4096, 1000, 97]
+    xin, yout, offs, plans = _make_set(torch, lengths, "f", seed=11)
+    lib_, pfx, s = _set_of(plans, "f")
+    ex = getattr(lib_, pfx + "gb300_execute_set")
+    wait = getattr(lib_, pfx + "gb300_set_wait_limit")
+    wait.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    stall = getattr(lib_, pfx + "gb300_set_test_stall")
+    stall.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    assert lib_.fftw_gb300_device_status() == 0
+    assert wait(s, 0.005) == 0
+    assert stall(s, 1) == 0
+    assert ex(s) == 0
+    torch.cuda.synchronize()
+    assert lib_.fftw_gb300_device_status() == 2
+    # the status word was cleared by the read
+    assert lib_.fftw_gb300_device_status() == 0
+    assert stall(s, 0) == 0
+    assert wait(s, 2.0) == 0
+    yout.zero_()
+    assert ex(s) == 0
+    torch.cuda.synchronize()
+    assert lib_.fftw_gb300_device_status() == 0
+    _check(restatement, xin, yout, offs, lengths, "f", -1)
+    # a limit outside (0, 60] s is refused
+    assert wait(s, 0.0) == -1 and wait(s, 100.0) == -1
+    getattr(lib_, pfx + "gb300_destroy_set")(s)
+
+
+def test_planset_uneven10k(lib, torch_cuda_set, restatement):
+    """The 10,000-transform uneven set (60% powers of two 2^6..2^16, 30%
+    7-smooth lengths in [60, 60000], 10% primes in [17, 4093], seed 7) as one
+    graph launch: every prime transform and a seeded sample of 200 others
+    against the oracle."""
+    torch = torch_cuda_set
+    import bench
+    lengths = bench.uneven_lengths(np.random.default_rng(7), 10000)
+    xin, yout, offs, plans = _make_set(torch, lengths, "f", seed=5)
+    lib_, pfx, s = _set_of(plans, "f")
+    assert getattr(lib_, pfx + "gb300_execute_set")(s) == 0
+    torch.cuda.synchronize()
+    assert lib_.fftw_gb300_device_status() == 0
+    primes = set(bench.primes_in(17, 4093))
+    prime_idx = [i for i, n in enumerate(lengths) if n in primes]
+    others = [i for i in range(len(lengths)) if lengths[i] not in primes]
+    sample = sorted(prime_idx + list(np.random.default_rng(1).choice(others, 200, replace=False)))
+    assert len(prime_idx) > 800
+    _check(restatement, xin, yout, offs, lengths, "f", -1, sample=sample)
+    getattr(lib_, pfx + "gb300_destroy_set")(s)
+    for p in plans:
+        p.destroy()
