@@ -397,27 +397,24 @@ def run_ours(args):
         rt_err = float(torch.linalg.vector_norm(xin / n - x0) / torch.linalg.vector_norm(x0))
         if not k:
             err = rt_err
-    elif kind == "r2r":
-        xs = xin[: k * n].cpu().numpy()
-        step()
-        torch.cuda.synchronize()
-        ref = Restatement().r2r_fast(xs.astype(np.float64 if prec == "f" else np.longdouble), n, R2R_KIND,
-                                     "d" if prec == "f" else "l", os.cpu_count() or 1)
-        err = rel_l2(yout[: k * n].cpu().numpy(), ref)
-    elif kind == "c2c":
-        xs = xin[: k * n].cpu().numpy()
-        step()
-        torch.cuda.synchronize()
-        ref = Restatement().c2c(xs.astype(np.complex128 if prec == "f" else np.clongdouble), shape, -1,
-                                "d" if prec == "f" else "l", os.cpu_count() or 1)
-        err = rel_l2(yout[: k * n].cpu().numpy(), ref)
     else:
-        xs = xin[: k * n].cpu().numpy()
+        # k transforms spread evenly over the batch (every CTA of a persistent
+        # kernel walks many tiles: the sample covers late tiles too)
+        sel = torch.from_numpy(np.linspace(0, howmany - 1, k).astype(np.int64)).cuda()
+        xs = xin.view(howmany, n)[sel].cpu().numpy()
         step()
         torch.cuda.synchronize()
-        ref = Restatement().r2c(xs.astype(np.float64 if prec == "f" else np.longdouble), shape,
-                                "d" if prec == "f" else "l", os.cpu_count() or 1)
-        err = rel_l2(yout[: k * nc].cpu().numpy(), ref)
+        no = nc if kind == "r2c" else n
+        ys = yout.view(howmany, no)[sel].cpu().numpy()
+        rdt, cdt_ = (np.float64, np.complex128) if prec == "f" else (np.longdouble, np.clongdouble)
+        if kind == "r2r":
+            ref = Restatement().r2r_fast(xs.astype(rdt), n, R2R_KIND, "d" if prec == "f" else "l",
+                                         os.cpu_count() or 1)
+        elif kind == "c2c":
+            ref = Restatement().c2c(xs.astype(cdt_), shape, -1, "d" if prec == "f" else "l", os.cpu_count() or 1)
+        else:
+            ref = Restatement().r2c(xs.astype(rdt), shape, "d" if prec == "f" else "l", os.cpu_count() or 1)
+        err = rel_l2(ys, ref)
 
     # the split-FP16 tensor-core form on the same batch, beside the FP32 form
     tc = None

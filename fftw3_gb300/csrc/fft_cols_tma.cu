@@ -6,8 +6,9 @@
  *
  * The tensor map views the pass input as [outer dims][row j < N][column];
  * one tile is tb columns x N rows, fetched as boxes of at most 16 columns
- * (128 bytes) x 256 rows with cp.async.bulk.tensor into one of two shared
- * slots while the tile in the other slot is transformed.  The boxes land
+ * (128 bytes) x 256 rows with cp.async.bulk.tensor into a shared slot: a
+ * CTA runs one or two compute groups over one slot more than groups, so a
+ * tile is on its way while every group transforms one.  The boxes land
  * row-major with the 16-byte-chunk swizzle that matches their row width
  * (32/64/128 bytes), so the transform-major gather that follows touches
  * eight different 16-byte chunks per eight consecutive rows.  From there the
@@ -18,7 +19,7 @@
  * output's strides allow, else with plain stores.
  *
  * Every wait on a slot is bounded (2 s of wall time); a copy that never
- * completes sets GB_STATUS_COPY_TIMEOUT and the CTA returns.
+ * completes sets GB_STATUS_COPY_TIMEOUT and the group leaves its loop.
  */
 #include <cuda.h>
 #include "fft_kernels.cuh"
@@ -126,8 +127,20 @@ __device__ __forceinline__ void ct_issue(const gb_pass &P, const CUtensorMap *tm
           }
 }
 
-template <int LOGN, int DIR>
-__global__ void __launch_bounds__(256, 3)
+/* CTAs per SM the registers are sized for: three of one group (85
+ * registers a thread), two of two groups (64) */
+__host__ __device__ constexpr int ct_minblocks(int G) { return G == 2 ? 2 : 3; }
+
+/* Byte offset of slot b: slots on 1024-byte boundaries (the period of the
+ * 128-byte swizzle the boxes land in) */
+__host__ __device__ inline int ct_slot_off(int nfft, int tb, int b) { return b * ((ct_slot_bytes(nfft, tb) + 1023) & ~1023); }
+
+/* G compute groups (P.threads threads each, own named barrier) over G + 1
+ * slots, as k_reg_tma: tile i (global tile blockIdx.x + i gridDim.x) is
+ * transformed by group i mod G in slot i mod (G + 1), and the group that
+ * finishes with a slot issues the boxes of the slot's next tile. */
+template <int LOGN, int DIR, int G>
+__global__ void __launch_bounds__(256 * G, ct_minblocks(G))
 k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out, const __grid_constant__ CUtensorMap tmap,
            const __grid_constant__ CUtensorMap omap, const int tstore)
 {
@@ -136,82 +149,110 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
      constexpr int E = reg_e(N);
      constexpr int T = N / E;
      constexpr int SMS = reg_sms(N);
-     /* no static shared memory (it would be padded to 1 KB and cost the third
-      * CTA per SM): slots and barriers all live in the dynamic allocation */
+     constexpr int NB = G + 1;
+     /* no static shared memory (it would be padded to 1 KB and cost a CTA per
+      * SM): slots, barriers and counters all live in the dynamic allocation */
      extern __shared__ __align__(1024) unsigned char gb_smem[];
      const int tb = P.tb, cb = ct_cb(tb);
      const int mask = cb >= 16 ? 7 : cb == 8 ? 3 : cb == 4 ? 1 : 0;
-     /* slots on 1024-byte boundaries (the swizzle pattern's period) */
      unsigned char *base = (unsigned char *)(((unsigned long long)gb_smem + 1023) & ~1023ull);
-     const int sb = (ct_slot_bytes(N, tb) + 1023) & ~1023;
-     unsigned char *const s0 = base, *const s1 = base + sb;
-     unsigned long long *const bar = (unsigned long long *)(s1 + ((ct_slot_bytes(N, tb) + 15) & ~15));
-     const int tl = threadIdx.x / T;
-     const int tid = threadIdx.x - tl * T;
-     const C *__restrict__ tw = (const C *)P.tw;
+     unsigned long long *const full = (unsigned long long *)(base + ct_slot_off(N, tb, NB - 1) +
+                                                             ((ct_slot_bytes(N, tb) + 15) & ~15));
+     int *const issued = (int *)(full + NB), *const consumed = issued + NB;
+     const int GT = P.threads;
+     const int g = (int)threadIdx.x / GT;
+     const int gtid = (int)threadIdx.x - g * GT;
+     const int tl = gtid / T;
+     const int tid = gtid - tl * T;
+     const C *__restrict__ tw = (const C *)P.tw_stage;
+     const auto gs = group_barrier<G>(g, GT);
+     const long long stride = gridDim.x;
 
      if (threadIdx.x == 0) {
-          mbar_init(&bar[0], 1);
-          mbar_init(&bar[1], 1);
+#pragma unroll
+          for (int b = 0; b < NB; ++b) {
+               mbar_init(&full[b], 1);
+               issued[b] = 0;
+               consumed[b] = 0;
+          }
           mbar_fence_init();
      }
      __syncthreads();
-     const long long stride = gridDim.x;
-     long long blk = blockIdx.x;
-     if (threadIdx.x == 0 && blk < P.nblocks) ct_issue<N>(P, &tmap, blk, s0, &bar[0]);
-     unsigned parity = 0;
-
-     for (int it = 0; blk < P.nblocks; blk += stride, ++it) {
-          const int b = it & 1;
-          unsigned char *const cur = b ? s1 : s0;
-          const long long nxt = blk + stride;
-          const bool issued = nxt < P.nblocks;
-          if (threadIdx.x == 0 && issued) {
-               /* that slot's boxes may still be going out to global memory */
-               if (tstore) bulk_wait_read();
-               fence_proxy_async_smem();
-               ct_issue<N>(P, &tmap, nxt, b ? s0 : s1, &bar[b ^ 1]);
-          }
-          const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u, GB_WAIT_NS);
-          if (!__syncthreads_and(ok)) {
-               if (threadIdx.x == 0) {
-                    if (issued) mbar_wait(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u, GB_WAIT_NS);
-                    if (P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
-               }
-               return;
-          }
-          parity ^= 1u << b;
-
-          const tile_t tile = tile_of(P, blk);
-          const long long v = tile.v0 + tl;
-          const bool valid = v < P.vn[0];
-          /* element j of column tl: box tl / cb, row j, chunk-swizzled */
-          const int colbase = (tl / cb) * N * cb * 8 + (tl % cb) * 8;
-          C x[E];
+     if (threadIdx.x == 0) {
 #pragma unroll
-          for (int e = 0; e < E; ++e) {
-               const int o = colbase + (tid + T * e) * cb * 8;
-               x[e] = *(const C *)(cur + ct_swz(o, mask));
+          for (int b = 0; b < NB; ++b) {
+               const long long blk = blockIdx.x + b * stride;
+               if (blk < P.nblocks) {
+                    ct_issue<N>(P, &tmap, blk, base + ct_slot_off(N, tb, b), &full[b]);
+                    issued[b] = 1;
+               }
           }
-          __syncthreads();
+     }
+
+     for (int i = g;; i += G) {
+          const long long blk = blockIdx.x + (long long)i * stride;
+          if (blk >= P.nblocks) break;
+          const int b = i % NB;
+          unsigned char *const cur = base + ct_slot_off(N, tb, b);
+          /* the slot's load for this tile exists (issued by the group done
+           * with the slot's previous tile) before its phase is waited on */
+          bool ok = true;
+          if (gtid == 0) {
+               const volatile int *iss = &issued[b];
+               const int need = i / NB + 1;
+               unsigned long long t0 = 0;
+               for (unsigned it = 0; *iss < need; ++it) {
+                    if (it == 0) t0 = globaltimer_ns();
+                    else if ((it & 63) == 0 && globaltimer_ns() - t0 > GB_WAIT_NS) {
+                         ok = false;
+                         break;
+                    }
+               }
+          }
+          if (!sync_and(gs, ok) || !sync_and(gs, mbar_wait(&full[b], (unsigned)((i / NB) & 1), GB_WAIT_NS))) {
+               if (gtid == 0 && P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
+               break;
+          }
+          if (gtid == 0) atomicAdd(&consumed[b], 1);
+
+          /* element j of column tl: box tl / cb, row j, chunk-swizzled */
+          C x[E];
+          {
+               const int colbase = (tl / cb) * N * cb * 8 + (tl % cb) * 8;
+#pragma unroll
+               for (int e = 0; e < E; ++e) {
+                    const int o = colbase + (tid + T * e) * cb * 8;
+                    x[e] = *(const C *)(cur + ct_swz(o, mask));
+               }
+          }
+          gs();
           C *const sm = (C *)cur;
           C *const smt = sm + tl * SMS;
-          reg_stages<C, N, DIR, 1>(x, tid, smt, tw);
+          reg_stages<C, N, DIR, 1>(x, tid, smt, tw, gs);
+          const tile_t tile = tile_of(P, blk);
+          const long long v = tile.v0 + tl;
+          const long long nxt = blk + NB * stride;
           if (P.post_N) {
                apply_post_twiddles<C, E, T>(P, P.post_vdim ? tile.vpost : v, tid, x);
           }
           if (P.store_mode == GB_MOVE_DIRECT) {
-               if (valid) {
+               /* the slot is free once every thread of the group is past the
+                * barrier after its last read (inside the stages) */
+               if (gtid == 0 && nxt < P.nblocks) {
+                    fence_proxy_async_smem();
+                    ct_issue<N>(P, &tmap, nxt, cur, &full[b]);
+                    atomicAdd(&issued[b], 1);
+               }
+               if (v < P.vn[0]) {
                     const long long bo = tile.bo + v * P.vos[0];
 #pragma unroll
                     for (int e = 0; e < E; ++e) io<C>::stc(out, bo, tid + T * e, P.os, x[e]);
                }
           } else if (tstore) {
                /* column tiles out through the output tensor map: the results
-                * take the boxes' swizzled layout in the slot, and one thread
-                * hands the boxes to the TMA engine */
-               /* layout constants recomputed from the launch parameters
-                * rather than kept live across the stages */
+                * take the boxes' swizzled layout in the slot, and the group's
+                * leader hands the boxes to the TMA engine, waits until they
+                * have been read out of the slot, and refills it */
                const int cbs = ct_cb(P.tb);
                const int ms = cbs >= 16 ? 7 : cbs == 8 ? 3 : cbs == 4 ? 1 : 0;
                const int cbase = (tl / cbs) * N * cbs * 8 + (tl % cbs) * 8;
@@ -221,8 +262,8 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
                     *(C *)(cur + ct_swz(o, ms)) = x[e];
                }
                fence_proxy_async_smem();
-               __syncthreads();
-               if (threadIdx.x == 0) {
+               gs();
+               if (gtid == 0) {
                     constexpr int ROWS = N < 256 ? N : 256;
                     int c[5] = {0, 0, 0, 0, 0};
                     ct_coords(P, blk, c);
@@ -234,36 +275,62 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
                               tma_tile_store(&omap, 1 + P.nv, c, cur + (k * N + r * ROWS) * cbs * 8);
                          }
                     bulk_commit();
+                    if (nxt < P.nblocks) {
+                         bulk_wait_read();
+                         fence_proxy_async_smem();
+                         ct_issue<N>(P, &tmap, nxt, cur, &full[b]);
+                         atomicAdd(&issued[b], 1);
+                    }
                }
           } else {
+               /* plain column stores through the slot (one group per CTA: the
+                * launch runs this case with G = 1) */
 #pragma unroll
                for (int e = 0; e < E; ++e) smt[pad_for(N, tid + T * e)] = x[e];
-               __syncthreads();
+               gs();
                coop_store<C, true, false>(P, out, sm, SMS, tile, N, P.store_mode, N);
+               gs();
+               if (gtid == 0 && nxt < P.nblocks) {
+                    fence_proxy_async_smem();
+                    ct_issue<N>(P, &tmap, nxt, cur, &full[b]);
+                    atomicAdd(&issued[b], 1);
+               }
           }
-          __syncthreads();   /* the slot is the target of a later tile's boxes */
      }
-     if (tstore && threadIdx.x == 0) bulk_wait_all();
+     /* each leader's stores complete before the CTA ends; a group that gave
+      * up may leave loads in flight: wait (bounded) for them */
+     if (tstore && gtid == 0) bulk_wait_all();
+     __syncthreads();
+     if (threadIdx.x == 0) {
+#pragma unroll
+          for (int b = 0; b < NB; ++b)
+               if (issued[b] > consumed[b]) mbar_wait(&full[b], (unsigned)((issued[b] - 1) & 1), GB_WAIT_NS);
+     }
 }
 
 template <int L>
-static const void *ct_lookup(int logn, int dir)
+static const void *ct_lookup(int logn, int dir, int groups)
 {
      if constexpr (L > 11) return 0;
      else {
-          if (logn == L) return dir < 0 ? (const void *)k_cols_tma<L, -1> : (const void *)k_cols_tma<L, 1>;
-          return ct_lookup<L + 1>(logn, dir);
+          if (logn == L) {
+               if (groups == 2) return dir < 0 ? (const void *)k_cols_tma<L, -1, 2> : (const void *)k_cols_tma<L, 1, 2>;
+               if (groups == 1) return dir < 0 ? (const void *)k_cols_tma<L, -1, 1> : (const void *)k_cols_tma<L, 1, 1>;
+               return 0;
+          }
+          return ct_lookup<L + 1>(logn, dir, groups);
      }
 }
 
 } /* namespace gb */
 
-extern "C" const void *gb_cols_tma_kernel(int logn, int dir) { return gb::ct_lookup<4>(logn, dir); }
+extern "C" const void *gb_cols_tma_kernel(int logn, int dir, int groups) { return gb::ct_lookup<4>(logn, dir, groups); }
 
-/* Shared memory of a k_cols_tma CTA: two slots on 1024-byte boundaries, the
- * two mbarriers, and the slack to align the first slot. */
-extern "C" int gb_cols_tma_smem(int nfft, int tb)
+/* Shared memory of a k_cols_tma CTA of g groups: g + 1 slots on 1024-byte
+ * boundaries, the mbarriers and load counters, and the slack to align the
+ * first slot. */
+extern "C" int gb_cols_tma_smem(int nfft, int tb, int groups)
 {
-     const int sb = (gb::ct_slot_bytes(nfft, tb) + 1023) & ~1023;
-     return sb + ((gb::ct_slot_bytes(nfft, tb) + 15) & ~15) + 16 + 1024;
+     return gb::ct_slot_off(nfft, tb, groups) + ((gb::ct_slot_bytes(nfft, tb) + 15) & ~15) + (groups + 1) * 16 +
+            1024;
 }

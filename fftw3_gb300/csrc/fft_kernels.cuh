@@ -160,7 +160,14 @@ __device__ __forceinline__ void apply_post_twiddles(const gb_pass &P, long long 
           for (int e = 0; e < E; ++e) x[e] = cmul(x[e], post_twiddle<C>(P, v * (long long)(tid + T * e)));
      } else {
           const long long s = v * T;
-          const C a = post_twiddle<C>(P, v * tid);
+          C a;
+          if (P.post_rows && v < P.post_rows_v) {
+               /* one correctly rounded entry, read coalesced across the lanes */
+               a = __ldg((const C *)P.post_rows + v * T + tid);
+               if (P.sign > 0) a.y = -a.y;
+          } else {
+               a = post_twiddle<C>(P, v * tid);
+          }
           const C w1 = post_twiddle<C>(P, s), w2 = post_twiddle<C>(P, 2 * s), w4 = post_twiddle<C>(P, 4 * s),
                   w8 = post_twiddle<C>(P, 8 * s);
           const C b[4] = {a, cmul(a, w1), cmul(a, w2), cmul(a, cmul(w1, w2))};
@@ -334,6 +341,41 @@ __device__ __forceinline__ void apply_twiddles(C *v, const C *__restrict__ tw, i
      }
 }
 
+/* Offset of stage NS's rows in the stage twiddle table of N (gb_pass.tw_stage):
+ * four rows of NS entries for every earlier twiddled stage. */
+__host__ __device__ constexpr int stage_tw_off(int N, int NS)
+{
+     int off = 0;
+     for (int s = reg_r0(N); s < NS; s *= 16) off += 4 * s;
+     return off;
+}
+__host__ __device__ constexpr int stage_tw_len(int N)
+{
+     int len = 0;
+     if (N >= 32)
+          for (int s = reg_r0(N); s * 16 <= N; s *= 16) len += 4 * s;
+     return len;
+}
+
+/* Twiddles of one radix-16 butterfly at position k of a stage of span NS,
+ * from that stage's rows of the stage table (tws points at them):
+ * W^(k m), m = N / (16 NS), for the powers 1, 2, 4, 8 (rows 0..3, read
+ * with consecutive k on consecutive lanes: coalesced), the other powers as
+ * products of at most two read or derived factors, as in apply_twiddles. */
+template <int DIR, typename C>
+__device__ __forceinline__ void apply_stage_twiddles16(C *v, const C *__restrict__ tws, int k, int NS)
+{
+     const C w1 = twid<DIR>(tws, k), w2 = twid<DIR>(tws, NS + k), w4 = twid<DIR>(tws, 2 * NS + k),
+             w8 = twid<DIR>(tws, 3 * NS + k);
+     const C w3 = cmul(w1, w2), w12 = cmul(w8, w4);
+     v[1] = cmul(v[1], w1); v[2] = cmul(v[2], w2); v[3] = cmul(v[3], w3); v[4] = cmul(v[4], w4);
+     v[5] = cmul(v[5], cmul(w4, w1)); v[6] = cmul(v[6], cmul(w4, w2)); v[7] = cmul(v[7], cmul(w4, w3));
+     v[8] = cmul(v[8], w8);
+     v[9] = cmul(v[9], cmul(w8, w1)); v[10] = cmul(v[10], cmul(w8, w2)); v[11] = cmul(v[11], cmul(w8, w3));
+     v[12] = cmul(v[12], w12);
+     v[13] = cmul(v[13], cmul(w12, w1)); v[14] = cmul(v[14], cmul(w12, w2)); v[15] = cmul(v[15], cmul(w12, w3));
+}
+
 /* x[e] = element tid + T*e of the swizzled transform in shared memory */
 template <typename C, int N>
 __device__ __forceinline__ void reg_gather(C (&x)[reg_e(N)], int tid, const C *smt)
@@ -378,8 +420,23 @@ __device__ __forceinline__ bool group_and(unsigned id, unsigned n, bool v)
      return r != 0;
 }
 
+/* The stages of one transform of N points held E per thread; tws is the
+ * stage twiddle table of N (gb_pass.tw_stage). */
+/* barrier + AND of v over the threads a sync object stands for */
+__device__ __forceinline__ bool sync_and(const cta_sync &, bool v) { return __syncthreads_and(v); }
+__device__ __forceinline__ bool sync_and(const group_sync &s, bool v) { return group_and(s.id, s.n, v); }
+
+/* The barrier of compute group g (of gt threads) in a CTA of G groups: the
+ * CTA-wide barrier when there is one group (any thread count), else named
+ * barrier 1 + g (gt a multiple of 32: a named barrier counts whole warps). */
+template <int G> __device__ __forceinline__ auto group_barrier(int g, int gt)
+{
+     if constexpr (G == 1) return cta_sync();
+     else return group_sync{(unsigned)(1 + g), (unsigned)gt};
+}
+
 template <typename C, int N, int DIR, int NS, typename S = cta_sync>
-__device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, const C *__restrict__ tw,
+__device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, const C *__restrict__ tws,
                                            const S &sync = S())
 {
      constexpr int E = reg_e(N);
@@ -397,7 +454,10 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
           C v[RAD];
 #pragma unroll
           for (int r = 0; r < RAD; ++r) v[r] = x[b + r * B];
-          if (NS > 1) apply_twiddles<DIR, RAD>(v, tw, k * (N / (NS * RAD)));
+          if constexpr (NS > 1) {
+               static_assert(RAD == 16, "twiddled stages are radix 16");
+               apply_stage_twiddles16<DIR>(v, tws + stage_tw_off(N, NS), k, NS);
+          }
           bfly<RAD, DIR>::run(v);
           if (LAST) {
 #pragma unroll
@@ -422,7 +482,7 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
           sync();
           reg_gather<C, N>(x, tid, smt);
           sync();
-          reg_stages<C, N, DIR, NS * RAD, S>(x, tid, smt, tw, sync);
+          reg_stages<C, N, DIR, NS * RAD, S>(x, tid, smt, tws, sync);
      }
 }
 
@@ -457,7 +517,7 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
      const int tl = threadIdx.x / T;
      const int tid = threadIdx.x - tl * T;
      C *smt = sm + tl * SMS;
-     const C *__restrict__ tw = (const C *)P.tw;
+     const C *__restrict__ tw = (const C *)P.tw_stage;
 
      for (long long blk = blockIdx.x; blk < P.nblocks; blk += gridDim.x) {
           const tile_t tile = tile_of(P, blk);
@@ -632,7 +692,9 @@ __global__ void __launch_bounds__(reg_maxthreads(1 << LOGN), reg_minblocks(1 << 
  * in buffer i mod (G + 1).  The TMA engine copies each tile into its buffer
  * (cp.async.bulk, completion on the buffer's mbarrier): the first G + 1
  * tiles at start, and tile i + G + 1 as soon as the group that transformed
- * tile i has last read that buffer.  So while every group transforms a
+ * tile i has last read that buffer.  A count of the loads issued per buffer
+ * lets a group that is ahead wait until its tile's load exists before it
+ * waits on the barrier's phase.  So while every group transforms a
  * tile, one more tile is on its way, and a group finds its next tile
  * already resident.  Results are stored straight from registers.
  * One group per CTA (two buffers) leaves each thread 85 registers and puts
@@ -697,8 +759,8 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
      const int tid = gtid - tl * T;
      const int tile_elems = P.tb * SMS;
      C *const base = (C *)gb_smem;
-     const C *__restrict__ tw = (const C *)P.tw;
-     const group_sync gs = {(unsigned)(1 + g), (unsigned)GT};
+     const C *__restrict__ tw = (const C *)P.tw_stage;
+     const auto gs = group_barrier<G>(g, GT);
      const long long stride = gridDim.x;
 
      if (threadIdx.x == 0) {
@@ -726,9 +788,27 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
           const long long blk = blockIdx.x + (long long)i * stride;
           if (blk >= P.nblocks) break;
           const int b = i % NB;
-          const unsigned parity = (unsigned)((i / NB) & 1);
           C *const cur = base + b * tile_elems;
-          if (!group_and(gs.id, gs.n, mbar_wait(&full[b], parity, GB_WAIT_NS))) {
+          /* The load of tile i is buffer b's load number i / NB; another group
+           * issues it once it is done with tile i - NB.  A parity wait tells
+           * apart only two consecutive phases, so the group's leader first makes
+           * sure that load was issued (buffer b's earlier load then has
+           * completed, and the barrier's current phase is this tile's); then
+           * every thread of the group waits for its bytes. */
+          bool ok = true;
+          if (gtid == 0) {
+               const volatile int *iss = &issued[b];
+               const int need = i / NB + 1;
+               unsigned long long t0 = 0;
+               for (unsigned it = 0; *iss < need; ++it) {
+                    if (it == 0) t0 = globaltimer_ns();
+                    else if ((it & 63) == 0 && globaltimer_ns() - t0 > GB_WAIT_NS) {
+                         ok = false;
+                         break;
+                    }
+               }
+          }
+          if (!sync_and(gs, ok) || !sync_and(gs, mbar_wait(&full[b], (unsigned)((i / NB) & 1), GB_WAIT_NS))) {
                /* the copy never completed: report and leave (the copies still
                 * in flight are drained below) */
                if (gtid == 0 && P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
@@ -742,7 +822,7 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
                for (int e = 0; e < E; ++e) x[e] = s0[T * e];
           }
           gs();
-          reg_stages<C, N, DIR, 1, group_sync>(x, tid, cur + tl * SMS, tw, gs);
+          reg_stages<C, N, DIR, 1>(x, tid, cur + tl * SMS, tw, gs);
           /* (the tile's indices are formed after the stages, which need every
            * register they can get) */
           C *smt = cur + tl * SMS;

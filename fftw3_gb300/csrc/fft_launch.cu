@@ -22,7 +22,7 @@ extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
 extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir, int groups);
 extern "C" const void *gb_tma_kernel_d(int logn, int kind, int dir, int groups);
 extern "C" const void *gb_tc_kernel(int nfft, int dir);
-extern "C" const void *gb_cols_tma_kernel(int logn, int dir);
+extern "C" const void *gb_cols_tma_kernel(int logn, int dir, int groups);
 extern "C" int gb_tc_smem(int nfft);
 
 namespace gb {
@@ -36,6 +36,41 @@ __global__ void k_twiddles(C *dst, long long n, long long count, long long mul)
           double c, s;
           long long m = (long long)(((unsigned long long)j * (unsigned long long)mul) % (unsigned long long)n);
           cexp_fp64(m, n, -1, &c, &s);
+          dst[j] = mk<C>((R)c, (R)s);
+     }
+}
+
+/* Stage twiddle table of a power-of-two length N (layout of gb_pass.tw_stage):
+ * entry (stage NS, row q, k) = exp(-2 pi i k (N / (16 NS)) 2^q / N), FP64
+ * with the exact octant reduction, rounded once. */
+template <typename C>
+__global__ void k_stage_twiddles(C *dst, int N, int len)
+{
+     typedef typename real_of<C>::T R;
+     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < len; j += gridDim.x * blockDim.x) {
+          int ns = reg_r0(N), idx = j;
+          while (idx >= 4 * ns) {
+               idx -= 4 * ns;
+               ns *= 16;
+          }
+          const int q = idx / ns, k = idx - q * ns;
+          const long long m = ((long long)k * (N / (16 * ns)) << q) % N;
+          double c, s;
+          cexp_fp64(m, N, -1, &c, &s);
+          dst[j] = mk<C>((R)c, (R)s);
+     }
+}
+
+/* Rows of the four-step twiddle: entry v T + t = exp(-2 pi i v t / N). */
+template <typename C>
+__global__ void k_post_rows(C *dst, long long N, int T, long long count)
+{
+     typedef typename real_of<C>::T R;
+     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < count;
+          j += (long long)gridDim.x * blockDim.x) {
+          const long long v = j / T, t = j - v * T;
+          double c, s;
+          cexp_fp64((v * t) % N, N, -1, &c, &s);
           dst[j] = mk<C>((R)c, (R)s);
      }
 }
@@ -192,6 +227,14 @@ static int gb_check(cudaError_t e, const char *what)
      return 0;
 }
 
+extern "C" int gb_device_smem_per_sm(void)
+{
+     int dev = 0, v = 0;
+     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+     if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess) return 0;
+     return v;
+}
+
 extern "C" int gb_device_max_smem(void)
 {
      int dev = 0, v = 0;
@@ -266,6 +309,31 @@ extern "C" int gb_twiddles(void *dst, int prec, long long n, long long count, lo
      return gb_check(cudaGetLastError(), "twiddle generation");
 }
 
+extern "C" int gb_stage_twiddles(void *dst, int prec, int nfft, void *stream)
+{
+     const int len = stage_tw_len(nfft);
+     int blocks = (len + 255) / 256;
+     if (len != gb_stage_tw_len(nfft)) {
+          snprintf(gb_errbuf, sizeof gb_errbuf, "stage twiddle layouts of host and device disagree");
+          return -1;
+     }
+     if (len == 0) return 0;
+     if (prec == 4) k_stage_twiddles<float2><<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, nfft, len);
+     else k_stage_twiddles<double2><<<blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, nfft, len);
+     return gb_check(cudaGetLastError(), "stage twiddle generation");
+}
+
+extern "C" int gb_post_rows(void *dst, int prec, long long N, int T, long long rows, void *stream)
+{
+     const long long count = rows * T;
+     long long blocks = (count + 255) / 256;
+     if (blocks > 4096) blocks = 4096;
+     if (count <= 0) return 0;
+     if (prec == 4) k_post_rows<float2><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, N, T, count);
+     else k_post_rows<double2><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, N, T, count);
+     return gb_check(cudaGetLastError(), "four-step twiddle rows");
+}
+
 extern "C" int gb_chirp(void *dst, int prec, long long n, int sign, void *stream)
 {
      int blocks = (int)((n + 255) / 256);
@@ -303,7 +371,7 @@ static const void *pick_kernel(const gb_pass *p)
      if (p->variant == GB_VAR_TMA_COLS) {
           int logn = 0;
           while ((1 << logn) < p->nfft) ++logn;
-          return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_cols_tma_kernel(logn, p->sign) : 0;
+          return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_cols_tma_kernel(logn, p->sign, p->groups) : 0;
      }
      if (p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA) {
           int logn = 0;
@@ -318,11 +386,11 @@ static const void *pick_kernel(const gb_pass *p)
      return p->prec == 4 ? (const void *)k_gen<float2> : (const void *)k_gen<double2>;
 }
 
-/* Threads of one CTA: a k_reg_tma CTA runs p->groups groups of p->threads
- * threads. */
+/* Threads of one CTA: a k_reg_tma or k_cols_tma CTA runs p->groups groups
+ * of p->threads threads. */
 static int cta_threads(const gb_pass *p)
 {
-     return p->variant == GB_VAR_TMA ? p->groups * p->threads : p->threads;
+     return (p->variant == GB_VAR_TMA || p->variant == GB_VAR_TMA_COLS) ? p->groups * p->threads : p->threads;
 }
 
 /* Number of CTAs launched for a pass: all tiles, capped; kernels stride over
@@ -342,11 +410,11 @@ static unsigned grid_of(const gb_pass *p, const void *fn)
                cudaGetLastError();
                per = 1;
           }
-          /* the calculator reports one CTA per SM for the tensor-core kernel,
-           * whose registers, shared memory and TMEM (64 columns) leave room for
-           * three; its CTAs never wait on one another, so a second wave is
-           * harmless if they cannot all be resident */
-          if (p->variant == GB_VAR_TC && per < 3) per = 3;
+          /* the calculator may report one CTA per SM for the tensor-core
+           * kernel, whose registers, shared memory and TMEM (64 columns) leave
+           * room for two; its CTAs never wait on one another, so a second wave
+           * is harmless if they cannot all be resident */
+          if (p->variant == GB_VAR_TC && per < 2) per = 2;
           if (per < 1) per = 1;
           if (g > (long long)per * sms) g = (long long)per * sms;
      }
@@ -423,7 +491,9 @@ static int cols_tma_ok(const gb_pass *p, const void *in)
      if (p->kind != GB_KIND_C2C || p->prec != 4 || p->load_mode != GB_MOVE_COLS) return 0;
      if (p->nfft < 16 || p->nfft > 2048 || p->tb < 2 || p->tb > 128 || (p->tb & (p->tb - 1)) || p->ltb < 0) return 0;
      if (p->threads != p->tb * T || p->threads > 256 || p->nv > 4) return 0;
-     if (p->smem < gb_cols_tma_smem(p->nfft, p->tb)) return 0;
+     if (p->groups < 1 || p->groups > 2 || (p->groups == 2 && p->threads % 32) ||
+         p->smem < gb_cols_tma_smem(p->nfft, p->tb, p->groups))
+          return 0;
      if ((uintptr_t)in % 16 || p->vis[0] != 1 || p->is <= 0 || (p->is * 8) % 16 || p->is * 8 >= (1LL << 40)) return 0;
      if (p->vn[0] >= (1LL << 31)) return 0;
      for (d = 1; d < p->nv; ++d)
@@ -501,7 +571,11 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
                     bad = "chirp missing";
                else if (p->pw == GB_PW_SPEC_MUL && !p->chirp_spec) bad = "chirp spectrum missing";
                else if (p->pw_chunks < 1 || p->threads != 256 || p->tb != 1) bad = "bad pointwise launch shape";
-          } else if (p->kind != GB_KIND_COPY && !p->tw) bad = "twiddle table missing";
+          } else if (p->kind != GB_KIND_COPY && (p->variant == GB_VAR_GEN || p->variant == GB_VAR_TC) && !p->tw)
+               bad = "twiddle table missing";
+          else if ((p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA || p->variant == GB_VAR_TMA_COLS ||
+                    p->variant == GB_VAR_TC) && p->kind != GB_KIND_COPY && stage_tw_len(p->nfft) > 0 && !p->tw_stage)
+               bad = "stage twiddle table missing";
           else if ((p->kind == GB_KIND_R2C || p->kind == GB_KIND_C2R) && p->n % 2 == 0 && !p->tw_half)
                bad = "half-length twiddle table missing";
           else if (p->kind == GB_KIND_BLUESTEIN && (!p->chirp || !p->chirp_spec)) bad = "chirp tables missing";
@@ -520,7 +594,8 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->post_N && (p->post_lS < 0 || (1LL << p->post_lS) != p->post_S || p->post_S * p->post_S < p->post_N))
                bad = "four-step twiddle table split is inconsistent";
           else if (p->variant == GB_VAR_REG && p->smem < p->tb * reg_sms(p->nfft) * 2 * p->prec) bad = "shared memory too small for the tile";
-          else if (p->variant == GB_VAR_TMA && (p->threads > tma_threads(p->nfft) || p->threads % 32 || p->is != 1 || p->os != 1 ||
+          else if (p->variant == GB_VAR_TMA && (p->threads > tma_threads(p->nfft) || (p->groups > 1 && p->threads % 32) ||
+                                                p->is != 1 || p->os != 1 ||
                                                 (p->kind != GB_KIND_C2C && p->kind != GB_KIND_R2C) ||
                                                 (p->kind == GB_KIND_R2C && p->n != 2 * p->nfft) ||
                                                 p->groups < 1 || p->groups > gb_tma_max_groups(p->prec) ||
@@ -531,10 +606,10 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->variant == GB_VAR_TMA_COLS && !cols_tma_ok(p, in))
                bad = "tensor-map column pass needs f32 c2c column tiles of 2..128 columns, 16..2048 points, even positive "
                      "strides, a 16-byte aligned input and two shared slots";
-          else if (p->variant == GB_VAR_TC && (p->prec != 4 || (p->nfft != 256 && p->nfft != 4096) ||
+          else if (p->variant == GB_VAR_TC && (p->prec != 4 || p->nfft < 256 || p->nfft > 4096 || (p->nfft & (p->nfft - 1)) ||
                                                p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||
                                                p->smem < gb_tc_smem(p->nfft) || (p->store_mode == GB_MOVE_DIRECT && p->os != 1)))
-               bad = "tensor-core pass needs f32 c2c of 256 or 4096 points, 256 threads";
+               bad = "tensor-core pass needs f32 c2c of 256 to 4096 points (a power of two), 256 threads";
           if (bad) {
                snprintf(gb_errbuf, sizeof gb_errbuf, "refused pass (kind %d nfft %d): %s", p->kind, p->nfft, bad);
                return -1;
@@ -569,6 +644,20 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           if (pv.smem > 48 * 1024 &&
               gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pv.smem),
                        "cudaFuncSetAttribute(max dynamic smem)"))
+               return -1;
+          p = &pv;
+     } else if (p->variant == GB_VAR_TMA_COLS && p->groups == 2 && p->store_mode != GB_MOVE_DIRECT && !tstore) {
+          /* plain column stores (no output tensor map) go through the slot
+           * with the CTA-wide tile walk: one group per CTA */
+          pv.groups = 1;
+          fn = pick_kernel(&pv);
+          if (!fn) return -1;
+          if (pv.smem > 48 * 1024 &&
+              (gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pv.smem),
+                        "cudaFuncSetAttribute(max dynamic smem)") ||
+               gb_check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared),
+                        "cudaFuncSetAttribute(shared memory carveout)")))
                return -1;
           p = &pv;
      }

@@ -19,7 +19,7 @@
  * so nothing is allocated when it runs.  The array's size is the limit:
  * n * howmany <= FFTWF_GB300_NOALLOC_MAX_POINTS (2^21 complex floats,
  * 16 MiB), and every GPU the entry point runs on holds the array (16 MiB +
- * 48.25 KiB of status word and twiddle tables) until the process exits.
+ * 30.75 KiB of status word and twiddle tables) until the process exits.
  *
  * Set-up: the first call on each device, with that device current, looks up
  * the array's device address (cudaGetSymbolAddress), which can load this
@@ -37,7 +37,7 @@
 #include <cuda_runtime.h>
 #include <pthread.h>
 #include <stdio.h>
-#include "fft_device.cuh"
+#include "fft_kernels.cuh"
 #include "gb_types.h"
 #include "fftw3_gb300.h"
 
@@ -50,46 +50,63 @@ constexpr int kStatusWords = 32;     /* 256 bytes: the status word, padded so th
 constexpr int kMinLog = 12, kMaxLog = 21;
 constexpr int kMaxDevices = 64;
 
-/* Table entries one call of length 2^L needs: n1 + n2 + S + ceil(n / S),
- * with n1 = 2^(L/2), n2 = n / n1 and S the least power of two whose square
- * reaches n (the same split the entry point uses). */
+/* Table entries one call of length 2^L needs: the stage twiddles of n1 and
+ * of n2 (the layout the register kernels read), S + ceil(n / S) for the
+ * four-step twiddle, with n1 = 2^(L/2), n2 = n / n1 and S the least power
+ * of two whose square reaches n (the same split the entry point uses). */
 constexpr long long table_words(int L)
 {
-     return (1LL << (L / 2)) + (1LL << (L - L / 2)) + (1LL << ((L + 1) / 2)) +
+     return gb::stage_tw_len(1 << (L / 2)) + gb::stage_tw_len(1 << (L - L / 2)) + (1LL << ((L + 1) / 2)) +
             ((1LL << L) + (1LL << ((L + 1) / 2)) - 1) / (1LL << ((L + 1) / 2));
 }
 constexpr long long max_table_words(int L)
 {
      return L > kMaxLog ? 0 : (table_words(L) > max_table_words(L + 1) ? table_words(L) : max_table_words(L + 1));
 }
-/* 6144 entries (at n = 2^21: 1024 + 2048 + 2048 + 1024), rounded up to a
+/* 3888 entries (at n = 2^21: 272 + 544 + 2048 + 1024), rounded up to a
  * multiple of 32 so the scratch that follows stays 256-byte aligned */
 constexpr int kTableWords = (int)((max_table_words(kMinLog) + 31) / 32 * 32);
-static_assert(table_words(21) == 6144 && table_words(20) == 4096 && table_words(12) == 256,
+static_assert(table_words(21) == 3888 && table_words(20) == 2592,
               "table layout of the four-step split");
 static_assert(kTableWords >= max_table_words(kMinLog), "tables must not reach into the scratch region");
 
 }  // namespace
 
-/* [status (256 B)] [twiddles of n1] [twiddles of n2] [exp(-2 pi i j / n), j < S]
- * [exp(-2 pi i j S / n), j < ceil(n / S)] ... [scratch: n * howmany] */
+/* [status (256 B)] [stage twiddles of n1] [stage twiddles of n2]
+ * [exp(-2 pi i j / n), j < S] [exp(-2 pi i j S / n), j < ceil(n / S)] ...
+ * [scratch: n * howmany] */
 static __device__ __align__(256) float2 gb_noalloc_scratch[kStatusWords + kTableWords + kMaxPoints];
 
 static_assert(((kStatusWords + kTableWords) * sizeof(float2)) % 256 == 0, "scratch region must stay 256-byte aligned");
 
-/* The four tables of one call, in one launch: entry j of a table of period
- * N with multiplier mul is exp(-2 pi i (j * mul mod N) / N), rounded once
- * from FP64 (the same values the planner's tables hold). */
-__global__ void k_noalloc_tables(float2 *t, long long n1, long long n2, long long n, long long S)
+/* Stage-table entry j of a power-of-two length N (the layout of
+ * gb_pass.tw_stage): its exponent of exp(-2 pi i m / N). */
+__device__ long long stage_exponent(int N, int j)
 {
-     const long long H = (n + S - 1) / S, total = n1 + n2 + S + H;
+     int ns = gb::reg_r0(N);
+     while (j >= 4 * ns) {
+          j -= 4 * ns;
+          ns *= 16;
+     }
+     const int q = j / ns, k = j - q * ns;
+     return ((long long)k * (N / (16 * ns)) << q) % N;
+}
+
+/* The four tables of one call, in one launch, each entry exp(-2 pi i m / N)
+ * rounded once from FP64 (the same values the planner's tables hold): the
+ * stage tables of n1 and n2, then exp(-2 pi i j / n), j < S, and
+ * exp(-2 pi i j S / n), j < ceil(n / S). */
+__global__ void k_noalloc_tables(float2 *t, int n1, int n2, long long n, long long S)
+{
+     const long long l1 = gb::stage_tw_len(n1), l2 = gb::stage_tw_len(n2);
+     const long long H = (n + S - 1) / S, total = l1 + l2 + S + H;
      for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total;
           j += (long long)gridDim.x * blockDim.x) {
           long long m, N;
-          if (j < n1) { m = j; N = n1; }
-          else if (j < n1 + n2) { m = j - n1; N = n2; }
-          else if (j < n1 + n2 + S) { m = j - n1 - n2; N = n; }
-          else { m = ((j - n1 - n2 - S) * S) % n; N = n; }
+          if (j < l1) { m = stage_exponent(n1, (int)j); N = n1; }
+          else if (j < l1 + l2) { m = stage_exponent(n2, (int)(j - l1)); N = n2; }
+          else if (j < l1 + l2 + S) { m = j - l1 - l2; N = n; }
+          else { m = ((j - l1 - l2 - S) * S) % n; N = n; }
           double c, s;
           gb::cexp_fp64(m, N, -1, &c, &s);
           t[j] = make_float2((float)c, (float)s);
@@ -163,7 +180,8 @@ static void noalloc_pass(gb_pass *P, int nfft, int sign, long long is, long long
      P->vn[1] = howmany; P->vis[1] = dist; P->vos[1] = dist;
      P->ntiles0 = (vn0 + tb - 1) / tb;
      P->nblocks = P->ntiles0 * howmany;
-     P->tw = tw;
+     P->tw = tw;        /* (the register kernel reads only the stage table) */
+     P->tw_stage = tw;
 }
 
 extern "C" int fftwf_gb300_dft_1d_noalloc(int n, int howmany, const fftwf_complex *in, fftwf_complex *out, int sign,
@@ -198,17 +216,18 @@ extern "C" int fftwf_gb300_dft_1d_noalloc(int n, int howmany, const fftwf_comple
      long long S = 1;
      int lS = 0;
      while (S * S < n) { S <<= 1; ++lS; }
-     if (n1 + n2 + S + (n + S - 1) / S > kTableWords) {
+     const long long l1 = gb::stage_tw_len((int)n1), l2 = gb::stage_tw_len((int)n2);
+     if (l1 + l2 + S + (n + S - 1) / S > kTableWords) {
           gb_set_error("fftwf_gb300_dft_1d_noalloc: internal: tables of n = %d exceed the fixed table region", n);
           return -1;
      }
-     float2 *status = area, *tw1 = area + kStatusWords, *tw2 = tw1 + n1, *lo = tw2 + n2, *hi = lo + S;
+     float2 *status = area, *tw1 = area + kStatusWords, *tw2 = tw1 + l1, *lo = tw2 + l2, *hi = lo + S;
      float2 *mid = area + kStatusWords + kTableWords;
 
      cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), st);
      if (e == cudaSuccess) {
-          const long long total = n1 + n2 + S + (n + S - 1) / S;
-          k_noalloc_tables<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(tw1, n1, n2, n, S);
+          const long long total = l1 + l2 + S + (n + S - 1) / S;
+          k_noalloc_tables<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(tw1, (int)n1, (int)n2, n, S);
           e = cudaGetLastError();
      }
      if (e != cudaSuccess) {

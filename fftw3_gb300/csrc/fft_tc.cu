@@ -1,8 +1,12 @@
 /*
  * Tensor-core form of the radix-16 stages (tcgen05, split FP16, FP32
- * accumulation), for batched c2c of N = 256 and 4096 (16^2, 16^3) in any
- * layout (rows, adjacent columns, or the two passes of a 65536 = 256 x 256
- * four-step with its W_N^(n2 k1) twiddle).
+ * accumulation), for batched c2c of N = 256 .. 4096 in any layout (rows,
+ * adjacent columns, or the two passes of a 65536 = 256 x 256 four-step with
+ * its W_N^(n2 k1) twiddle).  N = 512, 1024, 2048 begin with one FP32 stage
+ * of radix 2, 4 or 8, as the register kernels do; every radix-16 stage is a
+ * GEMM.  Row tiles of aligned transforms are copied in by the TMA engine
+ * (cp.async.bulk) while the previous tile is transformed; two CTAs share an
+ * SM.
  *
  * Per stage, each of the CTA's 256 threads owns one radix-16 butterfly: it
  * gathers its 16 inputs from the shared-memory copy of the transform(s),
@@ -88,26 +92,50 @@ __device__ __forceinline__ float row_scale(float m)
      return ldexpf(1.f, 13 - e);
 }
 
+/* Bulk copy of one row tile (TB transforms of N points, unit stride, each
+ * transform 16-byte aligned) into pre, completion on bar (one thread). */
+template <int N>
+__device__ __forceinline__ void tc_prefetch(const gb_pass &P, const void *in, long long blk, float2 *pre,
+                                            unsigned long long *bar)
+{
+     const tile_t tl = tile_of(P, blk);
+     const long long rem = P.vn[0] - tl.v0;
+     const int ntr = rem < P.tb ? (int)rem : P.tb;
+     mbar_expect_tx(bar, (unsigned)(N * 8) * (unsigned)ntr);
+     for (int t = 0; t < ntr; ++t)
+          bulk_g2s(pre + t * N, (const float2 *)in + tl.bi + (tl.v0 + t) * P.vis[0], (unsigned)(N * 8), bar);
+}
+
 template <int LOGN, int DIR>
-__global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+__global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
 {
      constexpr int N = 1 << LOGN;
      constexpr int T = N / 16;           /* butterflies per transform per stage */
      constexpr int TB = 256 / T;         /* transforms per CTA */
-     constexpr int S = LOGN / 4;         /* radix-16 stages */
+     constexpr int R0 = reg_r0(N);       /* 16, or the radix of an FP32 first stage */
+     constexpr int NS0 = R0 == 16 ? 1 : R0;
+     constexpr int S = R0 == 16 ? LOGN / 4 : (LOGN - (R0 == 2 ? 1 : R0 == 4 ? 2 : 3)) / 4;   /* GEMM stages */
      extern __shared__ __align__(1024) unsigned char sm[];
      __shared__ uint32_t tbase;
-     __shared__ __align__(8) unsigned long long bar;
+     __shared__ __align__(8) unsigned long long bar, pbar;
      unsigned char *As = sm;                           /* 2 groups x 24 KB */
      unsigned char *Bs = sm + 2 * TC_A_BYTES;          /* 6 KB */
+     /* the next row tile, copied in by the TMA engine while this one is
+      * transformed (32 KB) */
+     float2 *pre = (float2 *)(sm + 2 * TC_A_BYTES + TC_B_BYTES);
      /* the tile (TB x N complex, 32 KB) shares the A operand's 48 KB: a
       * stage reads it into registers before A is written, and the MMA has
       * completed before the stage's results are written back */
      float2 *dat = (float2 *)As;
      const float2 *__restrict__ tw = (const float2 *)P.tw;
+     const float2 *__restrict__ tws = (const float2 *)P.tw_stage;
      const int m = threadIdx.x;          /* butterfly row */
      const int tl = m / T, j = m - tl * T;
      const int g = m >> 7;               /* 128-row MMA group */
+
+     /* row tiles of 16-byte aligned transforms arrive by bulk copy */
+     bool pref = P.load_mode == GB_MOVE_ROWS && P.is == 1 && ((unsigned long long)in & 15) == 0;
+     for (int d = 0; d < P.nv; ++d) pref = pref && (P.vis[d] & 1) == 0;
 
      /* B: real form of the 16-point DFT matrix for this direction, split
       * hi/lo: rows n < 16 give Re(Y[n]), rows 16.. give Im(Y[n-16]) */
@@ -126,42 +154,96 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
           *(__half *)(Bs + tc::kmajor_off(n, k, TC_LBO_B)) = (blk >= 4) ? cl : ch;
      }
      if (threadIdx.x < 32) tc::tmem_alloc(&tbase, 64);
-     if (threadIdx.x == 0) { mbar_init(&bar, 1); mbar_fence_init(); }
+     if (threadIdx.x == 0) {
+          mbar_init(&bar, 1);
+          mbar_init(&pbar, 1);
+          mbar_fence_init();
+     }
      tc::fence_before_sync();
      __syncthreads();
      tc::fence_after_sync();
      const uint32_t tmem = tbase;
-     unsigned phase = 0;
-     bool ok = true;
+     unsigned phase = 0, pphase = 0;
+     bool ok = true, pending = false;
+     if (pref && threadIdx.x == 0 && blockIdx.x < P.nblocks) tc_prefetch<N>(P, in, blockIdx.x, pre, &pbar);
+     pending = pref && blockIdx.x < P.nblocks;
 
      for (long long blk = blockIdx.x; blk < P.nblocks && ok; blk += gridDim.x) {
           const tile_t tile = tile_of(P, blk);
-          /* load TB transforms: element-fast for unit-stride rows, transform-
-           * fast for adjacent columns (four-step tiles, strided axes) */
-          for (int i = threadIdx.x; i < TB * N; i += blockDim.x) {
-               int t, e;
-               if (P.load_mode == GB_MOVE_COLS) { t = i & (TB - 1); e = i / TB; }
-               else { t = i / N; e = i - t * N; }
-               const long long v = tile.v0 + t;
-               dat[t * N + e] = (v < P.vn[0]) ? ((const float2 *)in)[tile.bi + v * P.vis[0] + e * P.is]
-                                              : make_float2(0.f, 0.f);
+          /* src: where the first stage reads the tile (the bulk-copied buffer,
+           * or the tile gathered into dat with plain loads) */
+          const float2 *src = dat;
+          if (pref) {
+               ok = __syncthreads_and(mbar_wait(&pbar, pphase, 2000000000ull));
+               if (!ok) break;   /* (the copy stays pending: waited for below) */
+               pphase ^= 1u;
+               pending = false;
+               src = pre;
+          } else {
+               /* element-fast for unit-stride rows, transform-fast for
+                * adjacent columns (four-step tiles, strided axes) */
+               for (int i = threadIdx.x; i < TB * N; i += blockDim.x) {
+                    int t, e;
+                    if (P.load_mode == GB_MOVE_COLS) { t = i & (TB - 1); e = i / TB; }
+                    else { t = i / N; e = i - t * N; }
+                    const long long v = tile.v0 + t;
+                    dat[t * N + e] = (v < P.vn[0]) ? ((const float2 *)in)[tile.bi + v * P.vis[0] + e * P.is]
+                                                   : make_float2(0.f, 0.f);
+               }
+               __syncthreads();
           }
-          __syncthreads();
-          int NS = 1;
+          if constexpr (R0 != 16) {
+               /* first stage of radix R0 in FP32 (as the register kernels'),
+                * from src into dat */
+               constexpr int B = 16 / R0;
+               float2 x[16];
+#pragma unroll
+               for (int e = 0; e < 16; ++e) x[e] = src[tl * N + j + e * T];
+               __syncthreads();
+#pragma unroll
+               for (int b = 0; b < B; ++b) {
+                    float2 v[R0];
+#pragma unroll
+                    for (int r = 0; r < R0; ++r) v[r] = x[b + r * B];
+                    bfly<R0, DIR>::run(v);
+                    const int jj = j + b * T;
+#pragma unroll
+                    for (int q = 0; q < R0; ++q) dat[tl * N + jj * R0 + q] = v[q];
+               }
+               if (src == pre && threadIdx.x == 0 && blk + gridDim.x < P.nblocks) {
+                    /* every thread has read the buffer (the barrier above) */
+                    fence_proxy_async_smem();
+                    tc_prefetch<N>(P, in, blk + gridDim.x, pre, &pbar);
+               }
+               pending = src == pre && blk + gridDim.x < P.nblocks;
+               src = dat;
+               __syncthreads();
+          }
+          int NS = NS0;
 #pragma unroll 1
           for (int s = 0; s < S; ++s) {
                float2 x[16];
+               const float2 *st = src + tl * N;
                float2 *dt = dat + tl * N;
 #pragma unroll
-               for (int r = 0; r < 16; ++r) x[r] = dt[j + r * T];
+               for (int r = 0; r < 16; ++r) x[r] = st[j + r * T];
                const int k = j & (NS - 1);
-               if (NS > 1) apply_twiddles<DIR, 16>(x, tw, k * (N / (NS * 16)));
+               if (NS > 1) apply_stage_twiddles16<DIR>(x, tws + stage_tw_off(N, NS), k, NS);
                float mx = 0.f;
 #pragma unroll
                for (int r = 0; r < 16; ++r) mx = fmaxf(mx, fmaxf(fabsf(x[r].x), fabsf(x[r].y)));
                const float sc = row_scale(mx), inv = 1.f / sc;
-               /* every thread has its x: the tile's memory becomes A */
+               /* every thread has its x: the tile's memory becomes A (and a
+                * bulk-copied tile's buffer is free for the next one) */
                __syncthreads();
+               if (src == pre) {
+                    if (threadIdx.x == 0 && blk + gridDim.x < P.nblocks) {
+                         fence_proxy_async_smem();
+                         tc_prefetch<N>(P, in, blk + gridDim.x, pre, &pbar);
+                    }
+                    pending = blk + gridDim.x < P.nblocks;
+                    src = dat;
+               }
                /* A row: [hi.re | hi.im | lo.re | lo.im | hi.re | hi.im] */
                {
                     __half hr[16], hi[16], lr[16], li[16];
@@ -177,13 +259,13 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
                     const int row = m & 127;
 #pragma unroll
                     for (int c = 0; c < 12; ++c) {   /* 12 chunks of 8 K-elements */
-                         const __half *src = (c < 2) ? hr + 8 * c : (c < 4) ? hi + 8 * (c - 2) : (c < 6) ? lr + 8 * (c - 4)
-                                           : (c < 8) ? li + 8 * (c - 6) : (c < 10) ? hr + 8 * (c - 8) : hi + 8 * (c - 10);
+                         const __half *hsrc = (c < 2) ? hr + 8 * c : (c < 4) ? hi + 8 * (c - 2) : (c < 6) ? lr + 8 * (c - 4)
+                                            : (c < 8) ? li + 8 * (c - 6) : (c < 10) ? hr + 8 * (c - 8) : hi + 8 * (c - 10);
                          uint4 pk;
-                         pk.x = (uint32_t)__half_as_ushort(src[0]) | ((uint32_t)__half_as_ushort(src[1]) << 16);
-                         pk.y = (uint32_t)__half_as_ushort(src[2]) | ((uint32_t)__half_as_ushort(src[3]) << 16);
-                         pk.z = (uint32_t)__half_as_ushort(src[4]) | ((uint32_t)__half_as_ushort(src[5]) << 16);
-                         pk.w = (uint32_t)__half_as_ushort(src[6]) | ((uint32_t)__half_as_ushort(src[7]) << 16);
+                         pk.x = (uint32_t)__half_as_ushort(hsrc[0]) | ((uint32_t)__half_as_ushort(hsrc[1]) << 16);
+                         pk.y = (uint32_t)__half_as_ushort(hsrc[2]) | ((uint32_t)__half_as_ushort(hsrc[3]) << 16);
+                         pk.z = (uint32_t)__half_as_ushort(hsrc[4]) | ((uint32_t)__half_as_ushort(hsrc[5]) << 16);
+                         pk.w = (uint32_t)__half_as_ushort(hsrc[6]) | ((uint32_t)__half_as_ushort(hsrc[7]) << 16);
                          *(uint4 *)(arow + tc::kmajor_off(row, 8 * c, TC_LBO_A)) = pk;
                     }
                }
@@ -253,6 +335,8 @@ __global__ void __launch_bounds__(256) k_tc_fft(const gb_pass P, const void *__r
           }
      }
      if (!ok && threadIdx.x == 0 && P.status) atomicExch(P.status, GB_STATUS_COPY_TIMEOUT);
+     /* a copy still in flight lands before the CTA's shared memory goes */
+     if (pending && threadIdx.x == 0) mbar_wait(&pbar, pphase, 2000000000ull);
      tc::fence_before_sync();
      __syncthreads();
      if (threadIdx.x < 32) tc::tmem_dealloc(tmem, 64);
@@ -264,17 +348,23 @@ using namespace gb;
 
 extern "C" int *gb_device_status_ptr(void);
 
-/* bytes of dynamic shared memory the tensor-core FFT needs */
+/* bytes of dynamic shared memory the tensor-core FFT needs: A (shared with
+ * the tile), B, and the buffer the next row tile is copied into */
 extern "C" int gb_tc_smem(int nfft)
 {
-     return (int)(2 * TC_A_BYTES + TC_B_BYTES) + 0 * nfft;
+     return (int)(2 * TC_A_BYTES + TC_B_BYTES) + 256 * 16 * 8 + 0 * nfft;
 }
 
 extern "C" const void *gb_tc_kernel(int nfft, int dir)
 {
-     if (nfft == 256) return dir < 0 ? (const void *)k_tc_fft<8, -1> : (const void *)k_tc_fft<8, 1>;
-     if (nfft == 4096) return dir < 0 ? (const void *)k_tc_fft<12, -1> : (const void *)k_tc_fft<12, 1>;
-     return 0;
+     switch (nfft) {
+     case 256: return dir < 0 ? (const void *)k_tc_fft<8, -1> : (const void *)k_tc_fft<8, 1>;
+     case 512: return dir < 0 ? (const void *)k_tc_fft<9, -1> : (const void *)k_tc_fft<9, 1>;
+     case 1024: return dir < 0 ? (const void *)k_tc_fft<10, -1> : (const void *)k_tc_fft<10, 1>;
+     case 2048: return dir < 0 ? (const void *)k_tc_fft<11, -1> : (const void *)k_tc_fft<11, 1>;
+     case 4096: return dir < 0 ? (const void *)k_tc_fft<12, -1> : (const void *)k_tc_fft<12, 1>;
+     default: return 0;
+     }
 }
 
 /* One-CTA GEMM through the tcgen05 path (device pointers): D = A . B^T,

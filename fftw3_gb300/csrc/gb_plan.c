@@ -63,6 +63,16 @@ int gb_cuda_ready(void)
  * library lock): 1 = do not use the bulk-copy fed persistent variant */
 static int cfg_no_tma = 0;
 
+/* shared memory of one SM (two CTAs of a persistent kernel must fit, each
+ * with the 1 KB the system reserves) */
+static int smem_sm(void)
+{
+     static int v = 0;
+     if (!v) v = (!gb_dry && gb_cuda_ready()) ? gb_device_smem_per_sm() : 233472;
+     if (!v) v = 233472;
+     return v;
+}
+
 static int smem_max(void)
 {
      static int v = 0;
@@ -110,6 +120,36 @@ const void *gb_table_twiddle(int prec, long long n, long long count, long long m
      if (!p || gb_dry) return p;
      if (gb_twiddles(p, prec, n, count, mul, 0) || cudaDeviceSynchronize() != cudaSuccess) {
           gb_set_error("twiddle generation failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     return p;
+}
+
+/* the radix-16 stage twiddles of a power-of-two nfft in the coalesced layout
+ * of gb_pass.tw_stage */
+const void *gb_table_stage_twiddle(int prec, int nfft)
+{
+     const int len = gb_stage_tw_len(nfft);
+     void *p = tab_find(prec, 5, nfft, 0, 0);
+     if (p) return p;
+     p = tab_add(prec, 5, nfft, 0, 0, (size_t)(len ? len : 1) * 2 * prec);
+     if (!p || gb_dry) return p;
+     if (gb_stage_twiddles(p, prec, nfft, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("stage twiddle generation failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     return p;
+}
+
+/* rows of the four-step twiddle W_N^(v t), v < rows, t < T (gb_pass.post_rows) */
+static const void *table_post_rows(int prec, long long N, int T, long long rows)
+{
+     void *p = tab_find(prec, 6, N, T, rows);
+     if (p) return p;
+     p = tab_add(prec, 6, N, T, rows, (size_t)(rows * T) * 2 * prec);
+     if (!p || gb_dry) return p;
+     if (gb_post_rows(p, prec, N, T, rows, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("four-step twiddle rows failed: %s", gb_last_cuda_error());
           return 0;
      }
      return p;
@@ -409,9 +449,23 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                while ((1 << l) < tb) ++l;
                t.ltb = ((1 << l) == tb) ? l : -1;
                t.variant = GB_VAR_TMA_COLS;
-               t.smem = gb_cols_tma_smem((int)nfft, tb);
+               /* one compute group over two slots, three CTAs per SM (measured
+                * faster than two groups over three slots on every column pass);
+                * FFTW_GB300_TMA_GROUPS=2 asks for two where they fit */
+               {
+                    const char *genv = getenv("FFTW_GB300_TMA_GROUPS");
+                    t.groups = (genv && atoi(genv) == 2) ? 2 : 1;
+               }
+               /* a group of two is whole warps (its named barrier counts warps) */
+               if (t.threads % 32) t.groups = 1;
+               t.smem = gb_cols_tma_smem((int)nfft, tb, t.groups);
+               if (t.smem > smax || 2LL * (t.smem + 1024) > smem_sm()) {
+                    t.groups = 1;
+                    t.smem = gb_cols_tma_smem((int)nfft, tb, 1);
+               }
                if (t.smem <= smax && gb_cols_tma_plan_ok(&t)) {
                     P->variant = GB_VAR_TMA_COLS;
+                    P->groups = t.groups;
                     P->smem = t.smem;
                }
           }
@@ -424,13 +478,15 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                const int ein = kind == GB_KIND_R2C ? prec : csize(prec);   /* bytes per input element */
                for (i = 0; i < nv; ++i)
                     if ((P->vis[i] * ein) % 16) ok = 0;
-               /* compute groups per CTA: two (four transforms in flight per SM
-                * over three buffers a CTA) where one transform needs 512 threads
-                * (nfft 8192), else one; FFTW_GB300_TMA_GROUPS overrides.  One
+               /* compute groups per CTA: two for the float 8192-point core (one
+                * CTA of 2 x 512 threads and three buffers an SM: two tiles in
+                * flight where one group has one), one elsewhere, where three
+                * one-group CTAs an SM measured faster (CTA-wide barriers, 85
+                * registers a thread); FFTW_GB300_TMA_GROUPS overrides.  One
                 * buffer per group and one more; keep two CTAs of two groups or
                 * three of one group per SM */
                const char *genv = getenv("FFTW_GB300_TMA_GROUPS");
-               int groups = (nfft >= 8192 && prec == 4) ? 2 : 1;
+               int groups = (prec == 4 && nfft == 8192) ? 2 : 1;
                if (genv && (atoi(genv) == 1 || atoi(genv) == 2)) groups = atoi(genv);
                if (groups > gb_tma_max_groups(prec)) groups = gb_tma_max_groups(prec);
                const int nbuf = groups + 1;
@@ -497,6 +553,10 @@ static int pass_tables(gb_pass *P)
      if (P->kind == GB_KIND_COPY) return 0;
      P->tw = gb_table_twiddle(prec, P->nfft, P->nfft, 1);
      if (!P->tw) return -1;
+     if (P->nfft >= 32 && (P->nfft & (P->nfft - 1)) == 0) {
+          P->tw_stage = gb_table_stage_twiddle(prec, P->nfft);
+          if (!P->tw_stage) return -1;
+     }
      if ((P->kind == GB_KIND_R2C || P->kind == GB_KIND_C2R) && P->n % 2 == 0) {
           P->tw_half = gb_table_twiddle(prec, P->n, P->n / 2 + 1, 1);
           if (!P->tw_half) return -1;
@@ -520,6 +580,14 @@ static int pass_tables(gb_pass *P)
           P->post_lo = gb_table_twiddle(prec, P->post_N, S, 1);
           P->post_hi = gb_table_twiddle(prec, P->post_N, (P->post_N + S - 1) / S, S);
           if (!P->post_lo || !P->post_hi) return -1;
+          /* the factor of each thread's first element as one table read per
+           * thread, coalesced (register kernels of 16 elements a thread) */
+          if (P->nfft >= 256 && (P->nfft & (P->nfft - 1)) == 0 && P->post_N % P->nfft == 0 &&
+              P->post_N / 16 <= (1LL << 24)) {
+               P->post_rows_v = P->post_N / P->nfft;
+               P->post_rows = table_post_rows(prec, P->post_N, P->nfft / 16, P->post_rows_v);
+               if (!P->post_rows) return -1;
+          }
      }
      return 0;
 }
@@ -550,12 +618,14 @@ static void count_ops(gb_plan *p, const gb_pass *P, long long howmany)
      p->mul += 0.4 * per * howmany;
 }
 
-/* The split-FP16 tensor-core form (FFTW_GB300_TENSOR_CORE): f32 unit-stride
- * c2c of 256 or 4096 points, 256 threads (one radix-16 butterfly each). */
+/* The split-FP16 tensor-core form (FFTW_GB300_TENSOR_CORE): f32 c2c passes of
+ * 256 to 4096 points (a power of two), 256 threads (one radix-16 butterfly
+ * each). */
 static void use_tensor_cores(gb_pass *P)
 {
      int i;
-     if (P->kind != GB_KIND_C2C || P->prec != 4 || (P->nfft != 256 && P->nfft != 4096)) return;
+     if (P->kind != GB_KIND_C2C || P->prec != 4 || P->nfft < 256 || P->nfft > 4096 || (P->nfft & (P->nfft - 1)))
+          return;
      if (gb_tc_smem(P->nfft) > smem_max()) return;
      P->variant = GB_VAR_TC;
      P->tb = 256 / (P->nfft / 16);
@@ -1030,12 +1100,14 @@ static void describe(gb_plan *p)
                                      "half-copy", "herm-ext", "real-part", "chirp-in-real", "chirp-in-herm",
                                      "chirp-out-half", "chirp-out-real"};
           off += snprintf(p->desc + off, sizeof p->desc - off,
-                          "\n  (pass %s%s%s n=%d nfft=%d %s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
+                          "\n  (pass %s%s%s n=%d nfft=%d %s%s tb=%d thr=%d smem=%d ld=%s st=%s is=%lld os=%lld v=%lld%s)",
                           kk[P->kind], P->kind == GB_KIND_POINTWISE ? ":" : "",
                           P->kind == GB_KIND_POINTWISE && P->pw >= 0 && P->pw <= GB_PW_CHIRP_OUT_REAL ? pw[P->pw] : "",
                           P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" :
                           P->variant == GB_VAR_TMA_COLS ? "cols-tma" :
-                          P->variant == GB_VAR_TC ? "tc-split-fp16" : "gen", P->tb,
+                          P->variant == GB_VAR_TC ? "tc-split-fp16" : "gen",
+                          (P->variant == GB_VAR_TMA || P->variant == GB_VAR_TMA_COLS) && P->groups == 2 ? " groups=2" : "",
+                          P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
                           P->vn[0], P->post_N ? " +twiddle" : "");
           if (off >= (int)sizeof p->desc) off = (int)sizeof p->desc - 1;   /* truncated */

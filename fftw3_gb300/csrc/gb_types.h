@@ -53,7 +53,7 @@ enum gb_variant {
      GB_VAR_REG = 0,   /* power-of-two length, register-resident Stockham stages of radix <= 16 */
      GB_VAR_GEN = 1,   /* any smooth length, shared-memory Stockham stages, runtime radix list */
      GB_VAR_TMA = 2,   /* as GB_VAR_REG, persistent CTAs fed by bulk async copies (unit-stride c2c) */
-     GB_VAR_TC = 3,    /* radix-16 stages as split-FP16 tcgen05 GEMMs (nfft 256 or 4096, f32, unit stride) */
+     GB_VAR_TC = 3,    /* radix-16 stages as split-FP16 tcgen05 GEMMs (f32 c2c, nfft a power of two 256..4096) */
      GB_VAR_TMA_COLS = 4   /* as GB_VAR_REG for f32 c2c column tiles, persistent CTAs fed by tensor-map TMA boxes */
 };
 
@@ -89,6 +89,12 @@ typedef struct gb_pass {
      int rad[GB_MAXRAD];
      /* device tables (owned by the plan) */
      const void *tw;      /* exp(-2 pi i j / nfft), j < nfft */
+     /* power-of-two nfft: the twiddles of the radix-16 stages, laid out so a
+      * warp's reads are coalesced.  For each stage with span NS (NS = r0,
+      * 16 r0, 256 r0, ... below nfft, r0 the first stage's radix), four rows
+      * of NS entries: row q holds exp(-2 pi i k (nfft / (16 NS)) 2^q / nfft),
+      * k < NS.  Stages follow one another (gb_stage_tw_len entries in all). */
+     const void *tw_stage;
      const void *tw_half; /* r2c/c2r: exp(-2 pi i k / n), k <= n/2 */
      /* four-step: multiply output k of the transform whose index along
       * vector dimension 0 is v by exp(sign 2 pi i v k / post_N).  The
@@ -100,6 +106,12 @@ typedef struct gb_pass {
      int ltb;             /* log2(tb) when tb is a power of two, else -1 */
      const void *post_lo;
      const void *post_hi;
+     /* power-of-two nfft >= 256 (16 elements a thread, T = nfft / 16 threads a
+      * transform): the factor of thread t of transform v, W(v t), read with
+      * consecutive t on consecutive lanes: row v of post_rows (post_rows_v
+      * rows of T entries exp(sign-free -2 pi i v t / post_N)); 0 when absent */
+     const void *post_rows;
+     long long post_rows_v;
      /* Bluestein: chirp w[k] (k < n) and the spectrum of the padded chirp / nfft */
      const void *chirp;
      const void *chirp_spec;   /* Bluestein: chirp spectrum; Rader: spectrum of omega / (n-1) */
@@ -143,6 +155,22 @@ static inline int gb_pad_mult(int nfft)
      return (r == 16 && nfft >= 256) ? 2 : 1;
 }
 static inline int gb_reg_sms(int nfft) { return (nfft + gb_pad_mult(nfft) * (nfft >> 4) + 3) & ~1; }
+/* first-stage radix of a power-of-two length in the register kernels */
+static inline int gb_reg_r0(int nfft)
+{
+     int r = nfft;
+     while (r > 16) r /= 16;
+     return r;
+}
+/* entries of the stage twiddle table of a power-of-two nfft (0 below 32) */
+static inline int gb_stage_tw_len(int nfft)
+{
+     int len = 0, ns;
+     if (nfft < 32) return 0;
+     for (ns = gb_reg_r0(nfft); ns * 16 <= nfft; ns *= 16) len += 4 * ns;
+     return len;
+}
+
 /* Most compute groups a k_reg_tma CTA can run (prec: bytes per real): two
  * for float (64 registers a thread), one for double, whose 16 elements a
  * thread already fill 64 registers.  A CTA of g groups of gb_pass.threads
@@ -156,7 +184,9 @@ int gb_launch_queue(const gb_qitem *items, int nitems, int *head, int *ctrs, int
 int gb_queue_grid(int prec, int threads, int smem);
 int gb_pass_configure(gb_pass *p, int max_smem_optin);
 int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream);
-int gb_cols_tma_smem(int nfft, int tb);
+int gb_stage_twiddles(void *dst, int prec, int nfft, void *stream);
+int gb_post_rows(void *dst, int prec, long long N, int T, long long rows, void *stream);
+int gb_cols_tma_smem(int nfft, int tb, int groups);
 #define GB_SPLIT_MAXD 32   /* dims of a split-array problem: vector + transform dims */
 /* split-array pack (pack != 0: re/im strided -> dense complex buf) and
  * unpack (dense complex buf -> re/im strided); n/s: nd dims, strides in
@@ -166,6 +196,7 @@ int gb_split_copy(int pack, int prec, int nd, const long long *n, const long lon
 int gb_cols_tma_plan_ok(const gb_pass *p);
 int gb_chirp(void *dst, int prec, long long n, int sign, void *stream);
 int gb_device_max_smem(void);
+int gb_device_smem_per_sm(void);
 const char *gb_last_cuda_error(void);
 long long gb_launch_count(void);
 void gb_count_launch(void);   /* one more kernel launched outside gb_launch_pass */

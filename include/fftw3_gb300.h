@@ -17,7 +17,7 @@ extern "C" {
 #endif
 
 /* Planner flag (a bit the reference leaves unused): run the radix-16 stages
- * of f32 unit-stride c2c plans of 256 or 4096 points on the tensor cores,
+ * of f32 c2c passes of 256 to 4096 points (a power of two) on the tensor cores,
  * as split-FP16 (hi + lo) DFT-matrix GEMMs with FP32 accumulation. */
 #define FFTW_GB300_TENSOR_CORE (1U << 28)
 
@@ -49,7 +49,7 @@ extern double fftw_gb300_fp64_fma_gflops(void);
  * implicit synchronisation).  It runs the two-pass (four-step) kernels of
  * a long 1D plan with their scratch and twiddle tables in one fixed device
  * array of the library, which every GPU it runs on holds until exit
- * (16 MiB + 48.25 KiB).  howmany contiguous transforms of length n at distance
+ * (16 MiB + 30.75 KiB).  howmany contiguous transforms of length n at distance
  * n; in and out are device arrays (they may be the same); n is a power of
  * two from 2^12 to 2^21 and n * howmany <= FFTWF_GB300_NOALLOC_MAX_POINTS,
  * else it returns -1 without launching.  Enqueues on cuda_stream and

@@ -41,14 +41,15 @@ def test_tc_gemm_selftest(lib, torch_tc, ks):
     assert lib_.fftw_gb300_device_status() == 0
 
 
-@pytest.mark.parametrize("n", [256, 4096, 65536])
+@pytest.mark.parametrize("n", [256, 512, 1024, 2048, 4096, 65536])
 @pytest.mark.parametrize("dist", ["normal", "loguniform"])
 @pytest.mark.parametrize("sign", [-1, 1])
 def test_tc_fft_parity(lib, torch_tc, restatement, n, dist, sign):
-    """1D batches; 65536 runs as two tensor-core passes of 256 (four-step)."""
+    """1D batches; 512, 1024 and 2048 begin with an FP32 stage of radix 2,
+    4 or 8; 65536 runs as two tensor-core passes of 256 (four-step)."""
     import fftw3_gb300 as g
     torch = torch_tc
-    hm = {256: 1024, 4096: 64, 65536: 4}[n]
+    hm = {256: 1024, 512: 512, 1024: 256, 2048: 129, 4096: 64, 65536: 4}[n]
     rng = np.random.default_rng(n + (sign > 0))
     if dist == "normal":
         x = rng.standard_normal(n * hm) + 1j * rng.standard_normal(n * hm)
@@ -68,6 +69,25 @@ def test_tc_fft_parity(lib, torch_tc, restatement, n, dist, sign):
     assert g.load().fftw_gb300_device_status() == 0
 
 
+def test_tc_2d_512(lib, torch_tc, restatement):
+    """2D 512 x 512 (the 3D workload's axis length): rows and columns in the
+    tensor-core form, each beginning with a radix-2 FP32 stage."""
+    import fftw3_gb300 as g
+    torch = torch_tc
+    shape = [512, 512]
+    rng = np.random.default_rng(512)
+    tot = 512 * 512 * 2
+    x = (rng.uniform(-1, 1, tot) + 1j * rng.uniform(-1, 1, tot)).astype(np.complex64)
+    xi = torch.from_numpy(x).cuda()
+    yo = torch.empty_like(xi)
+    p = g.plan_many_dft(shape, 2, xi.data_ptr(), yo.data_ptr(), -1, g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE, "f")
+    assert p.describe().count("tc-split-fp16") == 2
+    p.execute()
+    ref = restatement.c2c(x.astype(np.complex128), shape, -1, "d", nthreads=4)
+    assert rel_l2(yo.cpu().numpy(), ref) <= 1e-6
+    assert g.load().fftw_gb300_device_status() == 0
+
+
 def test_tc_multid_columns(lib, torch_tc, restatement):
     """2D 256 x 256: the column axis runs through the tensor-core kernel with
     column tiles (strided loads and stores)."""
@@ -83,3 +103,37 @@ def test_tc_multid_columns(lib, torch_tc, restatement):
     p.execute()
     ref = restatement.c2c(x.astype(np.complex128), shape, -1, "d", nthreads=4)
     assert rel_l2(yo.cpu().numpy(), ref) <= 1e-6
+
+
+@pytest.mark.parametrize("n", [256, 4096, 65536])
+def test_tc_fft_loguniform_large_batch(lib, torch_tc, restatement, n):
+    """The precision-form workload's log-uniform variant (re and im with
+    magnitudes 10^U[-3,3) and random signs, generated on the device) at 2^26
+    points per length: transforms spread over the whole batch against the
+    FP64 oracle, each within the float bound."""
+    import fftw3_gb300 as g
+    from conftest import rel_l2_f
+    torch = torch_tc
+    hm = (1 << 26) // n
+    gen = torch.Generator(device="cuda").manual_seed(n + 3)
+
+    def mag():
+        m = torch.pow(10.0, torch.rand(n * hm, device="cuda", generator=gen, dtype=torch.float64) * 6 - 3)
+        s = torch.randint(0, 2, (n * hm,), device="cuda", generator=gen).to(torch.float64) * 2 - 1
+        return (m * s).to(torch.float32)
+
+    x = torch.complex(mag(), mag())
+    y = torch.empty_like(x)
+    p = g.plan_many_dft([n], hm, x.data_ptr(), y.data_ptr(), -1, g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE, "f")
+    assert "tc-split-fp16" in p.describe()
+    p.execute()
+    torch.cuda.synchronize()
+    sel = np.linspace(0, hm - 1, 16).astype(int)
+    xs = x.view(hm, n).cpu().numpy()[sel]
+    ys = y.view(hm, n).cpu().numpy()[sel]
+    worst = 0.0
+    for a, b in zip(xs, ys):
+        err = rel_l2_f(b, restatement.c2c(a.astype(np.complex128), [n], -1, "d"))
+        worst = max(worst, err)
+    assert worst <= 1e-6, f"worst rel L2 {worst:.3e}"
+    assert g.load().fftw_gb300_device_status() == 0

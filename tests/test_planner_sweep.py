@@ -113,3 +113,33 @@ def test_split_sweep():
         else:
             p = g.plan_guru_split_dft_c2r(dims, hd, base, base + (1 << 34), base + (2 << 34), prec=prec)
         check(p)
+
+
+@pytest.mark.parametrize("groups", [None, "2"])
+def test_two_group_passes_are_whole_warps(lib, monkeypatch, groups):
+    """A persistent pass with two compute groups per CTA synchronises each
+    group with its own named barrier, which counts whole warps: every such
+    pass the planner emits has a thread count per group that is a multiple
+    of 32 (small column tiles keep one group and the CTA-wide barrier), by
+    default and when two groups are asked for everywhere."""
+    import re
+    import fftw3_gb300 as g
+    if groups:
+        monkeypatch.setenv("FFTW_GB300_TMA_GROUPS", groups)
+    g.set_dry_run(True)
+    try:
+        shapes = [[16, 16], [32, 16], [16, 64], [8, 8, 8], [64, 64], [128, 32], [512, 512, 512], [256, 256],
+                  [2048, 8], [16, 2048], [65536], [1 << 20], [4096], [256], [64], [2, 1024], [1024, 4], [8192]]
+        seen = 0
+        for shape in shapes:
+            for hm in (1, 3, 64):
+                for prec in ("f", "d"):
+                    p = g.plan_many_dft(shape, hm, 1 << 20, 1 << 24, -1, g.FFTW_ESTIMATE, prec)
+                    for line in p.describe().splitlines():
+                        m = re.search(r"(reg-tma|cols-tma)( groups=2)? tb=(\d+) thr=(\d+)", line)
+                        if m and m.group(2):
+                            seen += 1
+                            assert int(m.group(4)) % 32 == 0, (shape, hm, prec, line)
+        assert seen > 0
+    finally:
+        g.set_dry_run(False)
