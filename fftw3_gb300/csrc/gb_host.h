@@ -106,6 +106,7 @@ struct gb_plan {
      void *r2r_mid;             /* dense real intermediate between stages (rank > 1) */
      void *stream;              /* cudaStream_t; 0 = legacy default stream */
      int async;                 /* 1: execute does not wait for completion */
+     int tc_stages;             /* tensor-core GEMM stages the plan's passes hold (planning only) */
      int in_align, out_align;   /* alignment of the planning arrays (bytes, capped at 16) */
      double add, mul, fma;      /* operation counts */
      double measured_ms;        /* time of one execute measured by the tuner (0 if not measured) */

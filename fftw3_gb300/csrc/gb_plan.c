@@ -620,12 +620,21 @@ static void count_ops(gb_plan *p, const gb_pass *P, long long howmany)
 
 /* The split-FP16 tensor-core form (FFTW_GB300_TENSOR_CORE): f32 c2c passes of
  * 256 to 4096 points (a power of two), 256 threads (one radix-16 butterfly
- * each). */
-static void use_tensor_cores(gb_pass *P)
+ * each).  Each GEMM stage carries the hi + lo split's error (about four
+ * times a FP32 radix-16 stage's), so a plan takes the form for at most
+ * GB_TC_MAX_STAGES GEMM stages in all (measured: 4096 with 3 stages 6.5e-7,
+ * 65536 and 2^20 with 4 stages 8.7e-7 and 9.1e-7, 512^3 with 6 stages
+ * 1.3e-6 rel L2, beyond the float bound of 1e-6); later passes of a plan
+ * over that budget stay in the FP32 form. */
+#define GB_TC_MAX_STAGES 4
+static void use_tensor_cores(gb_plan *p, gb_pass *P)
 {
-     int i;
+     int i, stages;
      if (P->kind != GB_KIND_C2C || P->prec != 4 || P->nfft < 256 || P->nfft > 4096 || (P->nfft & (P->nfft - 1)))
           return;
+     stages = P->nfft == 4096 ? 3 : 2;
+     if (p->tc_stages + stages > GB_TC_MAX_STAGES) return;
+     p->tc_stages += stages;
      if (gb_tc_smem(P->nfft) > smem_max()) return;
      P->variant = GB_VAR_TC;
      P->tb = 256 / (P->nfft / 16);
@@ -786,7 +795,7 @@ static int add_fourstep_cols(builder *b, long long n, int sign, long long is, lo
      if (config_pass(&sa->pass, prec, GB_KIND_C2C, n1, sign, (n / n1) * is, nup, 2 + no, va, 0, 1)) { --p->nstep; return -1; }
      sa->pass.post_N = n;
      sa->pass.post_vdim = 1;
-     if (p->flags & GB_FLAG_TENSOR_CORE) use_tensor_cores(&sa->pass);
+     if (p->flags & GB_FLAG_TENSOR_CORE) use_tensor_cores(p, &sa->pass);
      if (pass_tables(&sa->pass)) { b->err = 1; return 0; }
      /* pass B */
      vb[0].n = nu; vb[0].is = 1; vb[0].os = v[u].os;
@@ -800,7 +809,7 @@ static int add_fourstep_cols(builder *b, long long n, int sign, long long is, lo
           p->nstep -= 2;
           return -1;
      }
-     if (p->flags & GB_FLAG_TENSOR_CORE) use_tensor_cores(&sb->pass);
+     if (p->flags & GB_FLAG_TENSOR_CORE) use_tensor_cores(p, &sb->pass);
      if (pass_tables(&sb->pass)) { b->err = 1; return 0; }
      count_ops(p, &sa->pass, outer * nu * (n / n1));
      count_ops(p, &sb->pass, outer * nu * n1);
@@ -870,7 +879,7 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           p->step[p->nstep++] = keep;
           s = &p->step[p->nstep - 1];
      }
-     if (rc == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
+     if (rc == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(p, &s->pass);
      if (rc == 0) {
           if (pass_tables(&s->pass)) { b->err = 1; return; }
           count_ops(p, &s->pass, howmany);
@@ -970,7 +979,7 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           if (na > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
           /* dim 0 stays n2: the twiddle W_n^(n2 k1) indexes it */
           r1 = config_pass(&s->pass, prec, GB_KIND_C2C, n1, sign, n2 * is, 1, na, va, 0, 1);
-          if (r1 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
+          if (r1 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(p, &s->pass);
           s->pass.post_N = n;
           if (r1 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass A config failed"); b->err = 1; return; }
           count_ops(p, &s->pass, howmany * n2);
@@ -988,7 +997,7 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           s->src = mid; s->dst = dst;
           if (nb > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
           r2 = config_pass(&s->pass, prec, GB_KIND_C2C, n2, sign, n1, n1 * os, nb, vb, 0, 1);
-          if (r2 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(&s->pass);
+          if (r2 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(p, &s->pass);
           if (r2 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass B config failed"); b->err = 1; return; }
           count_ops(p, &s->pass, howmany * n1);
           return;

@@ -137,3 +137,24 @@ def test_tc_fft_loguniform_large_batch(lib, torch_tc, restatement, n):
         worst = max(worst, err)
     assert worst <= 1e-6, f"worst rel L2 {worst:.3e}"
     assert g.load().fftw_gb300_device_status() == 0
+
+
+def test_tc_3d_stage_budget(lib, torch_tc, restatement):
+    """3D 256^3 in place: the tensor-core form takes passes until the plan
+    holds four GEMM stages (two axes here), the third axis stays FP32, and
+    the forward transform of the whole array stays within the float bound."""
+    import fftw3_gb300 as g
+    from conftest import rel_l2_f
+    torch = torch_tc
+    shape = [256, 256, 256]
+    tot = 256 ** 3
+    rng = np.random.default_rng(3)
+    x = (rng.uniform(-1, 1, tot) + 1j * rng.uniform(-1, 1, tot)).astype(np.complex64)
+    a = torch.from_numpy(x).cuda()
+    p = g.Plan(g.load().fftwf_plan_dft_3d(*shape, a.data_ptr(), a.data_ptr(), -1,
+                                          g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE), "f")
+    assert p.describe().count("tc-split-fp16") == 2 and len(p.passes()) == 3
+    p.execute()
+    ref = restatement.c2c(x.astype(np.complex128), shape, -1, "d", nthreads=8)
+    assert rel_l2_f(a.cpu().numpy(), ref) <= 1e-6
+    assert g.load().fftw_gb300_device_status() == 0
