@@ -341,30 +341,41 @@ __device__ __forceinline__ void apply_twiddles(C *v, const C *__restrict__ tw, i
      }
 }
 
-/* Offset of stage NS's rows in the stage twiddle table of N (gb_pass.tw_stage):
- * four rows of NS entries for every earlier twiddled stage. */
-__host__ __device__ constexpr int stage_tw_off(int N, int NS)
+/* Rows per stage of the stage twiddle table (gb_pass.tw_stage) for complex
+ * elements of csize bytes: four for float (powers 1, 2, 4, 8), fifteen for
+ * double (powers 1..15). */
+__host__ __device__ constexpr int stage_tw_rows(int csize) { return csize == 16 ? 15 : 4; }
+
+/* Offset of stage NS's rows in the stage twiddle table of N: rows of NS
+ * entries for every earlier twiddled stage. */
+__host__ __device__ constexpr int stage_tw_off(int N, int NS, int rows = 4)
 {
      int off = 0;
-     for (int s = reg_r0(N); s < NS; s *= 16) off += 4 * s;
+     for (int s = reg_r0(N); s < NS; s *= 16) off += rows * s;
      return off;
 }
-__host__ __device__ constexpr int stage_tw_len(int N)
+__host__ __device__ constexpr int stage_tw_len(int N, int rows = 4)
 {
      int len = 0;
      if (N >= 32)
-          for (int s = reg_r0(N); s * 16 <= N; s *= 16) len += 4 * s;
+          for (int s = reg_r0(N); s * 16 <= N; s *= 16) len += rows * s;
      return len;
 }
 
 /* Twiddles of one radix-16 butterfly at position k of a stage of span NS,
- * from that stage's rows of the stage table (tws points at them):
- * W^(k m), m = N / (16 NS), for the powers 1, 2, 4, 8 (rows 0..3, read
- * with consecutive k on consecutive lanes: coalesced), the other powers as
- * products of at most two read or derived factors, as in apply_twiddles. */
+ * from that stage's rows of the stage table (tws points at them), read with
+ * consecutive k on consecutive lanes (coalesced): W^(k m p), m = N / (16 NS).
+ * Double reads all fifteen powers (one rounding each, no FP64 products);
+ * float reads the powers 1, 2, 4, 8 and forms the others as products of at
+ * most two read or derived factors, as in apply_twiddles. */
 template <int DIR, typename C>
 __device__ __forceinline__ void apply_stage_twiddles16(C *v, const C *__restrict__ tws, int k, int NS)
 {
+     if constexpr (sizeof(C) == 16) {
+#pragma unroll
+          for (int q = 1; q < 16; ++q) v[q] = cmul(v[q], twid<DIR>(tws, (q - 1) * NS + k));
+          return;
+     }
      const C w1 = twid<DIR>(tws, k), w2 = twid<DIR>(tws, NS + k), w4 = twid<DIR>(tws, 2 * NS + k),
              w8 = twid<DIR>(tws, 3 * NS + k);
      const C w3 = cmul(w1, w2), w12 = cmul(w8, w4);
@@ -456,7 +467,7 @@ __device__ __forceinline__ void reg_stages(C (&x)[reg_e(N)], int tid, C *smt, co
           for (int r = 0; r < RAD; ++r) v[r] = x[b + r * B];
           if constexpr (NS > 1) {
                static_assert(RAD == 16, "twiddled stages are radix 16");
-               apply_stage_twiddles16<DIR>(v, tws + stage_tw_off(N, NS), k, NS);
+               apply_stage_twiddles16<DIR>(v, tws + stage_tw_off(N, NS, stage_tw_rows(sizeof(C))), k, NS);
           }
           bfly<RAD, DIR>::run(v);
           if (LAST) {
@@ -719,7 +730,8 @@ __device__ __forceinline__ void tma_issue(const gb_pass &P, const void *in, long
      mbar_expect_tx(bar, bytes * (unsigned)ntr);
      for (int t = 0; t < ntr; ++t) {
           const long long off = tl.bi + (tl.v0 + t) * P.vis[0];
-          const void *src = (KIND == GB_KIND_R2C) ? (const void *)((const R *)in + off) : (const void *)((const C *)in + off);
+          const void *src = (KIND == GB_KIND_R2C || KIND == GB_KIND_DCT2) ? (const void *)((const R *)in + off)
+                                                                            : (const void *)((const C *)in + off);
           bulk_g2s(dst + t * tma_sms(N), src, bytes, bar);
      }
 }
@@ -731,16 +743,18 @@ __host__ __device__ constexpr int tma_threads(int nfft) { return (nfft / reg_e(n
 __host__ __device__ constexpr int tma_max_groups(int csize) { return csize == 8 ? 2 : 1; }
 
 /* CTAs per SM the register budget is sized for: 64 registers a thread for
- * two groups, 85 for one group of 256 threads */
-__host__ __device__ constexpr int tma_minblocks(int nfft, int G)
+ * two groups, 85 for one group of 256 threads (float), 128 for double, whose
+ * elements take two registers each (its CTAs hold half as many transforms:
+ * shared memory, not registers, limits how many share an SM) */
+__host__ __device__ constexpr int tma_minblocks(int nfft, int G, int csize)
 {
-     return G * tma_threads(nfft) >= 1024 ? 1 : G == 2 ? 2 : (tma_threads(nfft) > 256 ? 1 : 3);
+     return G * tma_threads(nfft) >= 1024 ? 1 : G == 2 ? 2 : (tma_threads(nfft) > 256 ? 1 : csize == 16 ? 2 : 3);
 }
 
 #define GB_WAIT_NS 2000000000ull   /* bound on any wait for a copy: 2 s */
 
 template <typename C, int LOGN, int DIR, int KIND, int G>
-__global__ void __launch_bounds__(G * tma_threads(1 << LOGN), tma_minblocks(1 << LOGN, G))
+__global__ void __launch_bounds__(G * tma_threads(1 << LOGN), tma_minblocks(1 << LOGN, G, sizeof(C)))
 k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
 {
      typedef typename real_of<C>::T R;
@@ -816,7 +830,21 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
           }
           if (gtid == 0) atomicAdd(&consumed[b], 1);
           C x[E];
-          {
+          if constexpr (KIND == GB_KIND_DCT2) {
+               /* Makhoul's permutation v_j = x_{2j} (j < N), v_{2N-1-j} = x_{2j+1}
+                * read from the slot: complex element m = (v_{2m}, v_{2m+1}) is
+                * (x_{4m}, x_{4m+2}) for m < N/2 and, with mm = N-1-m,
+                * (x_{4mm+3}, x_{4mm+1}) above: the same four reals serve both */
+               const C *s0 = cur + tl * SMS;
+#pragma unroll
+               for (int e = 0; e < E; ++e) {
+                    const int m = tid + T * e;
+                    const bool lo = 2 * m < N;
+                    const int q = lo ? m : N - 1 - m;
+                    const C a = s0[2 * q], c = s0[2 * q + 1];
+                    x[e] = lo ? mk<C>(a.x, c.x) : mk<C>(c.y, a.y);
+               }
+          } else {
                const C *s0 = cur + tl * SMS + tid;
 #pragma unroll
                for (int e = 0; e < E; ++e) x[e] = s0[T * e];
@@ -833,7 +861,7 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
           const long long v = tile.v0 + tl;
           const bool valid = v < P.vn[0];
           const long long bo = tile.bo + v * P.vos[0];
-          if constexpr (KIND == GB_KIND_R2C) {
+          if constexpr (KIND == GB_KIND_R2C || KIND == GB_KIND_DCT2) {
                /* hc2c post-pass (rdft/ct-hc2c.c:197-210):
                 * X[k] = (Z[k] + conj Z[N-k])/2 + W_2N^k (Z[k] - conj Z[N-k])/(2i) */
 #pragma unroll
@@ -842,7 +870,6 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
                /* each output straight to HBM as it is formed (no array of
                 * results held across the loop) */
                const C *__restrict__ th = (const C *)P.tw_half;
-               C *o = (C *)out + bo + tid;
 #pragma unroll
                for (int e = 0; e < E; ++e) {
                     const int k = tid + T * e;
@@ -850,11 +877,29 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
                     bq.y = -bq.y;
                     const C ev = cscale(cadd(a, bq), (R)0.5), dd = csub(a, bq);
                     const C od = mk<C>(dd.y * (R)0.5, -dd.x * (R)0.5);
-                    if (valid) o[T * e] = cadd(ev, cmul(__ldg(th + k), od));
+                    const C X = cadd(ev, cmul(__ldg(th + k), od));
+                    if constexpr (KIND == GB_KIND_R2C) {
+                         if (valid) ((C *)out)[bo + tid + T * e] = X;
+                    } else {
+                         /* DCT-II (reodft/reodft010e-r2hc.c): p = exp(-i pi k / 2n) V_k,
+                          * y_k = 2 Re p and, as exp(-i pi (n-k) / 2n) = -i conj of
+                          * the former, y_{n-k} = -2 Im p */
+                         const C p = cmul(__ldg((const C *)P.chirp + k), X);
+                         if (valid) {
+                              R *y = (R *)out + bo;
+                              y[k] = (R)2 * p.x;
+                              if (k) y[2 * N - k] = (R)-2 * p.y;
+                         }
+                    }
                }
                if (valid && tid == 0) {
                     const C z0 = smt[pad_for(N, 0)];
-                    o[N] = mk<C>(z0.x - z0.y, 0);
+                    if constexpr (KIND == GB_KIND_R2C) {
+                         ((C *)out)[bo + N] = mk<C>(z0.x - z0.y, 0);
+                    } else {
+                         /* y_N = 2 Re(exp(-i pi / 4) V_N), V_N real */
+                         ((R *)out)[bo + N] = (R)2 * __ldg((const C *)P.chirp + N).x * (z0.x - z0.y);
+                    }
                }
                gs();   /* the buffer is the next bulk copy's target */
                if (gtid == 0 && nxt < P.nblocks) {

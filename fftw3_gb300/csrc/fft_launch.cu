@@ -41,20 +41,23 @@ __global__ void k_twiddles(C *dst, long long n, long long count, long long mul)
 }
 
 /* Stage twiddle table of a power-of-two length N (layout of gb_pass.tw_stage):
- * entry (stage NS, row q, k) = exp(-2 pi i k (N / (16 NS)) 2^q / N), FP64
- * with the exact octant reduction, rounded once. */
+ * entry (stage NS, row q, k) = exp(-2 pi i k (N / (16 NS)) p / N) with
+ * p = 2^q (four rows, float) or p = q + 1 (fifteen rows, double), FP64 with
+ * the exact octant reduction, rounded once. */
 template <typename C>
 __global__ void k_stage_twiddles(C *dst, int N, int len)
 {
      typedef typename real_of<C>::T R;
+     constexpr int rows = stage_tw_rows(sizeof(C));
      for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < len; j += gridDim.x * blockDim.x) {
           int ns = reg_r0(N), idx = j;
-          while (idx >= 4 * ns) {
-               idx -= 4 * ns;
+          while (idx >= rows * ns) {
+               idx -= rows * ns;
                ns *= 16;
           }
           const int q = idx / ns, k = idx - q * ns;
-          const long long m = ((long long)k * (N / (16 * ns)) << q) % N;
+          const long long p = rows == 4 ? (1LL << q) : (long long)(q + 1);
+          const long long m = ((long long)k * (N / (16 * ns)) * p) % N;
           double c, s;
           cexp_fp64(m, N, -1, &c, &s);
           dst[j] = mk<C>((R)c, (R)s);
@@ -311,9 +314,9 @@ extern "C" int gb_twiddles(void *dst, int prec, long long n, long long count, lo
 
 extern "C" int gb_stage_twiddles(void *dst, int prec, int nfft, void *stream)
 {
-     const int len = stage_tw_len(nfft);
+     const int len = stage_tw_len(nfft, stage_tw_rows(2 * prec));
      int blocks = (len + 255) / 256;
-     if (len != gb_stage_tw_len(nfft)) {
+     if (len != gb_stage_tw_len(nfft, prec)) {
           snprintf(gb_errbuf, sizeof gb_errbuf, "stage twiddle layouts of host and device disagree");
           return -1;
      }
@@ -377,7 +380,7 @@ static const void *pick_kernel(const gb_pass *p)
           int logn = 0;
           while ((1 << logn) < p->nfft) ++logn;
           if (p->variant == GB_VAR_TMA)
-               return (p->kind == GB_KIND_C2C || p->kind == GB_KIND_R2C)
+               return (p->kind == GB_KIND_C2C || p->kind == GB_KIND_R2C || p->kind == GB_KIND_DCT2)
                            ? (p->prec == 4 ? gb_tma_kernel_f(logn, p->kind, p->sign, p->groups)
                                            : gb_tma_kernel_d(logn, p->kind, p->sign, p->groups))
                            : 0;
@@ -576,8 +579,11 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if ((p->variant == GB_VAR_REG || p->variant == GB_VAR_TMA || p->variant == GB_VAR_TMA_COLS ||
                     p->variant == GB_VAR_TC) && p->kind != GB_KIND_COPY && stage_tw_len(p->nfft) > 0 && !p->tw_stage)
                bad = "stage twiddle table missing";
-          else if ((p->kind == GB_KIND_R2C || p->kind == GB_KIND_C2R) && p->n % 2 == 0 && !p->tw_half)
+          else if ((p->kind == GB_KIND_R2C || p->kind == GB_KIND_C2R || p->kind == GB_KIND_DCT2) && p->n % 2 == 0 &&
+                   !p->tw_half)
                bad = "half-length twiddle table missing";
+          else if (p->kind == GB_KIND_DCT2 && (p->variant != GB_VAR_TMA || !p->chirp || p->n != 2 * p->nfft))
+               bad = "fused DCT-II pass needs the bulk-copy kernel and its cosine table";
           else if (p->kind == GB_KIND_BLUESTEIN && (!p->chirp || !p->chirp_spec)) bad = "chirp tables missing";
           else if (p->kind == GB_KIND_RADER && (p->variant != GB_VAR_GEN || !p->perm || !p->chirp_spec || p->nfft != p->n - 1))
                bad = "Rader pass needs its permutation and omega tables";
@@ -596,8 +602,8 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
           else if (p->variant == GB_VAR_REG && p->smem < p->tb * reg_sms(p->nfft) * 2 * p->prec) bad = "shared memory too small for the tile";
           else if (p->variant == GB_VAR_TMA && (p->threads > tma_threads(p->nfft) || (p->groups > 1 && p->threads % 32) ||
                                                 p->is != 1 || p->os != 1 ||
-                                                (p->kind != GB_KIND_C2C && p->kind != GB_KIND_R2C) ||
-                                                (p->kind == GB_KIND_R2C && p->n != 2 * p->nfft) ||
+                                                (p->kind != GB_KIND_C2C && p->kind != GB_KIND_R2C && p->kind != GB_KIND_DCT2) ||
+                                                ((p->kind == GB_KIND_R2C || p->kind == GB_KIND_DCT2) && p->n != 2 * p->nfft) ||
                                                 p->groups < 1 || p->groups > gb_tma_max_groups(p->prec) ||
                                                 p->groups * p->threads > 1024 ||
                                                 p->smem < (p->groups + 1) * p->tb * tma_sms(p->nfft) * 2 * p->prec))

@@ -22,6 +22,7 @@ static const void *tma_pick(int kind, int dir)
      if constexpr (L < 6 || L > 13 || G > tma_max_groups(sizeof(GB_CT))) return 0;
      else {
           if (kind == GB_KIND_R2C) return (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_R2C, G>;
+          if (kind == GB_KIND_DCT2) return (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_DCT2, G>;
           return dir < 0 ? (const void *)k_reg_tma<GB_CT, L, -1, GB_KIND_C2C, G>
                          : (const void *)k_reg_tma<GB_CT, L, 1, GB_KIND_C2C, G>;
      }

@@ -115,6 +115,11 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
      constexpr int R0 = reg_r0(N);       /* 16, or the radix of an FP32 first stage */
      constexpr int NS0 = R0 == 16 ? 1 : R0;
      constexpr int S = R0 == 16 ? LOGN / 4 : (LOGN - (R0 == 2 ? 1 : R0 == 4 ? 2 : 3)) / 4;   /* GEMM stages */
+     /* the tile in dat takes the register kernels' swizzled layout (element p
+      * of transform t at t * SMS + pad_for(N, p)): the strided stage stores
+      * stay free of bank conflicts */
+     constexpr int SMS = reg_sms(N);
+     static_assert(256 / T * SMS * 8 <= 2 * (int)TC_A_BYTES, "the swizzled tile fits the A operand's memory");
      extern __shared__ __align__(1024) unsigned char sm[];
      __shared__ uint32_t tbase;
      __shared__ __align__(8) unsigned long long bar, pbar;
@@ -187,8 +192,8 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
                     if (P.load_mode == GB_MOVE_COLS) { t = i & (TB - 1); e = i / TB; }
                     else { t = i / N; e = i - t * N; }
                     const long long v = tile.v0 + t;
-                    dat[t * N + e] = (v < P.vn[0]) ? ((const float2 *)in)[tile.bi + v * P.vis[0] + e * P.is]
-                                                   : make_float2(0.f, 0.f);
+                    dat[t * SMS + pad_for(N, e)] = (v < P.vn[0]) ? ((const float2 *)in)[tile.bi + v * P.vis[0] + e * P.is]
+                                                                 : make_float2(0.f, 0.f);
                }
                __syncthreads();
           }
@@ -197,8 +202,13 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
                 * from src into dat */
                constexpr int B = 16 / R0;
                float2 x[16];
+               if (src == pre) {
 #pragma unroll
-               for (int e = 0; e < 16; ++e) x[e] = src[tl * N + j + e * T];
+                    for (int e = 0; e < 16; ++e) x[e] = pre[tl * N + j + e * T];
+               } else {
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) x[e] = dat[tl * SMS + pad_for(N, j + e * T)];
+               }
                __syncthreads();
 #pragma unroll
                for (int b = 0; b < B; ++b) {
@@ -208,7 +218,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
                     bfly<R0, DIR>::run(v);
                     const int jj = j + b * T;
 #pragma unroll
-                    for (int q = 0; q < R0; ++q) dat[tl * N + jj * R0 + q] = v[q];
+                    for (int q = 0; q < R0; ++q) dat[tl * SMS + pad_for(N, jj * R0 + q)] = v[q];
                }
                if (src == pre && threadIdx.x == 0 && blk + gridDim.x < P.nblocks) {
                     /* every thread has read the buffer (the barrier above) */
@@ -223,10 +233,14 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
 #pragma unroll 1
           for (int s = 0; s < S; ++s) {
                float2 x[16];
-               const float2 *st = src + tl * N;
-               float2 *dt = dat + tl * N;
+               float2 *dt = dat + tl * SMS;
+               if (src == pre) {
 #pragma unroll
-               for (int r = 0; r < 16; ++r) x[r] = st[j + r * T];
+                    for (int r = 0; r < 16; ++r) x[r] = pre[tl * N + j + r * T];
+               } else {
+#pragma unroll
+                    for (int r = 0; r < 16; ++r) x[r] = dt[pad_for(N, j + r * T)];
+               }
                const int k = j & (NS - 1);
                if (NS > 1) apply_stage_twiddles16<DIR>(x, tws + stage_tw_off(N, NS), k, NS);
                float mx = 0.f;
@@ -297,8 +311,18 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
                const bool last = (s == S - 1);
                if (!last) {
                     const int base = (j / NS) * NS * 16 + k;
+                    if (NS == 1 && pad_mult(N) == 2) {
+                         /* 16 consecutive outputs, 16-byte aligned in the swizzle:
+                          * eight 128-bit stores, a quarter warp's conflict-free */
+                         float4 *d4 = (float4 *)(dt + pad_for(N, base));
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) dt[base + q * NS] = make_float2(v[q] * inv, v[16 + q] * inv);
+                         for (int q = 0; q < 8; ++q)
+                              d4[q] = make_float4(v[2 * q] * inv, v[16 + 2 * q] * inv, v[2 * q + 1] * inv,
+                                                  v[17 + 2 * q] * inv);
+                    } else {
+#pragma unroll
+                         for (int q = 0; q < 16; ++q) dt[pad_for(N, base + q * NS)] = make_float2(v[q] * inv, v[16 + q] * inv);
+                    }
                } else {
                     /* outputs j + q*T in natural order; four-step passes also
                      * apply W_postN^(v*k) */
@@ -315,7 +339,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
                          }
                     } else {
 #pragma unroll
-                         for (int q = 0; q < 16; ++q) dt[j + q * T] = y[q];
+                         for (int q = 0; q < 16; ++q) dt[pad_for(N, j + q * T)] = y[q];
                     }
                }
                tc::fence_before_sync();
@@ -329,7 +353,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
                     if (P.store_mode == GB_MOVE_COLS) { t = i & (TB - 1); e = i / TB; }
                     else { t = i / N; e = i - t * N; }
                     const long long v = tile.v0 + t;
-                    if (v < P.vn[0]) ((float2 *)out)[tile.bo + v * P.vos[0] + e * P.os] = dat[t * N + e];
+                    if (v < P.vn[0]) ((float2 *)out)[tile.bo + v * P.vos[0] + e * P.os] = dat[t * SMS + pad_for(N, e)];
                }
                __syncthreads();
           }

@@ -58,6 +58,8 @@ typedef struct gb_r2r_axis {
      gb_r2r_vec vec;
      void *tw;                  /* device twiddle table of the stage (NULL: none) */
      struct gb_plan *inner;     /* the core transform on r2r_buf[0] -> r2r_buf[1] */
+     int fused;                 /* 1: the stage also runs as the single pass fpass */
+     gb_pass fpass;             /* REDFT10 of unit-stride rows: load, r2c and post-twiddle in one kernel */
 } gb_r2r_axis;
 
 struct gb_plan {
@@ -155,6 +157,8 @@ int gb_r2r_tune(gb_plan *p, unsigned flags);
 typedef struct gb_wisdom_entry {
      char key[256];
      int variant, tb, load_mode, store_mode, n1;
+     int groups;    /* compute groups per CTA of a bulk-copy pass (0: the planner's choice) */
+     int order;     /* radix order of a runtime-radix pass (0: the planner's; see gb_factor_order) */
 } gb_wisdom_entry;
 const gb_wisdom_entry *gb_wisdom_lookup(const char *key);
 void gb_wisdom_store(const gb_wisdom_entry *e);
@@ -170,7 +174,13 @@ void gb_tables_free(void);
 
 /* helpers shared with the plan-set compiler */
 int gb_factor_radices(long long n, int *rad);
+#define GB_RADIX_ORDERS 3
+int gb_factor_order(long long n, int *rad, int order);
 int gb_pass_tables(gb_pass *P);
+/* one pass of kind over a batch (nv <= GB_MAXV vector dims), as the planner
+ * configures its passes; 0 on success */
+int gb_config_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os, int nv,
+                   const gb_dim *v);
 
 /* plan sets (gb_set.c) */
 typedef struct gb_set gb_set;

@@ -62,6 +62,9 @@ int gb_cuda_ready(void)
 /* planner-wide choice set by add_1d from wisdom (the planner runs under the
  * library lock): 1 = do not use the bulk-copy fed persistent variant */
 static int cfg_no_tma = 0;
+/* and, from the same wisdom entry: compute groups of a bulk-copy pass (0 =
+ * the planner's choice) and the radix order of a runtime-radix pass */
+static int cfg_groups = 0, cfg_order = 0;
 
 /* shared memory of one SM (two CTAs of a persistent kernel must fit, each
  * with the 1 KB the system reserves) */
@@ -129,7 +132,7 @@ const void *gb_table_twiddle(int prec, long long n, long long count, long long m
  * of gb_pass.tw_stage */
 const void *gb_table_stage_twiddle(int prec, int nfft)
 {
-     const int len = gb_stage_tw_len(nfft);
+     const int len = gb_stage_tw_len(nfft, prec);
      void *p = tab_find(prec, 5, nfft, 0, 0);
      if (p) return p;
      p = tab_add(prec, 5, nfft, 0, 0, (size_t)(len ? len : 1) * 2 * prec);
@@ -329,6 +332,38 @@ static int gb_factor(long long n, int *rad)
 static int csize(int prec) { return 2 * prec; }
 
 int gb_factor_radices(long long n, int *rad) { return gb_factor(n, rad); }
+
+/* The radix list of a runtime-radix pass in one of GB_RADIX_ORDERS orders
+ * (the tuner's choice, recorded in wisdom): 0 = radix 16 first, then 8, 4,
+ * 2 and the odd primes ascending (gb_factor); 1 = no radix 16: radix 8
+ * first, then 4, 2 and the odd primes descending; 2 = the odd primes
+ * descending first, then 16, 8, 4, 2.  Returns the number of stages, or -1
+ * when n has a prime factor above 13. */
+int gb_factor_order(long long n, int *rad, int order)
+{
+     static const int odd[] = {13, 11, 7, 5, 3};
+     int k = 0, i, p2[GB_MAXRAD], np2 = 0, po[GB_MAXRAD], npo = 0;
+     if (order <= 0 || order >= GB_RADIX_ORDERS) return gb_factor(n, rad);
+     for (i = 0; i < 5; ++i)
+          while (n % odd[i] == 0 && npo < GB_MAXRAD) { po[npo++] = odd[i]; n /= odd[i]; }
+     if (order == 1) {
+          while (n % 8 == 0 && np2 < GB_MAXRAD) { p2[np2++] = 8; n /= 8; }
+     } else {
+          while (n % 16 == 0 && np2 < GB_MAXRAD) { p2[np2++] = 16; n /= 16; }
+          if (n % 8 == 0) { p2[np2++] = 8; n /= 8; }
+     }
+     if (n % 4 == 0) { p2[np2++] = 4; n /= 4; }
+     if (n % 2 == 0) { p2[np2++] = 2; n /= 2; }
+     if (n != 1 || np2 + npo > GB_MAXRAD) return -1;
+     if (order == 1) {
+          for (i = 0; i < np2; ++i) rad[k++] = p2[i];
+          for (i = 0; i < npo; ++i) rad[k++] = po[i];
+     } else {
+          for (i = 0; i < npo; ++i) rad[k++] = po[i];
+          for (i = 0; i < np2; ++i) rad[k++] = p2[i];
+     }
+     return k;
+}
 static int reg_max_log(int prec) { return prec == 4 ? 14 : 13; }
 static int reg_e(int nfft) { return nfft < 16 ? nfft : 16; }
 static int reg_sms(int nfft) { return gb_reg_sms(nfft); }
@@ -487,6 +522,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
                 * three of one group per SM */
                const char *genv = getenv("FFTW_GB300_TMA_GROUPS");
                int groups = (prec == 4 && nfft == 8192) ? 2 : 1;
+               if (cfg_groups == 1 || cfg_groups == 2) groups = cfg_groups;   /* the tuner's choice */
                if (genv && (atoi(genv) == 1 || atoi(genv) == 2)) groups = atoi(genv);
                if (groups > gb_tma_max_groups(prec)) groups = gb_tma_max_groups(prec);
                const int nbuf = groups + 1;
@@ -512,7 +548,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
      } else {
           int k, tb;
           long long sm1, L = nfft;
-          k = gb_factor(nfft, P->rad);
+          k = gb_factor_order(nfft, P->rad, cfg_order);
           if (k < 0) return -1;
           P->nrad = k;
           P->variant = GB_VAR_GEN;
@@ -593,6 +629,13 @@ static int pass_tables(gb_pass *P)
 }
 
 int gb_pass_tables(gb_pass *P) { return pass_tables(P); }
+
+int gb_config_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os, int nv,
+                   const gb_dim *v)
+{
+     if (nv > GB_MAXV) return -1;
+     return config_pass(P, prec, kind, n, sign, is, os, nv, v, 0, 0);
+}
 
 /* ------------------------------------------------------------ plan building */
 typedef struct {
@@ -864,9 +907,13 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           for (i = 0; i < s->nloop; ++i) s->loop[i] = v[i];
      }
      cfg_no_tma = (w && w->variant == GB_VAR_REG);
+     cfg_groups = w ? w->groups : 0;
+     cfg_order = w ? w->order : 0;
      rc = config_pass(&s->pass, prec, kind, n, sign, is, os, nvk - s->nloop, v + s->nloop,
                       (w && w->tb > 0) ? w->tb : 0, 0);
      cfg_no_tma = 0;
+     cfg_groups = 0;
+     cfg_order = 0;
      if (rc == 0 && kind == GB_KIND_C2C && !(w && w->tb > 0) && src != mid && dst != mid &&
          (s->pass.load_mode == GB_MOVE_COLS || s->pass.store_mode == GB_MOVE_COLS) &&
          s->pass.tb * csize(prec) < 32 && s->nloop == 0) {
@@ -1103,7 +1150,7 @@ static void describe(gb_plan *p)
                      kn[p->prb.kind], p->prb.prec == 4 ? "f32" : "f64");
      for (i = 0; i < p->nstep && off < (int)sizeof p->desc - 64; ++i) {
           const gb_pass *P = &p->step[i].pass;
-          static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy", "rader", "pointwise"};
+          static const char *kk[] = {"c2c", "r2c", "c2r", "bluestein", "copy", "rader", "pointwise", "dct2"};
           static const char *mv[] = {"direct", "rows", "cols"};
           static const char *pw[] = {"hc2c-post", "hc2c-pre", "chirp-in", "spec-mul", "chirp-out", "promote",
                                      "half-copy", "herm-ext", "real-part", "chirp-in-real", "chirp-in-herm",
@@ -1119,6 +1166,15 @@ static void describe(gb_plan *p)
                           P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
                           P->vn[0], P->post_N ? " +twiddle" : "");
+          if (P->variant == GB_VAR_GEN && P->nrad > 0 && off < (int)sizeof p->desc - 64) {
+               /* the runtime radix list, before the closing parenthesis */
+               int r;
+               --off;
+               off += snprintf(p->desc + off, sizeof p->desc - off, " rad=");
+               for (r = 0; r < P->nrad && off < (int)sizeof p->desc - 8; ++r)
+                    off += snprintf(p->desc + off, sizeof p->desc - off, r ? ".%d" : "%d", P->rad[r]);
+               off += snprintf(p->desc + off, sizeof p->desc - off, ")");
+          }
           if (off >= (int)sizeof p->desc) off = (int)sizeof p->desc - 1;   /* truncated */
      }
      if (off < (int)sizeof p->desc - 1) snprintf(p->desc + off, sizeof p->desc - off, ")");

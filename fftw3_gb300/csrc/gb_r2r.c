@@ -196,11 +196,31 @@ gb_plan *gb_mkr2r(int prec, int rank, const gb_dim *dims, const int *kinds, int 
                     return 0;
                }
           }
+          /* REDFT10 of unit-stride rows whose starts are 16-byte aligned, of a
+           * power-of-two length the bulk-copy kernel takes: the permuted load,
+           * the r2c and the cosine post-twiddle in one pass (one read and one
+           * write of the array instead of three of each) */
+          if (a->kind == FFTW_REDFT10 && a->is == 1 && a->os == 1 && a->n >= 128 && a->n <= 16384 &&
+              (a->n & (a->n - 1)) == 0 && a->vec.nv >= 1 && a->vec.nv <= GB_MAXV && (a->tw || gb_dry_run())) {
+               gb_dim vd[GB_MAXV];
+               int ok = 1;
+               for (e = 0; e < a->vec.nv; ++e) {
+                    vd[e].n = a->vec.n[e]; vd[e].is = a->vec.is[e]; vd[e].os = a->vec.os[e];
+                    if ((a->vec.is[e] * prec) % 16) ok = 0;
+               }
+               if (ok && gb_config_pass(&a->fpass, prec, GB_KIND_R2C, a->n, -1, 1, 1, a->vec.nv, vd) == 0 &&
+                   a->fpass.variant == GB_VAR_TMA && gb_pass_tables(&a->fpass) == 0) {
+                    a->fpass.kind = GB_KIND_DCT2;
+                    a->fpass.chirp = a->tw;
+                    a->fused = 1;
+               }
+          }
           for (s = 0; s < a->inner->nstep && p->nstep < GB_MAXPASS; ++s) p->step[p->nstep++] = a->inner->step[s];
           p->add += a->inner->add; p->mul += a->inner->mul; p->fma += a->inner->fma;
           if (len < (int)sizeof p->desc)
-               len += snprintf(p->desc + len, sizeof p->desc - (size_t)len, " (dim %d kind %d n %lld pre %s post)",
-                               rank - 1 - i, a->kind, a->n, a->inner->desc);
+               len += snprintf(p->desc + len, sizeof p->desc - (size_t)len, " (dim %d kind %d n %lld %s%s post)",
+                               rank - 1 - i, a->kind, a->n, a->fused ? "fused-dct2 or pre " : "pre ",
+                               a->inner->desc);
      }
      if (len < (int)sizeof p->desc) snprintf(p->desc + len, sizeof p->desc - (size_t)len, ")");
      return p;
@@ -225,6 +245,17 @@ static int r2r_device(const void *ptr, void **dev)
      if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) { *dev = (void *)ptr; return 1; }
      if (a.type == cudaMemoryTypeHost && a.devicePointer) { *dev = a.devicePointer; return 1; }
      return 0;
+}
+
+/* device (or managed) memory, which the bulk-copy kernels may read */
+static int r2r_in_hbm(const void *ptr)
+{
+     struct cudaPointerAttributes a;
+     if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+          cudaGetLastError();
+          return 0;
+     }
+     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
 /* element span [lo, hi] (in reals) the problem touches on the input (out = 0)
@@ -298,6 +329,14 @@ static int execute_r2r_locked(gb_plan *p, void *in, void *out)
           gb_r2r_axis *a = &p->r2r_ax[i];
           const void *src = a->src_mid ? p->r2r_mid : din;
           void *dst = a->dst_mid ? p->r2r_mid : dout;
+          if (a->fused && ((uintptr_t)src % 16) == 0 && r2r_in_hbm(src) && r2r_in_hbm(dst)) {
+               /* the bulk copies read device memory at 16-byte aligned rows */
+               if (gb_launch_pass(&a->fpass, src, dst, st)) {
+                    gb_set_error("r2r pass launch failed: %s", gb_last_cuda_error());
+                    goto done;
+               }
+               continue;
+          }
           if (gb_r2r_pre(prec, a->kind, a->n, a->V, src, a->is, &a->vec, p->r2r_buf[0], a->tw, st)) goto done;
           a->inner->stream = p->stream;
           a->inner->async = 1;

@@ -3,7 +3,10 @@
  * 518-615 search, kernel/timer.c:142-181 measurement) for the choices this
  * library has for one batched 1D c2c transform of length n:
  *   - the kernel variant of a power-of-two length (bulk-copy fed persistent
- *     CTAs vs plain register kernel),
+ *     CTAs vs plain register kernel), and the bulk-copy pass's threads per
+ *     CTA (one or two compute groups),
+ *   - the radix order of a smooth, not power-of-two length (runtime-radix
+ *     stages: radix 16 first, radix 8 at most, or the odd primes first),
  *   - the transforms per CTA (tile) of a single-pass kernel,
  *   - the split n = n1 * n2 of a two-pass length,
  *   - Bluestein vs Rader for a prime length.
@@ -105,6 +108,17 @@ int gb_tune(gb_plan *p, unsigned flags)
           cand[nc].variant = -1; cand[nc].tb = 0; cand[nc].n1 = 0; ++nc;    /* the heuristic choice */
           if ((n & (n - 1)) == 0 && n >= 64 && n <= 8192) {
                cand[nc].variant = GB_VAR_REG; cand[nc].tb = 0; ++nc;       /* no bulk-copy pipeline */
+               if (prb->prec == 4) {
+                    /* threads per CTA of the bulk-copy pass: one or two
+                     * compute groups (over two or three tile buffers) */
+                    cand[nc].variant = -1; cand[nc].groups = 1; ++nc;
+                    cand[nc].variant = -1; cand[nc].groups = 2; ++nc;
+               }
+          } else if ((n & (n - 1)) != 0) {
+               /* radix order of the runtime-radix stages */
+               int rad[GB_MAXRAD], o;
+               for (o = 1; o < GB_RADIX_ORDERS; ++o)
+                    if (gb_factor_order(n, rad, o) > 0) { cand[nc].variant = -1; cand[nc].order = o; ++nc; }
           }
           for (i = 0; i < ntb && nc < 40; ++i) {
                cand[nc].variant = -1; cand[nc].tb = tbs[i]; ++nc;

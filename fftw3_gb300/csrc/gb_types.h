@@ -28,7 +28,9 @@ enum gb_kind {
      GB_KIND_BLUESTEIN = 3, /* complex n -> complex n through a chirp convolution of length nfft */
      GB_KIND_COPY = 4,      /* rank-0 problem: element copy */
      GB_KIND_RADER = 5,     /* prime n: cyclic convolution of length n-1 through the generator permutation */
-     GB_KIND_POINTWISE = 6  /* element-wise pass between multi-pass stages (field pw) */
+     GB_KIND_POINTWISE = 6, /* element-wise pass between multi-pass stages (field pw) */
+     GB_KIND_DCT2 = 7       /* REDFT10 of n reals in one pass: permuted load, r2c of n, cosine
+                             * post-twiddle (chirp: exp(-i pi q / 2n), q < n), n reals out */
 };
 
 /* Element-wise passes of multi-pass plans (lengths beyond one CTA). */
@@ -91,9 +93,12 @@ typedef struct gb_pass {
      const void *tw;      /* exp(-2 pi i j / nfft), j < nfft */
      /* power-of-two nfft: the twiddles of the radix-16 stages, laid out so a
       * warp's reads are coalesced.  For each stage with span NS (NS = r0,
-      * 16 r0, 256 r0, ... below nfft, r0 the first stage's radix), four rows
-      * of NS entries: row q holds exp(-2 pi i k (nfft / (16 NS)) 2^q / nfft),
-      * k < NS.  Stages follow one another (gb_stage_tw_len entries in all). */
+      * 16 r0, 256 r0, ... below nfft, r0 the first stage's radix), rows of NS
+      * entries exp(-2 pi i k (nfft / (16 NS)) p / nfft), k < NS: float has four
+      * rows, p = 1, 2, 4, 8 (the other powers derived, FP32 multiplies being
+      * cheap); double has fifteen, p = 1..15 (FP64 multiplies are the
+      * bottleneck of double passes).  Stages follow one another
+      * (gb_stage_tw_len entries in all). */
      const void *tw_stage;
      const void *tw_half; /* r2c/c2r: exp(-2 pi i k / n), k <= n/2 */
      /* four-step: multiply output k of the transform whose index along
@@ -162,12 +167,14 @@ static inline int gb_reg_r0(int nfft)
      while (r > 16) r /= 16;
      return r;
 }
+/* rows per stage of the stage twiddle table (prec: bytes per real) */
+static inline int gb_stage_tw_rows(int prec) { return prec == 8 ? 15 : 4; }
 /* entries of the stage twiddle table of a power-of-two nfft (0 below 32) */
-static inline int gb_stage_tw_len(int nfft)
+static inline int gb_stage_tw_len(int nfft, int prec)
 {
      int len = 0, ns;
      if (nfft < 32) return 0;
-     for (ns = gb_reg_r0(nfft); ns * 16 <= nfft; ns *= 16) len += 4 * ns;
+     for (ns = gb_reg_r0(nfft); ns * 16 <= nfft; ns *= 16) len += gb_stage_tw_rows(prec) * ns;
      return len;
 }
 

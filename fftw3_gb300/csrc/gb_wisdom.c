@@ -5,8 +5,11 @@
  * (kernel/planner.c:790-826):
  *
  *   (fftw-3.3.10-gb300 fftwf_wisdom #x<signature>
- *     (gb300-pass "c2c p4 n4096" #x<variant> #x<tb> #x<load> #x<store> #x<n1>)
+ *     (gb300-pass "c2c p4 n4096" #x<variant> #x<tb> #x<load> #x<store> #x<n1> #x<groups> #x<order>)
  *   )
+ *
+ * (an entry with only the first five numbers, as earlier versions wrote
+ * them, reads with groups and order 0: the planner's choices)
  *
  * The preamble and signature differ from the reference's, so a file written
  * by one library is rejected by the other (the reference rejects a
@@ -73,8 +76,8 @@ int gb_wisdom_export(int prec, void (*emit)(char c, void *), void *data)
      emits(emit, data, buf);
      for (n = wis; n; n = n->next) {
           if (n->prec != prec) continue;
-          snprintf(buf, sizeof buf, "  (gb300-pass \"%s\" #x%x #x%x #x%x #x%x #x%x)\n", n->e.key, n->e.variant,
-                   n->e.tb, n->e.load_mode, n->e.store_mode, n->e.n1);
+          snprintf(buf, sizeof buf, "  (gb300-pass \"%s\" #x%x #x%x #x%x #x%x #x%x #x%x #x%x)\n", n->e.key,
+                   n->e.variant, n->e.tb, n->e.load_mode, n->e.store_mode, n->e.n1, n->e.groups, n->e.order);
           emits(emit, data, buf);
      }
      emits(emit, data, ")\n");
@@ -132,7 +135,7 @@ static int read_str(rd *r, char *out, int cap)
 int gb_wisdom_import(int prec, int (*getc_fn)(void *), void *data)
 {
      rd r;
-     unsigned long long sig, v[5];
+     unsigned long long sig, v[7];
      gb_wisdom_entry got[1024];
      int ngot = 0, i;
      r.g = getc_fn; r.d = data;
@@ -149,11 +152,16 @@ int gb_wisdom_import(int prec, int (*getc_fn)(void *), void *data)
           if (!read_str(&r, got[ngot].key, sizeof got[ngot].key)) return 0;
           for (i = 0; i < 5; ++i)
                if (!read_hex(&r, &v[i])) return 0;
+          v[5] = v[6] = 0;
+          skipws(&r);
+          if (r.c == '#' && (!read_hex(&r, &v[5]) || !read_hex(&r, &v[6]))) return 0;
           if (!expect(&r, ")")) return 0;
           if (prec_of_key(got[ngot].key) != prec) return 0;
           got[ngot].variant = (int)v[0]; got[ngot].tb = (int)v[1];
           got[ngot].load_mode = (int)v[2]; got[ngot].store_mode = (int)v[3]; got[ngot].n1 = (int)v[4];
-          if (got[ngot].tb < 0 || got[ngot].tb > 1024 || got[ngot].n1 < 0) return 0;
+          got[ngot].groups = (int)v[5]; got[ngot].order = (int)v[6];
+          if (got[ngot].tb < 0 || got[ngot].tb > 1024 || got[ngot].n1 < 0 || v[5] > 2 || v[6] >= GB_RADIX_ORDERS)
+               return 0;
           ++ngot;
      }
      for (i = 0; i < ngot; ++i) gb_wisdom_store(&got[i]);

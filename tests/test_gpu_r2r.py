@@ -215,3 +215,41 @@ def test_r2r_rank0_copy(lib, torch_cuda):
     torch.cuda.synchronize()
     want = src.reshape(40, 21)[:, 0:21:3].ravel()
     assert np.array_equal(dd.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("n,hm", [(128, 37), (256, 9), (2048, 5), (4096, 3), (16384, 2), (4096, 4096)])
+@pytest.mark.parametrize("inplace", [False, True])
+def test_redft10_fused_pass(lib, torch_cuda, restatement, prec, n, hm, inplace):
+    """DCT-II of unit-stride rows of a power-of-two length runs as one pass
+    (the permuted load, the r2c and the cosine post-twiddle in one kernel):
+    against the oracle's defining sum on rows spread over the batch."""
+    torch = torch_cuda
+    rng = np.random.default_rng(n + hm + inplace)
+    x = rng.standard_normal(n * hm).astype(RT[prec])
+    dx = torch.from_numpy(x).cuda()
+    dy = dx if inplace else torch.zeros_like(dx)
+    p = plan_many(lib, prec, n, hm, dx.data_ptr(), dy.data_ptr(), 5)
+    pfx = "fftwf_" if prec == "f" else "fftw_"
+    sp = getattr(lib, pfx + "sprint_plan")
+    sp.restype = ctypes.c_char_p
+    sp.argtypes = [ctypes.c_void_p]
+    # (a double transform of 8192 complex points takes more shared memory
+    # than the bulk-copy kernel has: it keeps the three-kernel form)
+    fused = not (prec == "d" and n > 8192)
+    assert (b"fused-dct2" in sp(p)) == fused
+    before = lib.fftw_gb300_launch_count()
+    run(lib, prec, p, dx.data_ptr(), dy.data_ptr())
+    torch.cuda.synchronize()
+    if fused:
+        assert lib.fftw_gb300_launch_count() - before == 1
+    rows = sorted(set(np.linspace(0, hm - 1, min(hm, 8)).astype(int).tolist()))
+    y = dy.cpu().numpy().reshape(hm, n)
+    xs = x.reshape(hm, n)
+    for t in rows:
+        xt = xs[t].astype(np.float64 if prec == "f" else np.longdouble)
+        if n <= 2048:
+            ref = restatement.r2r(xt, n, 5, "d" if prec == "f" else "l")
+        else:
+            ref = restatement.r2r_fast(xt, n, 5, "d" if prec == "f" else "l", 1)
+        assert rel_l2(y[t].astype(np.float64), ref.astype(np.float64)) <= TOL[prec], f"row {t}"

@@ -231,3 +231,36 @@ def test_c2r_multid_preserve_input_in_place(lib):
     f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint]
     assert f(64, 64, 1 << 20, 1 << 20, g.FFTW_ESTIMATE | g.FFTW_PRESERVE_INPUT)
     assert not f(64, 64, 1 << 20, 1 << 30, g.FFTW_ESTIMATE | g.FFTW_PRESERVE_INPUT)
+
+
+def test_wisdom_groups_and_radix_order(lib):
+    """Wisdom records the tuner's threads per CTA of a bulk-copy pass (one
+    or two compute groups) and the radix order of a runtime-radix pass; the
+    planner follows both, and entries written with five numbers (no groups,
+    no order) still import."""
+    import fftw3_gb300 as g
+    g.set_dry_run(True)
+    try:
+        lib.fftwf_forget_wisdom()
+        w = (b'(fftw-3.3.10-gb300 fftwf_wisdom #x67623330304c4942\n'
+             b'  (gb300-pass "c2c p4 n4096" #xffffffff #x0 #x0 #x0 #x0 #x2 #x0)\n'
+             b'  (gb300-pass "c2c p4 n6000" #xffffffff #x0 #x0 #x0 #x0 #x0 #x1)\n'
+             b'  (gb300-pass "c2c p4 n3000" #xffffffff #x0 #x0 #x0 #x0 #x0 #x2)\n)\n')
+        assert lib.fftwf_import_wisdom_from_string(w) == 1
+        p = g.plan_many_dft([4096], 64, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f")
+        assert "reg-tma groups=2" in p.describe()
+        p = g.plan_many_dft([6000], 8, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f")
+        assert "rad=8.2.5.5.5.3" in p.describe(), p.describe()
+        p = g.plan_many_dft([3000], 8, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f")
+        assert "rad=5.5.5.3.8" in p.describe(), p.describe()
+        exported = ctypes.string_at(lib.fftwf_export_wisdom_to_string())
+        assert b'"c2c p4 n4096" #xffffffff #x0 #x0 #x0 #x0 #x2 #x0)' in exported
+        # out-of-range choices are refused and leave the wisdom as it was
+        bad = w.replace(b"#x2 #x0)", b"#x7 #x0)")
+        assert lib.fftwf_import_wisdom_from_string(bad) == 0
+        lib.fftwf_forget_wisdom()
+        p = g.plan_many_dft([6000], 8, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f")
+        assert "rad=16.3.5.5.5" in p.describe() or "rad=16" in p.describe(), p.describe()
+    finally:
+        lib.fftwf_forget_wisdom()
+        g.set_dry_run(False)
