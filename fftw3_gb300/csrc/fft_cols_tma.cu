@@ -159,6 +159,10 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
      unsigned long long *const full = (unsigned long long *)(base + ct_slot_off(N, tb, NB - 1) +
                                                              ((ct_slot_bytes(N, tb) + 15) & ~15));
      int *const issued = (int *)(full + NB), *const consumed = issued + NB;
+     /* a refill each group's leader owes (tile, slot; the slot of its previous
+      * tile), read and written by that leader only */
+     long long *const pend_tile = (long long *)(consumed + NB);
+     int *const pend_slot = (int *)(pend_tile + G);
      const int GT = P.threads;
      const int g = (int)threadIdx.x / GT;
      const int gtid = (int)threadIdx.x - g * GT;
@@ -189,6 +193,7 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
           }
      }
 
+     if (gtid == 0) pend_tile[g] = -1;
      for (int i = g;; i += G) {
           const long long blk = blockIdx.x + (long long)i * stride;
           if (blk >= P.nblocks) break;
@@ -219,13 +224,32 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
           C x[E];
           {
                const int colbase = (tl / cb) * N * cb * 8 + (tl % cb) * 8;
+               if constexpr (T % 8 == 0) {
+                    /* rows tid + T e share tid's swizzle (T e moves whole periods
+                     * of eight rows): one swizzled base, a constant stride */
+                    const unsigned char *p0 = cur + ct_swz(colbase + tid * cb * 8, mask);
+                    const int st = T * cb * 8;
 #pragma unroll
-               for (int e = 0; e < E; ++e) {
-                    const int o = colbase + (tid + T * e) * cb * 8;
-                    x[e] = *(const C *)(cur + ct_swz(o, mask));
+                    for (int e = 0; e < E; ++e) x[e] = *(const C *)(p0 + e * st);
+               } else {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                         const int o = colbase + (tid + T * e) * cb * 8;
+                         x[e] = *(const C *)(cur + ct_swz(o, mask));
+                    }
                }
           }
           gs();
+          /* the previous tile's slot, refilled now that its boxes had the
+           * stages' time to be read out by the TMA engine */
+          if (gtid == 0 && pend_tile[g] >= 0) {
+               const int pb = pend_slot[g];
+               bulk_wait_read();
+               fence_proxy_async_smem();
+               ct_issue<N>(P, &tmap, pend_tile[g], base + ct_slot_off(N, tb, pb), &full[pb]);
+               atomicAdd(&issued[pb], 1);
+               pend_tile[g] = -1;
+          }
           C *const sm = (C *)cur;
           C *const smt = sm + tl * SMS;
           reg_stages<C, N, DIR, 1>(x, tid, smt, tw, gs);
@@ -244,9 +268,10 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
                     atomicAdd(&issued[b], 1);
                }
                if (v < P.vn[0]) {
-                    const long long bo = tile.bo + v * P.vos[0];
+                    C *o = (C *)out + tile.bo + v * P.vos[0] + (long long)tid * P.os;
+                    const long long st = (long long)T * P.os;
 #pragma unroll
-                    for (int e = 0; e < E; ++e) io<C>::stc(out, bo, tid + T * e, P.os, x[e]);
+                    for (int e = 0; e < E; ++e) o[e * st] = x[e];
                }
           } else if (tstore) {
                /* column tiles out through the output tensor map: the results
@@ -256,10 +281,17 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
                const int cbs = ct_cb(P.tb);
                const int ms = cbs >= 16 ? 7 : cbs == 8 ? 3 : cbs == 4 ? 1 : 0;
                const int cbase = (tl / cbs) * N * cbs * 8 + (tl % cbs) * 8;
+               if constexpr (T % 8 == 0) {
+                    unsigned char *p0 = cur + ct_swz(cbase + tid * cbs * 8, ms);
+                    const int st = T * cbs * 8;
 #pragma unroll
-               for (int e = 0; e < E; ++e) {
-                    const int o = cbase + (tid + T * e) * cbs * 8;
-                    *(C *)(cur + ct_swz(o, ms)) = x[e];
+                    for (int e = 0; e < E; ++e) *(C *)(p0 + e * st) = x[e];
+               } else {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                         const int o = cbase + (tid + T * e) * cbs * 8;
+                         *(C *)(cur + ct_swz(o, ms)) = x[e];
+                    }
                }
                fence_proxy_async_smem();
                gs();
@@ -275,11 +307,12 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
                               tma_tile_store(&omap, 1 + P.nv, c, cur + (k * N + r * ROWS) * cbs * 8);
                          }
                     bulk_commit();
+                    /* the slot's next tile is issued once the group has gathered
+                     * its next tile (above), not here: waiting now for the boxes
+                     * to be read out would hold the whole group */
                     if (nxt < P.nblocks) {
-                         bulk_wait_read();
-                         fence_proxy_async_smem();
-                         ct_issue<N>(P, &tmap, nxt, cur, &full[b]);
-                         atomicAdd(&issued[b], 1);
+                         pend_tile[g] = nxt;
+                         pend_slot[g] = b;
                     }
                }
           } else {
@@ -297,8 +330,16 @@ k_cols_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out,
                }
           }
      }
-     /* each leader's stores complete before the CTA ends; a group that gave
+     /* a refill still owed is issued (its tile belongs to another group);
+      * each leader's stores complete before the CTA ends; a group that gave
       * up may leave loads in flight: wait (bounded) for them */
+     if (gtid == 0 && pend_tile[g] >= 0) {
+          const int pb = pend_slot[g];
+          bulk_wait_read();
+          fence_proxy_async_smem();
+          ct_issue<N>(P, &tmap, pend_tile[g], base + ct_slot_off(N, tb, pb), &full[pb]);
+          atomicAdd(&issued[pb], 1);
+     }
      if (tstore && gtid == 0) bulk_wait_all();
      __syncthreads();
      if (threadIdx.x == 0) {
@@ -327,10 +368,10 @@ static const void *ct_lookup(int logn, int dir, int groups)
 extern "C" const void *gb_cols_tma_kernel(int logn, int dir, int groups) { return gb::ct_lookup<4>(logn, dir, groups); }
 
 /* Shared memory of a k_cols_tma CTA of g groups: g + 1 slots on 1024-byte
- * boundaries, the mbarriers and load counters, and the slack to align the
- * first slot. */
+ * boundaries, the mbarriers and load counters, each group's owed refill, and
+ * the slack to align the first slot. */
 extern "C" int gb_cols_tma_smem(int nfft, int tb, int groups)
 {
      return gb::ct_slot_off(nfft, tb, groups) + ((gb::ct_slot_bytes(nfft, tb) + 15) & ~15) + (groups + 1) * 16 +
-            1024;
+            groups * 16 + 1024;
 }
