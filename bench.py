@@ -480,7 +480,10 @@ def run_ours(args):
 def run_uneven(args):
     """10,000 independent fftwf c2c forward transforms of seeded uneven
     lengths as one plan set: one work-queue kernel in one CUDA graph launch
-    per step; beside it the same plans executed one after another."""
+    per step, the set planned with FFTW_MEASURE (the set tuner picks each
+    length's item body, radix order, prime algorithm and long split and keeps
+    them in wisdom); beside it the set with the planner's defaults and the
+    same plans executed one after another."""
     import ctypes
     import numpy as np
     import torch
@@ -507,27 +510,60 @@ def run_uneven(args):
     lib.fftwf_gb300_execute_set.argtypes = [ctypes.c_void_p]
     lib.fftwf_gb300_set_stream_set.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
     lib.fftwf_gb300_set_info.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 5
-    t0 = time.perf_counter()
-    s = lib.fftwf_gb300_plan_set(len(plans), arr, g.FFTW_ESTIMATE)
-    set_s = time.perf_counter() - t0
-    if not s:
-        raise RuntimeError("plan set failed: " + g.last_error())
     stream = torch.cuda.current_stream()
-    lib.fftwf_gb300_set_stream_set(s, stream.cuda_stream, 1)
-    info = [ctypes.c_int() for _ in range(5)]
-    lib.fftwf_gb300_set_info(s, *[ctypes.byref(v) for v in info])
     fl = sum(5.0 * n * math.log2(n) for n in lengths if n > 1)
-    for _ in range(args.warmup):
-        lib.fftwf_gb300_execute_set(s)
-    torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+
+    def make_set(flags):
+        t0 = time.perf_counter()
+        s = lib.fftwf_gb300_plan_set(len(plans), arr, flags)
+        if not s:
+            raise RuntimeError("plan set failed: " + g.last_error())
+        lib.fftwf_gb300_set_stream_set(s, stream.cuda_stream, 1)
+        return s, time.perf_counter() - t0
+
+    def time_set(s):
+        for _ in range(args.warmup):
+            lib.fftwf_gb300_execute_set(s)
+        torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
             lib.fftwf_gb300_execute_set(s)
         ev1.record(stream)
         torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / args.steps
+        return ev0.elapsed_time(ev1) / args.steps
+
+    # the planner's defaults, then the set tuner's choices (every length
+    # timed on scratch arrays within a 120 s limit, kept in wisdom)
+    s_est, est_build_s = make_set(g.FFTW_ESTIMATE)
+    if args.no_tune:
+        s, set_s, ms_est = s_est, est_build_s, None
+    else:
+        ms_est = time_set(s_est)
+        lib.fftwf_gb300_destroy_set.argtypes = [ctypes.c_void_p]
+        lib.fftwf_gb300_destroy_set(s_est)
+        lib.fftwf_set_timelimit(120.0)
+        s, set_s = make_set(g.FFTW_MEASURE)
+        lib.fftwf_set_timelimit(-1.0)
+    info = [ctypes.c_int() for _ in range(5)]
+    lib.fftwf_gb300_set_info(s, *[ctypes.byref(v) for v in info])
+    wis = ctypes.string_at(lib.fftwf_export_wisdom_to_string()).decode()
+    tuned = wis.count('"set p4 n')
+    # what the set tuner chose: fields variant tb load store n1 groups order
+    choices = {"register_body": 0, "rader": 0, "bluestein": 0, "other_split": 0, "radix_order": 0, "tile": 0}
+    for line in wis.splitlines():
+        if '"set p4 n' not in line:
+            continue
+        f = [int(v, 16) for v in line.split('"')[2].replace(")", "").replace("#x", "").split()]
+        f = [v - (1 << 32) if v >= 1 << 31 else v for v in f]
+        choices["register_body"] += f[0] == 0
+        choices["rader"] += f[0] == 5
+        choices["bluestein"] += f[0] == 3
+        choices["other_split"] += f[4] != 0
+        choices["radix_order"] += f[6] != 0
+        choices["tile"] += f[1] != 0
+    with ClockSampler(0) as clk:
+        ms = time_set(s)
     # the same plans one after another (async, one launch or more each)
     for p in plans:
         p.set_stream(stream.cuda_stream)
@@ -564,7 +600,12 @@ def run_uneven(args):
         "config": {"workload": f"uneven{count}: {count} fftwf c2c forward plans, seeded lengths (60% 2^6..2^16, 30% 2^a3^b5^c7^d in [60,60000], 10% primes in [17,4093]) as one plan set",
                    "distinct_lengths": len(set(lengths)), "points": int(offs[-1]),
                    "queue_items": info[0].value, "long_transforms": info[2].value, "grid": info[3].value,
-                   "smem": info[4].value, "plan_s": round(plan_s, 2), "set_build_s": round(set_s, 2),
+                   "smem": info[4].value, "plan_s": round(plan_s, 2), "set_tune_and_build_s": round(set_s, 2),
+                   "tuned_lengths": tuned, "tuner_choices": choices,
+                   "set_planning": "FFTW_ESTIMATE" if args.no_tune else "FFTW_MEASURE (the set tuner), 120 s limit",
+                   "estimate_set": None if ms_est is None else {
+                       "ms_per_step": round(ms_est, 4), "value": round(fl / (ms_est * 1e-3) / 1e9, 2),
+                       "build_s": round(est_build_s, 2)},
                    "rel_l2_max_sample": max(errs), "rel_l2_median_sample": float(np.median(errs)),
                    "sampled_transforms": len(sample)},
         "gbs": round(alg / (ms * 1e-3) / 1e9, 1),
@@ -689,6 +730,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tc", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="uneven10k: the planner's defaults only (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

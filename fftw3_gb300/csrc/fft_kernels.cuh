@@ -946,23 +946,31 @@ __device__ __forceinline__ void gen_stage(const C *src, C *dst, int N, int Ns, i
 {
      const int nb = N / RAD;
      const int twstep = N / (Ns * RAD);
-     for (int idx = threadIdx.x; idx < tb * nb; idx += blockDim.x) {
-          const int t = idx / nb;
-          const int j = idx - t * nb;
+     /* butterfly idx = t nb + j of transform t, j = jq Ns + k: the divisions
+      * are done once, and each step of blockDim.x advances (t, j, jq, k) by
+      * precomputed quotients and remainders (nb is a multiple of Ns) */
+     const int B = blockDim.x, nq = nb / Ns;
+     int t = threadIdx.x / nb, j = threadIdx.x - t * nb;
+     int jq = j / Ns, k = j - jq * Ns;
+     const int dt = B / nb, dj = B - dt * nb;
+     const int djq = dj / Ns, dk = dj - djq * Ns;
+     for (int idx = threadIdx.x; idx < tb * nb; idx += B) {
           const C *s = src + t * sms;
           C *d = dst + t * sms;
           C v[RAD];
 #pragma unroll
           for (int r = 0; r < RAD; ++r) v[r] = s[j + r * nb];
-          const int k = j % Ns;
           if (Ns > 1) {
 #pragma unroll
                for (int r = 1; r < RAD; ++r) v[r] = cmul(v[r], twid<DIR>(tw, r * k * twstep));
           }
           bfly<RAD, DIR>::run(v);
-          const int base = (j / Ns) * Ns * RAD + k;
+          const int base = jq * Ns * RAD + k;
 #pragma unroll
           for (int q = 0; q < RAD; ++q) d[base + q * Ns] = v[q];
+          t += dt; j += dj; jq += djq; k += dk;
+          if (k >= Ns) { k -= Ns; ++jq; }
+          if (j >= nb) { j -= nb; jq -= nq; ++t; }
      }
 }
 
@@ -1027,6 +1035,37 @@ __device__ __forceinline__ void tile_index(int idx, int tb, int L, int mode, int
      } else { t = idx / L; j = idx - t * L; }
 }
 
+/* idx = q D + r, walked in steps of B (the block) with one division at the
+ * start: each step adds B's quotient and remainder and carries once. */
+struct idx_walk {
+     int q, r, dq, dr, D;
+     __device__ __forceinline__ idx_walk(int idx, int D_, int B) : D(D_)
+     {
+          q = idx / D;
+          r = idx - q * D;
+          dq = B / D;
+          dr = B - dq * D;
+     }
+     __device__ __forceinline__ void step()
+     {
+          q += dq;
+          r += dr;
+          if (r >= D) { r -= D; ++q; }
+     }
+};
+
+/* tile_index as a walk: rows of L (t = q, j = r) or columns of tb (j = q,
+ * t = r) */
+struct tile_walk {
+     idx_walk w;
+     bool cols;
+     __device__ __forceinline__ tile_walk(int idx, int tb, int L, int mode, int B)
+         : w(idx, mode == GB_MOVE_COLS ? tb : L, B), cols(mode == GB_MOVE_COLS) {}
+     __device__ __forceinline__ int t() const { return cols ? w.r : w.q; }
+     __device__ __forceinline__ int j() const { return cols ? w.q : w.r; }
+     __device__ __forceinline__ void step() { w.step(); }
+};
+
 /* One tile of k_gen: load, stages (direction from P.sign), store.  Also the
  * body of the work-queue kernel.  b0/b1: two shared buffers of tb*(nfft+1). */
 template <typename C>
@@ -1049,16 +1088,17 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           C *dst = (kind == GB_KIND_C2C || kind == GB_KIND_R2C) ? b0 : b1;
           const int L = (kind == GB_KIND_RADER) ? n : (kind == GB_KIND_C2R) ? n / 2 + 1 : N;
           constexpr int U = 4;   /* loads in flight per thread */
+          tile_walk wk(threadIdx.x, tb, L, P.load_mode, blockDim.x);
           for (int idx0 = threadIdx.x; idx0 < tb * L; idx0 += U * blockDim.x) {
                C x[U];
                int slot[U];
 #pragma unroll
                for (int u = 0; u < U; ++u) {
                     const int idx = idx0 + u * blockDim.x;
+                    const int t = wk.t(), j = wk.j();
+                    wk.step();
                     slot[u] = -1;
                     if (idx < tb * L) {
-                         int t, j;
-                         tile_index(idx, tb, L, P.load_mode, t, j, P.ltb);
                          if (tile.v0 + t < vn0) {
                               if (kind == GB_KIND_R2C) {
                                    const R *r = (const R *)src_of<R>(P, tile, A, t);
@@ -1085,9 +1125,9 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
      } else if (kind == GB_KIND_BLUESTEIN) {
           /* b = x conj(w), zero-padded to nfft (dft/bluestein.c:82-95) */
           const C *__restrict__ w = (const C *)P.chirp;
-          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
-               int t, j;
-               tile_index(idx, tb, N, P.load_mode, t, j, P.ltb);
+          tile_walk wk(threadIdx.x, tb, N, P.load_mode, blockDim.x);
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
+               const int t = wk.t(), j = wk.j();
                C x = mk<C>(0, 0);
                if (j < n && tile.v0 + t < vn0) x = cmul(src_of<C>(P, tile, A, t)[j * P.is], cconj(__ldg(w + j)));
                b0[t * sms + j] = x;
@@ -1097,8 +1137,9 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
      if (kind == GB_KIND_RADER) {
           /* dft/rader.c:95-165: b[k] = x[g^k], k < n-1; x[0] kept in the unused
            * slot N of buffer 0 */
-          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
-               const int t = idx / N, k = idx - t * N;
+          idx_walk wk(threadIdx.x, N, blockDim.x);
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
+               const int t = wk.q, k = wk.r;
                b0[t * sms + k] = b1[t * sms + __ldg(P.perm + k)];
                if (k == 0) b0[t * sms + N] = b1[t * sms];
           }
@@ -1137,8 +1178,9 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
            * also records X[0] = x[0] + B[0] in slot N of buffer 1. */
           res = gen_fft<C, -1>(b0, b1, P, N, sms, tw);
           const C *__restrict__ W = (const C *)P.chirp_spec;
-          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
-               const int t = idx / N, k = idx - t * N;
+          idx_walk wk(threadIdx.x, N, blockDim.x);
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
+               const int t = wk.q, k = wk.r;
                const C bk = res[t * sms + k];
                if (kind == GB_KIND_RADER && k == 0) b1[t * sms + N] = cadd(b0[t * sms + N], bk);
                res[t * sms + k] = cmul(bk, __ldg(W + k));
@@ -1153,9 +1195,9 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
 
      /* ---------------- store ---------------- */
      if (kind == GB_KIND_C2C) {
-          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
-               int t, k;
-               tile_index(idx, tb, N, P.store_mode, t, k, P.ltb);
+          tile_walk wk(threadIdx.x, tb, N, P.store_mode, blockDim.x);
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
+               const int t = wk.t(), k = wk.j();
                const long long v = tile.v0 + t;
                if (v < vn0) {
                     C y = res[t * sms + k];
@@ -1166,18 +1208,18 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
      } else if (kind == GB_KIND_BLUESTEIN) {
           /* X[k] = conv[k] conj(w[k]), k < n */
           const C *__restrict__ w = (const C *)P.chirp;
-          for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x) {
-               int t, k;
-               tile_index(idx, tb, n, P.store_mode, t, k, P.ltb);
+          tile_walk wk(threadIdx.x, tb, n, P.store_mode, blockDim.x);
+          for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x, wk.step()) {
+               const int t = wk.t(), k = wk.j();
                if (tile.v0 + t < vn0)
                     dst_of<C>(P, tile, A, t)[k * P.os] = cmul(res[t * sms + k], cconj(__ldg(w + k)));
           }
      } else if (kind == GB_KIND_RADER) {
           /* X[0] from slot N of buffer 1; X[g^-k] = x[0] + conv[k] */
           const int *__restrict__ lg = P.perm + N;
-          for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x) {
-               int t, j;
-               tile_index(idx, tb, n, P.store_mode, t, j, P.ltb);
+          tile_walk wk(threadIdx.x, tb, n, P.store_mode, blockDim.x);
+          for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x, wk.step()) {
+               const int t = wk.t(), j = wk.j();
                if (tile.v0 + t < vn0) {
                     const C y = (j == 0) ? b1[t * sms + N] : cadd(b0[t * sms + N], res[t * sms + __ldg(lg + j - 1)]);
                     dst_of<C>(P, tile, A, t)[j * P.os] = y;

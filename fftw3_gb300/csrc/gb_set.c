@@ -19,13 +19,25 @@
  * row tiles, so no wait can block a claimed item.  Prime singles whose
  * convolution needs twice the tile (nb up to 8192 single / 4096 double) go to
  * a second queue with larger tiles, launched first in the same graph.
+ *
+ * Per length, the items' configuration is the tuner's when wisdom holds an
+ * entry "set p<prec> n<n>" (the item body, register stages or runtime-radix
+ * stages; the radix order; Rader or Bluestein for a prime; the split of a long
+ * length; transforms per item), else the planner's defaults.  A set planned
+ * without FFTW_ESTIMATE tunes every length wisdom does not cover: each
+ * candidate runs as a set of that length alone on scratch device arrays,
+ * timed with CUDA events, and the fastest is stored in wisdom (exported with
+ * fftw_export_wisdom), as the reference's measuring planner times candidate
+ * plans (kernel/planner.c:518-615, kernel/timer.c:142-181).
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
 #include <stddef.h>
+#include <time.h>
 #include <cuda_runtime_api.h>
+#include "fftw3.h"
 #include "gb_host.h"
 
 #define GB_Q_GROUP 32
@@ -74,7 +86,8 @@ static long long pow2_at_least(long long v)
 
 /* Fill the pass fields a queue item needs (the shared-memory tile body). */
 static int item_pass(gb_pass *P, int prec, int kind, long long n, int sign, long long is, long long os,
-                     long long vn0, long long vis0, long long vos0, int tb, int cols_in, int cols_out, int threads)
+                     long long vn0, long long vis0, long long vos0, int tb, int cols_in, int cols_out, int threads,
+                     int body, int order)
 {
      memset(P, 0, sizeof *P);
      P->ltb = -1;
@@ -90,10 +103,21 @@ static int item_pass(gb_pass *P, int prec, int kind, long long n, int sign, long
      P->nv = 1;
      P->vn[0] = vn0; P->vis[0] = vis0; P->vos[0] = vos0;
      P->ntiles0 = 1; P->nblocks = 1;
-     P->nrad = gb_factor_radices(P->nfft, P->rad);
+     P->nrad = (kind == GB_KIND_C2C && order > 0) ? gb_factor_order(P->nfft, P->rad, order)
+                                                   : gb_factor_radices(P->nfft, P->rad);
      if (P->nrad < 0) return -1;
      if (gb_pass_tables(P)) return -1;
      if (P->ltb >= 0 && (1 << P->ltb) != P->tb) return -1;
+     /* the register body (when asked for) of a power-of-two float c2c of
+      * 64..4096 points in the small-tile queue: 256 / (nfft/16) transforms a
+      * round; the shared memory holds a round of the register layout (rows
+      * beyond the item's transforms included) */
+     if (body == GB_VAR_REG && kind == GB_KIND_C2C && prec == 4 && threads == 256 && P->nfft >= 64 &&
+         P->nfft <= 4096 && (P->nfft & (P->nfft - 1)) == 0 && (long long)tb * (P->nfft / 16) <= 256) {
+          const int round = 256 / (P->nfft / 16), lay = round * gb_reg_sms(P->nfft) * 2 * prec;
+          P->variant = GB_VAR_REG;
+          if (lay > P->smem) P->smem = lay;
+     }
      return 0;
 }
 
@@ -135,11 +159,49 @@ static int cmp_key(const void *a, const void *b)
      return 0;
 }
 
+/* The configuration of one length's items in a set. */
+typedef struct {
+     int body;       /* GB_VAR_REG or GB_VAR_GEN: the body of power-of-two float items */
+     int order;      /* radix order of runtime-radix items (gb_factor_order) */
+     int prime;      /* GB_KIND_RADER / GB_KIND_BLUESTEIN for a prime, 0: the planner's */
+     int tbmax;      /* transforms per single item, 0: as many as the tile holds (up to 32) */
+     long long n1;   /* split n = n1 * n2 of a long length, 0: the planner's */
+} set_cfg;
+
+static void set_key(char *key, size_t cap, int prec, long long n) { snprintf(key, cap, "set p%d n%lld", prec, n); }
+
+/* A length's configuration: the wisdom entry "set p<prec> n<n>" (variant =
+ * the body of a smooth length's items or the kind of a prime's, tb = the
+ * transforms per item, n1 = the split, order = the radix order), else the
+ * defaults (runtime-radix body, order 0).  FFTW_GB300_QUEUE_BODY=reg|gen
+ * overrides the body. */
+static set_cfg length_cfg(int prec, long long n)
+{
+     set_cfg c = {GB_VAR_GEN, 0, 0, 0, 0};
+     char key[64];
+     const gb_wisdom_entry *w;
+     const char *e = getenv("FFTW_GB300_QUEUE_BODY");
+     set_key(key, sizeof key, prec, n);
+     w = gb_wisdom_lookup(key);
+     if (w) {
+          if (w->variant == GB_VAR_REG || w->variant == GB_VAR_GEN) c.body = w->variant;
+          if (w->variant == GB_KIND_RADER || w->variant == GB_KIND_BLUESTEIN) c.prime = w->variant;
+          c.order = w->order;
+          c.tbmax = w->tb;
+          c.n1 = w->n1;
+     }
+     if (e && !strcmp(e, "reg")) c.body = GB_VAR_REG;
+     else if (e && !strcmp(e, "gen")) c.body = GB_VAR_GEN;
+     return c;
+}
+
 /* How a prime (or non-smooth) length runs as a single: Rader (n-1 smooth)
  * or Bluestein (power-of-two convolution), in the small-tile queue when its
- * FFT fits cap_s, else in the large-tile queue (cap_l).  *large is set for
- * the latter; -1 when neither fits. */
-static int prime_kind(int prec, long long n, int cap_s, int cap_l, int *large)
+ * FFT fits cap_s, else in the large-tile queue (cap_l).  want is the set
+ * tuner's choice (0: none; then the plan tuner's wisdom or
+ * FFTW_GB300_PRIME=rader asks for Rader).  *large is set for the latter; -1
+ * when neither fits. */
+static int prime_kind(int prec, long long n, int cap_s, int cap_l, int want, int *large)
 {
      int rad[GB_MAXRAD];
      const char *e = getenv("FFTW_GB300_PRIME");
@@ -150,7 +212,12 @@ static int prime_kind(int prec, long long n, int cap_s, int cap_l, int *large)
      int want_rader;
      snprintf(key, sizeof key, "c2c p%d n%lld", prec, n);
      w = gb_wisdom_lookup(key);
-     want_rader = rader && ((w && w->variant == GB_KIND_RADER) || (!w && e && !strcmp(e, "rader")));
+     if (want) want_rader = rader && want == GB_KIND_RADER;
+     else want_rader = rader && ((w && w->variant == GB_KIND_RADER) || (!w && e && !strcmp(e, "rader")));
+     if (want == GB_KIND_BLUESTEIN && nb <= cap_l) {
+          *large = nb > cap_s;
+          return GB_KIND_BLUESTEIN;
+     }
      *large = 0;
      if (want_rader && n - 1 <= cap_s) return GB_KIND_RADER;
      if (nb <= cap_s) return GB_KIND_BLUESTEIN;
@@ -162,25 +229,45 @@ static int prime_kind(int prec, long long n, int cap_s, int cap_l, int *large)
      return -1;
 }
 
+/* small-tile queue: 2 x (4096+1) complex64 (2048 complex128) = 65.5 KB,
+ * three 256-thread CTAs per SM; large-tile queue: twice that, one 512-thread
+ * CTA per SM, only for what the small tiles cannot hold */
+static int cap_small(int prec) { return prec == 4 ? 4096 : 2048; }
+
+/* Splits n = d * (n / d) of a long length with both factors within a tile
+ * and 13-smooth, d ascending (at most maxd of them). */
+static int long_splits(long long n, int cap, long long *d, int maxd)
+{
+     int rad[GB_MAXRAD], k = 0;
+     long long q;
+     for (q = 2; q <= cap && k < maxd; ++q)
+          if (n % q == 0 && n / q <= cap && gb_factor_radices(q, rad) >= 0 && gb_factor_radices(n / q, rad) >= 0)
+               d[k++] = q;
+     return k;
+}
+
+/* The split of a long length: the configured n1 when it is one of the
+ * splits, else the largest n1 <= sqrt(n) (0: none). */
+static long long long_n1(long long n, int cap, long long want)
+{
+     long long d[64], best = 0;
+     int k = long_splits(n, cap, d, 64), i;
+     for (i = 0; i < k; ++i) {
+          if (d[i] == want) return want;
+          if (d[i] * d[i] <= n) best = d[i];
+     }
+     return best;
+}
+
+static gb_set *build_set(int prec, xform *xs, int nx);
+static void tune_set(int prec, const xform *xs, int nx, unsigned flags);
+
 gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
 {
      gb_set *S;
      xform *xs;
-     int nx = 0, i, j;
-     /* small-tile queue: 2 x (4096+1) complex64 (2048 complex128) = 65.5 KB,
-      * three 256-thread CTAs per SM; large-tile queue: twice that, one
-      * 512-thread CTA per SM, only for what the small tiles cannot hold */
-     const int cap_s = prec == 4 ? 4096 : 2048, cap_l = 2 * cap_s, cap = cap_s;
-     int cs = 2 * prec;
-     qvec QA = {0, 0, 0}, QM = {0, 0, 0}, QB = {0, 0, 0}, QL = {0, 0, 0};
-     gb_qitem *A, *M, *B, *Lg;
-     int na, nm, nb, nl;
-     int smem_l = 0;
-     void **hptr = 0;
-     int nptr = 0, cap_ptr;
-     long long scratch_elems = 0;
-     int nctr = 0, smem = 0;
-     (void)flags;
+     int nx = 0, i;
+     const int cs = 2 * prec;
      if (gb_dry_run() || !gb_cuda_ready()) {
           gb_set_error("plan sets need a GPU");
           return 0;
@@ -207,6 +294,41 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                x->out = (char *)pr->out + (pr->vrank ? t * pr->vec[0].os : 0) * cs;
           }
      }
+     if (flags & FFTW_WISDOM_ONLY) {
+          /* every length needs the tuner's entry */
+          for (i = 0; i < nx; ++i) {
+               char key[64];
+               set_key(key, sizeof key, prec, xs[i].n);
+               if (!gb_wisdom_lookup(key)) {
+                    gb_set_error("plan set: FFTW_WISDOM_ONLY and no wisdom for length %lld", xs[i].n);
+                    free(xs);
+                    return 0;
+               }
+          }
+     } else if (!(flags & FFTW_ESTIMATE)) {
+          tune_set(prec, xs, nx, flags);
+     }
+     S = build_set(prec, xs, nx);
+     free(xs);
+     return S;
+}
+
+/* The queue items of transforms xs (sorted here), their device copies and
+ * the set that runs them. */
+static gb_set *build_set(int prec, xform *xs, int nx)
+{
+     gb_set *S;
+     int i, j;
+     const int cap_s = cap_small(prec), cap_l = 2 * cap_s, cap = cap_s;
+     int cs = 2 * prec;
+     qvec QA = {0, 0, 0}, QM = {0, 0, 0}, QB = {0, 0, 0}, QL = {0, 0, 0};
+     gb_qitem *A, *M, *B, *Lg;
+     int na, nm, nb, nl;
+     int smem_l = 0;
+     void **hptr = 0;
+     int nptr = 0, cap_ptr;
+     long long scratch_elems = 0;
+     int nctr = 0, smem = 0;
      qsort(xs, (size_t)nx, sizeof(xform), cmp_key);
      cap_ptr = 2 * nx + 2;
      hptr = (void **)calloc((size_t)cap_ptr, sizeof(void *));
@@ -216,8 +338,9 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           long long n = x->n;
           int rad[GB_MAXRAD], kind = GB_KIND_C2C, g, large = 0;
           int smooth = gb_factor_radices(n, rad) >= 0;
+          const set_cfg cf = length_cfg(prec, n);
           if (n <= cap_s && smooth) kind = GB_KIND_C2C;
-          else if (!smooth && (kind = prime_kind(prec, n, cap_s, cap_l, &large)) > 0) { /* single */ }
+          else if (!smooth && (kind = prime_kind(prec, n, cap_s, cap_l, cf.prime, &large)) > 0) { /* single */ }
           else kind = -1;
           if (kind >= 0) {
                /* group transforms with the same key */
@@ -226,9 +349,11 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                long long nfft = kind == GB_KIND_BLUESTEIN ? pow2_at_least(2 * n - 1) : kind == GB_KIND_RADER ? n - 1 : n;
                int tbmax = (int)((2LL * (cq + 1) * cs) / (2LL * (nfft + 1) * cs));
                if (tbmax > GB_Q_GROUP) tbmax = GB_Q_GROUP;
+               if (cf.tbmax > 0 && cf.tbmax < tbmax) tbmax = cf.tbmax;
                if (tbmax < 1) tbmax = 1;
                for (g = 0; i + g < nx && g < tbmax && cmp_key(&xs[i], &xs[i + g]) == 0; ++g) {}
-               if (item_pass(&tmp, prec, kind, n, x->sign, x->is, x->os, g, 0, 0, g, 0, 0, thr)) goto fail;
+               if (item_pass(&tmp, prec, kind, n, x->sign, x->is, x->os, g, 0, 0, g, 0, 0, thr, cf.body, cf.order))
+                    goto fail;
                {
                     gb_qitem *q = qpush(large ? &QL : &QM);
                     if (!q) goto fail;
@@ -250,20 +375,20 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           }
           {
                /* long transform: n = n1 * n2 with both factors in one CTA */
-               long long n1 = 0, n2, d, k0;
+               long long n1 = long_n1(n, cap, cf.n1), n2, k0;
                int tbc = prec == 4 ? 16 : 8, ctr = nctr++;
                gb_pass pa, pb;
                int nta = 0;
-               for (d = 2; d * d <= n; ++d)
-                    if (n % d == 0 && d <= cap && n / d <= cap && gb_factor_radices(d, rad) >= 0 &&
-                        gb_factor_radices(n / d, rad) >= 0)
-                         n1 = d;
                if (!n1) { gb_set_error("plan set: length %lld has no two-pass split", n); goto fail; }
                n2 = n / n1;
+               /* columns per tile: the tuner's (a power of two) or 16 (8 double) */
+               if (cf.tbmax > 0 && cf.tbmax < tbc && (cf.tbmax & (cf.tbmax - 1)) == 0) tbc = cf.tbmax;
                while (tbc > 1 && 2LL * tbc * ((n1 > n2 ? n1 : n2) + 1) * cs > 2LL * (cap + 1) * cs) tbc >>= 1;
                /* pass A: columns n2 (stride is), n1-point transforms with
                 * element stride n2*is into scratch [n2][k1] */
-               if (item_pass(&pa, prec, GB_KIND_C2C, n1, x->sign, n2 * x->is, 1, n2, x->is, n1, tbc, 1, 0, 256)) goto fail;
+               if (item_pass(&pa, prec, GB_KIND_C2C, n1, x->sign, n2 * x->is, 1, n2, x->is, n1, tbc, 1, 0, 256, cf.body,
+                             cf.order))
+                    goto fail;
                pa.post_N = n;
                if (gb_pass_tables(&pa)) goto fail;
                for (k0 = 0; k0 < n2; k0 += tbc) {
@@ -279,7 +404,9 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                if (pa.smem > smem) smem = pa.smem;
                /* pass B: k1 columns of scratch (stride 1), n2-point transforms
                 * with element stride n1, into out[k1 + n1*k2] */
-               if (item_pass(&pb, prec, GB_KIND_C2C, n2, x->sign, n1, n1 * x->os, n1, 1, x->os, tbc, 1, 1, 256)) goto fail;
+               if (item_pass(&pb, prec, GB_KIND_C2C, n2, x->sign, n1, n1 * x->os, n1, 1, x->os, tbc, 1, 1, 256, cf.body,
+                             cf.order))
+                    goto fail;
                for (k0 = 0; k0 < n1; k0 += tbc) {
                     gb_qitem *q = qpush(&QB);
                     if (!q) goto fail;
@@ -365,10 +492,10 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
           }
           free(all);
      }
-     free(QA.v); free(QM.v); free(QB.v); free(QL.v); free(hptr); free(xs);
+     free(QA.v); free(QM.v); free(QB.v); free(QL.v); free(hptr);
      return S;
 fail:
-     free(QA.v); free(QM.v); free(QB.v); free(QL.v); free(hptr); free(xs);
+     free(QA.v); free(QM.v); free(QB.v); free(QL.v); free(hptr);
      return 0;
 }
 
@@ -506,4 +633,176 @@ void gb_destroy_set(gb_set *S)
      cudaFree(S->d_ptrs);
      if (S->d_scratch) cudaFree(S->d_scratch);
      free(S);
+}
+
+/* ---- set tuner ---- */
+
+static double set_now_s(void)
+{
+     struct timespec ts;
+     clock_gettime(CLOCK_MONOTONIC, &ts);
+     return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+/* ms per execute (best of reps) of a set of cnt transforms of length n on
+ * the scratch arrays, under the configuration wisdom now holds for n; 1e30
+ * when it does not build or run */
+static double time_candidate(int prec, long long n, int sign, int cnt, char *din, char *dout, cudaStream_t st,
+                             int reps)
+{
+     const int cs = 2 * prec;
+     xform *xs = (xform *)malloc(sizeof(xform) * (size_t)cnt);
+     gb_set *S;
+     double best = 1e30;
+     int i;
+     if (!xs) return best;
+     for (i = 0; i < cnt; ++i) {
+          xs[i].n = n; xs[i].sign = sign; xs[i].is = 1; xs[i].os = 1;
+          xs[i].in = din + (size_t)i * (size_t)n * cs;
+          xs[i].out = dout + (size_t)i * (size_t)n * cs;
+     }
+     S = build_set(prec, xs, cnt);
+     free(xs);
+     if (!S) return best;
+     gb_set_stream_of_set(S, st, 1);
+     if (!gb_execute_set(S)) {
+          cudaEvent_t a, b;
+          cudaEventCreate(&a);
+          cudaEventCreate(&b);
+          for (i = 0; i < reps; ++i) {
+               float ms;
+               cudaEventRecord(a, st);
+               if (gb_execute_set(S)) { best = 1e30; break; }
+               cudaEventRecord(b, st);
+               if (cudaEventSynchronize(b) != cudaSuccess) { best = 1e30; break; }
+               cudaEventElapsedTime(&ms, a, b);
+               if (ms < best) best = ms;
+          }
+          cudaEventDestroy(a);
+          cudaEventDestroy(b);
+     }
+     cudaStreamSynchronize(st);
+     gb_destroy_set(S);
+     return best;
+}
+
+/* a radix order whose stage list differs from the default's */
+static int order_differs(long long n, int order)
+{
+     int r0[GB_MAXRAD], r1[GB_MAXRAD], k0 = gb_factor_radices(n, r0), k1 = gb_factor_order(n, r1, order), i;
+     if (k1 < 0) return 0;
+     if (k0 != k1) return 1;
+     for (i = 0; i < k0; ++i)
+          if (r0[i] != r1[i]) return 1;
+     return 0;
+}
+
+typedef struct { long long n, pts; int sign; } lclass;
+
+static int cmp_class_pts(const void *a, const void *b)
+{
+     const lclass *x = (const lclass *)a, *y = (const lclass *)b;
+     return x->pts < y->pts ? 1 : x->pts > y->pts ? -1 : 0;
+}
+
+/* Tune every length of the set that wisdom does not cover, lengths with
+ * the most points first, within fftw_set_timelimit. */
+static void tune_set(int prec, const xform *xs, int nx, unsigned flags)
+{
+     const int cap_s = cap_small(prec), cap_l = 2 * cap_s, cs = 2 * prec;
+     const long long target = 1LL << 21;   /* points of a candidate's timing set */
+     const int patient = (flags & (FFTW_PATIENT | FFTW_EXHAUSTIVE)) != 0, reps = patient ? 7 : 3;
+     double t0 = set_now_s(), limit = gb_get_timelimit();
+     xform *srt;
+     lclass *cl;
+     int ncl = 0, i, k;
+     long long maxn = 0;
+     char *din = 0, *dout = 0;
+     cudaStream_t st = 0;
+     if (nx <= 0) return;
+     srt = (xform *)malloc(sizeof(xform) * (size_t)nx);
+     cl = (lclass *)malloc(sizeof(lclass) * (size_t)nx);
+     if (!srt || !cl) { free(srt); free(cl); return; }
+     memcpy(srt, xs, sizeof(xform) * (size_t)nx);
+     qsort(srt, (size_t)nx, sizeof(xform), cmp_key);
+     for (i = 0; i < nx;) {
+          int j = i;
+          long long pts = 0;
+          while (j < nx && srt[j].n == srt[i].n) pts += srt[j++].n;
+          cl[ncl].n = srt[i].n; cl[ncl].sign = srt[i].sign; cl[ncl].pts = pts;
+          if (srt[i].n > maxn) maxn = srt[i].n;
+          ++ncl;
+          i = j;
+     }
+     free(srt);
+     qsort(cl, (size_t)ncl, sizeof(lclass), cmp_class_pts);
+     {
+          size_t bytes = (size_t)(maxn > target ? maxn : target) * cs;
+          if (cudaMalloc((void **)&din, bytes) != cudaSuccess || cudaMalloc((void **)&dout, bytes) != cudaSuccess ||
+              cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+               cudaGetLastError();
+               goto done;
+          }
+          cudaMemset(din, 0, bytes);
+     }
+     for (k = 0; k < ncl; ++k) {
+          const long long n = cl[k].n;
+          char key[64];
+          gb_wisdom_entry cand[8], best_e;
+          int nc = 1, c, rad[GB_MAXRAD], cnt;
+          const int smooth = gb_factor_radices(n, rad) >= 0, pow2 = (n & (n - 1)) == 0;
+          double best = 1e30;
+          if (limit > 0 && set_now_s() - t0 > limit) break;
+          set_key(key, sizeof key, prec, n);
+          if (gb_wisdom_lookup(key)) continue;
+          memset(cand, 0, sizeof cand);
+          for (c = 0; c < 8; ++c) cand[c].variant = -1;
+          /* cand[0]: the defaults */
+          if (smooth && n <= cap_s) {
+               if (prec == 4 && pow2 && n >= 64 && n <= 4096) cand[nc++].variant = GB_VAR_REG;
+               else if (!pow2)
+                    for (c = 1; c < GB_RADIX_ORDERS; ++c)
+                         if (order_differs(n, c)) cand[nc++].order = c;
+               if (patient && n <= 1024) { cand[nc].tb = 8; ++nc; }
+          } else if (smooth) {
+               long long d[64], def = long_n1(n, cap_s, 0);
+               int nd = long_splits(n, cap_s, d, 64), at = -1;
+               for (c = 0; c < nd; ++c)
+                    if (d[c] == def) at = c;
+               if (at > 0) cand[nc++].n1 = (int)d[at - 1];
+               if (at >= 0 && at + 1 < nd) cand[nc++].n1 = (int)d[at + 1];
+               if (prec == 4 && pow2) cand[nc++].variant = GB_VAR_REG;
+               if (patient) { cand[nc].tb = 8; ++nc; }
+          } else if (is_prime_ll(n) && n - 1 <= cap_l && gb_factor_radices(n - 1, rad) >= 0 &&
+                     pow2_at_least(2 * n - 1) <= cap_l) {
+               /* the other algorithm than the planner's choice */
+               int large;
+               const int def = prime_kind(prec, n, cap_s, cap_l, 0, &large);
+               cand[nc++].variant = def == GB_KIND_RADER ? GB_KIND_BLUESTEIN : GB_KIND_RADER;
+          }
+          best_e = cand[0];
+          if (nc > 1) {
+               cnt = (int)(target / n);
+               if (cnt < 1) cnt = 1;
+               for (c = 0; c < nc; ++c) {
+                    double t;
+                    if (c > 0 && limit > 0 && set_now_s() - t0 > limit) break;
+                    strcpy(cand[c].key, key);
+                    gb_wisdom_store(&cand[c]);
+                    t = time_candidate(prec, n, cl[k].sign, cnt, din, dout, st, reps);
+                    /* a set of one length alone only approximates the mix:
+                     * another configuration replaces the defaults (cand[0])
+                     * when it is faster by more than 5% */
+                    if (c > 0) t *= 1.05;
+                    if (t < best) { best = t; best_e = cand[c]; }
+               }
+          }
+          strcpy(best_e.key, key);
+          gb_wisdom_store(&best_e);
+     }
+done:
+     if (st) cudaStreamDestroy(st);
+     if (din) cudaFree(din);
+     if (dout) cudaFree(dout);
+     free(cl);
 }

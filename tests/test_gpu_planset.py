@@ -48,7 +48,7 @@ def _check(restatement, xin, yout, offs, lengths, prec, sign, sample=None):
     return worst
 
 
-def _set_of(plans, prec):
+def _set_of(plans, prec, flags=None):
     import fftw3_gb300 as g
     lib = g.load()
     pfx = "fftwf_" if prec == "f" else "fftw_"
@@ -56,7 +56,7 @@ def _set_of(plans, prec):
     f = getattr(lib, pfx + "gb300_plan_set")
     f.restype = ctypes.c_void_p
     f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint]
-    s = f(len(plans), arr, g.FFTW_ESTIMATE)
+    s = f(len(plans), arr, g.FFTW_ESTIMATE if flags is None else flags)
     assert s, g.last_error()
     getattr(lib, pfx + "gb300_execute_set").argtypes = [ctypes.c_void_p]
     getattr(lib, pfx + "gb300_destroy_set").argtypes = [ctypes.c_void_p]
@@ -96,6 +96,74 @@ def test_planset_mixed_lengths(lib, torch_cuda_set, restatement, prec):
     torch.cuda.synchronize()
     assert rel_l2(y2.cpu().numpy(), y1.cpu().numpy()) < (2e-6 if prec == "f" else 1e-13)
     getattr(lib_, pfx + "gb300_destroy_set")(s)
+
+
+def test_planset_register_body(lib, torch_cuda_set, restatement, monkeypatch):
+    """Power-of-two float items (64..4096 points: singles and the passes of
+    long lengths) with the register-stage body instead of the runtime-radix
+    one: every transform against the oracle, and the same set with the
+    runtime-radix body agrees."""
+    torch = torch_cuda_set
+    import bench
+    lengths = bench.uneven_lengths(np.random.default_rng(9), 200)
+    lengths += [64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384, 32768, 65536, 60000, 97]
+    xin, yout, offs, plans = _make_set(torch, lengths, "f", seed=9)
+    monkeypatch.setenv("FFTW_GB300_QUEUE_BODY", "reg")
+    lib_, pfx, s = _set_of(plans, "f")
+    assert getattr(lib_, pfx + "gb300_execute_set")(s) == 0
+    torch.cuda.synchronize()
+    assert lib_.fftw_gb300_device_status() == 0
+    _check(restatement, xin, yout, offs, lengths, "f", -1)
+    y_reg = yout.clone()
+    getattr(lib_, pfx + "gb300_destroy_set")(s)
+    monkeypatch.setenv("FFTW_GB300_QUEUE_BODY", "gen")
+    lib_, pfx, s = _set_of(plans, "f")
+    yout.zero_()
+    assert getattr(lib_, pfx + "gb300_execute_set")(s) == 0
+    torch.cuda.synchronize()
+    assert rel_l2(yout.cpu().numpy(), y_reg.cpu().numpy()) < 2e-6
+    getattr(lib_, pfx + "gb300_destroy_set")(s)
+
+
+def test_planset_tuned(lib, torch_cuda_set, restatement):
+    """A set planned with FFTW_MEASURE: every length is tuned (item body,
+    radix order, Rader or Bluestein, long split) on scratch arrays and
+    recorded in wisdom as "set p4 n<n>"; the tuned set is correct; the same
+    set plans under FFTW_WISDOM_ONLY from the exported wisdom, and a length
+    wisdom does not cover is refused."""
+    import fftw3_gb300 as g
+    torch = torch_cuda_set
+    lib_ = g.load()
+    lib_.fftwf_forget_wisdom()
+    lengths = [64, 64, 256, 1024, 4096, 60, 210, 1000, 3000, 97, 193, 4093, 8192, 16384, 65536, 60000, 6000] * 3
+    xin, yout, offs, plans = _make_set(torch, lengths, "f", seed=13)
+    lib_.fftwf_set_timelimit(120.0)
+    xin_copy = xin.clone()
+    _, pfx, s = _set_of(plans, "f", flags=g.FFTW_MEASURE)
+    lib_.fftwf_set_timelimit(-1.0)
+    # tuning ran on scratch arrays: the caller's input is untouched
+    assert torch.equal(xin, xin_copy)
+    w = ctypes.string_at(lib_.fftwf_export_wisdom_to_string()).decode()
+    for n in set(lengths):
+        assert f'"set p4 n{n}"' in w, n
+    assert lib_.fftwf_gb300_execute_set(s) == 0
+    torch.cuda.synchronize()
+    assert lib_.fftw_gb300_device_status() == 0
+    _check(restatement, xin, yout, offs, lengths, "f", -1)
+    lib_.fftwf_gb300_destroy_set(s)
+    # wisdom round trip: forget, import, plan with FFTW_WISDOM_ONLY
+    lib_.fftwf_forget_wisdom()
+    assert lib_.fftwf_import_wisdom_from_string(w.encode()) == 1
+    _, pfx, s = _set_of(plans, "f", flags=g.FFTW_ESTIMATE | g.FFTW_WISDOM_ONLY)
+    yout.zero_()
+    assert lib_.fftwf_gb300_execute_set(s) == 0
+    torch.cuda.synchronize()
+    _check(restatement, xin, yout, offs, lengths, "f", -1)
+    lib_.fftwf_gb300_destroy_set(s)
+    extra = g.plan_many_dft([5000], 1, xin.data_ptr(), yout.data_ptr(), -1, g.FFTW_ESTIMATE, "f")
+    arr = (ctypes.c_void_p * (len(plans) + 1))(*([p.ptr for p in plans] + [extra.ptr]))
+    assert not lib_.fftwf_gb300_plan_set(len(plans) + 1, arr, g.FFTW_ESTIMATE | g.FFTW_WISDOM_ONLY)
+    lib_.fftwf_forget_wisdom()
 
 
 def test_planset_backward_and_rader(lib, torch_cuda_set, restatement, monkeypatch):
