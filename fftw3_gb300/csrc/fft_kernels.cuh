@@ -940,6 +940,32 @@ k_reg_tma(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
  * k_gen: runtime radix list, shared-memory ping-pong
  * ==================================================================== */
 
+/* Shared-memory layout of the runtime-radix body: element i of a transform
+ * at gpad(i) = i + i/16, transforms gen_sms(N) = N + N/16 + 1 apart.  The
+ * gap after every 16 elements spreads the Stockham stores of the first
+ * stages (16 j + q, 8 j + q, 4 j + q, ... for consecutive j) over the banks,
+ * and the odd stride keeps adjacent transforms (column tiles) apart. */
+__device__ __forceinline__ int gpad(int i) { return i + (i >> 4); }
+
+/* One element copied global -> shared without passing through registers
+ * (cp.async: 8 bytes through L1 for complex float, 16 bytes around it for
+ * complex double), so a thread keeps all its tile loads in flight at once;
+ * cp_async_wait_all completes the thread's copies. */
+template <typename C> __device__ __forceinline__ void cp_async_elem(C *dst, const C *src)
+{
+     const unsigned d = smem_u32(dst);
+     if constexpr (sizeof(C) == 16)
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+     else
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all_groups()
+{
+     asm volatile("cp.async.commit_group;" ::: "memory");
+     asm volatile("cp.async.wait_all;" ::: "memory");
+}
+__host__ __device__ constexpr int gen_sms(int nfft) { return nfft + (nfft >> 4) + 1; }
+
 template <typename C, int DIR, int RAD>
 __device__ __forceinline__ void gen_stage(const C *src, C *dst, int N, int Ns, int tb, int sms,
                                           const C *__restrict__ tw)
@@ -959,7 +985,7 @@ __device__ __forceinline__ void gen_stage(const C *src, C *dst, int N, int Ns, i
           C *d = dst + t * sms;
           C v[RAD];
 #pragma unroll
-          for (int r = 0; r < RAD; ++r) v[r] = s[j + r * nb];
+          for (int r = 0; r < RAD; ++r) v[r] = s[gpad(j + r * nb)];
           if (Ns > 1) {
 #pragma unroll
                for (int r = 1; r < RAD; ++r) v[r] = cmul(v[r], twid<DIR>(tw, r * k * twstep));
@@ -967,7 +993,7 @@ __device__ __forceinline__ void gen_stage(const C *src, C *dst, int N, int Ns, i
           bfly<RAD, DIR>::run(v);
           const int base = jq * Ns * RAD + k;
 #pragma unroll
-          for (int q = 0; q < RAD; ++q) d[base + q * Ns] = v[q];
+          for (int q = 0; q < RAD; ++q) d[gpad(base + q * Ns)] = v[q];
           t += dt; j += dj; jq += djq; k += dk;
           if (k >= Ns) { k -= Ns; ++jq; }
           if (j >= nb) { j -= nb; jq -= nq; ++t; }
@@ -1067,13 +1093,14 @@ struct tile_walk {
 };
 
 /* One tile of k_gen: load, stages (direction from P.sign), store.  Also the
- * body of the work-queue kernel.  b0/b1: two shared buffers of tb*(nfft+1). */
+ * body of the work-queue kernel.  b0/b1: two shared buffers of
+ * tb * gen_sms(nfft). */
 template <typename C>
 __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A, C *b0, C *b1)
 {
      typedef typename real_of<C>::T R;
      const int N = P.nfft;
-     const int sms = N + 1;
+     const int sms = gen_sms(N);
      const int tb = P.tb;
      const C *__restrict__ tw = (const C *)P.tw;
      const int n = P.n;
@@ -1082,7 +1109,18 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
      const long long vn0 = P.vn[0];
 
      /* ---------------- load ---------------- */
-     if (kind == GB_KIND_C2C || kind == GB_KIND_RADER || (kind == GB_KIND_C2R) || (kind == GB_KIND_R2C && half)) {
+     if (kind == GB_KIND_C2C && !A.l2only) {
+          /* complex elements straight into b0, every copy of the thread in
+           * flight at once (an input written earlier in the same launch,
+           * l2only, takes the register path below: it must not be read
+           * through L1) */
+          tile_walk wk(threadIdx.x, tb, N, P.load_mode, blockDim.x);
+          for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
+               const int t = wk.t(), j = wk.j();
+               if (tile.v0 + t < vn0) cp_async_elem<C>(b0 + t * sms + gpad(j), src_of<C>(P, tile, A, t) + (long long)j * P.is);
+          }
+          cp_async_wait_all_groups();
+     } else if (kind == GB_KIND_C2C || kind == GB_KIND_RADER || (kind == GB_KIND_C2R) || (kind == GB_KIND_R2C && half)) {
           /* complex elements (real pairs for even r2c) into b0, or into b1
            * for the kinds that rearrange them afterwards */
           C *dst = (kind == GB_KIND_C2C || kind == GB_KIND_R2C) ? b0 : b1;
@@ -1107,7 +1145,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                                    const C *sp = src_of<C>(P, tile, A, t) + (long long)j * P.is;
                                    x[u] = A.l2only ? __ldcg(sp) : *sp;
                               }
-                              slot[u] = t * sms + j;
+                              slot[u] = t * sms + gpad(j);
                          }
                     }
                }
@@ -1120,7 +1158,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
                int t, j;
                tile_index(idx, tb, N, P.load_mode, t, j, P.ltb);
-               if (tile.v0 + t < vn0) b0[t * sms + j] = mk<C>(src_of<R>(P, tile, A, t)[j * P.is], 0);
+               if (tile.v0 + t < vn0) b0[t * sms + gpad(j)] = mk<C>(src_of<R>(P, tile, A, t)[j * P.is], 0);
           }
      } else if (kind == GB_KIND_BLUESTEIN) {
           /* b = x conj(w), zero-padded to nfft (dft/bluestein.c:82-95) */
@@ -1130,7 +1168,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                const int t = wk.t(), j = wk.j();
                C x = mk<C>(0, 0);
                if (j < n && tile.v0 + t < vn0) x = cmul(src_of<C>(P, tile, A, t)[j * P.is], cconj(__ldg(w + j)));
-               b0[t * sms + j] = x;
+               b0[t * sms + gpad(j)] = x;
           }
      }
      __syncthreads();
@@ -1140,8 +1178,8 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           idx_walk wk(threadIdx.x, N, blockDim.x);
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
                const int t = wk.q, k = wk.r;
-               b0[t * sms + k] = b1[t * sms + __ldg(P.perm + k)];
-               if (k == 0) b0[t * sms + N] = b1[t * sms];
+               b0[t * sms + gpad(k)] = b1[t * sms + gpad(__ldg(P.perm + k))];
+               if (k == 0) b0[t * sms + gpad(N)] = b1[t * sms];
           }
           __syncthreads();
      } else if (kind == GB_KIND_C2R) {
@@ -1151,21 +1189,21 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                const C *__restrict__ th = (const C *)P.tw_half;
                for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
                     const int t = idx / N, k = idx - t * N;
-                    C a = b1[t * sms + k], b = b1[t * sms + N - k];
+                    C a = b1[t * sms + gpad(k)], b = b1[t * sms + gpad(N - k)];
                     if (k == 0) { a.y = 0; b.y = 0; }
                     b.y = -b.y;
                     C s = cadd(a, b), d = csub(a, b);
                     C w = __ldg(th + k);
                     C cd = mk<C>(w.x * d.x + w.y * d.y, w.x * d.y - w.y * d.x);
-                    b0[t * sms + k] = mk<C>(s.x - cd.y, s.y + cd.x);
+                    b0[t * sms + gpad(k)] = mk<C>(s.x - cd.y, s.y + cd.x);
                }
           } else {
                /* odd n: Hermitian extension of X[0..(n-1)/2] */
                for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
                     const int t = idx / N, k = idx - t * N;
-                    C a = (k < nc) ? b1[t * sms + k] : cconj(b1[t * sms + (N - k)]);
+                    C a = (k < nc) ? b1[t * sms + gpad(k)] : cconj(b1[t * sms + gpad((N - k))]);
                     if (k == 0) a.y = 0;
-                    b0[t * sms + k] = a;
+                    b0[t * sms + gpad(k)] = a;
                }
           }
           __syncthreads();
@@ -1181,9 +1219,9 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           idx_walk wk(threadIdx.x, N, blockDim.x);
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
                const int t = wk.q, k = wk.r;
-               const C bk = res[t * sms + k];
-               if (kind == GB_KIND_RADER && k == 0) b1[t * sms + N] = cadd(b0[t * sms + N], bk);
-               res[t * sms + k] = cmul(bk, __ldg(W + k));
+               const C bk = res[t * sms + gpad(k)];
+               if (kind == GB_KIND_RADER && k == 0) b1[t * sms + gpad(N)] = cadd(b0[t * sms + gpad(N)], bk);
+               res[t * sms + gpad(k)] = cmul(bk, __ldg(W + k));
           }
           __syncthreads();
           res = gen_fft<C, 1>(res, res == b0 ? b1 : b0, P, N, sms, tw);
@@ -1200,7 +1238,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                const int t = wk.t(), k = wk.j();
                const long long v = tile.v0 + t;
                if (v < vn0) {
-                    C y = res[t * sms + k];
+                    C y = res[t * sms + gpad(k)];
                     if (P.post_N) y = cmul(y, post_twiddle<C>(P, (P.post_vdim ? tile.vpost : v) * (long long)k));
                     dst_of<C>(P, tile, A, t)[k * P.os] = y;
                }
@@ -1212,7 +1250,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x, wk.step()) {
                const int t = wk.t(), k = wk.j();
                if (tile.v0 + t < vn0)
-                    dst_of<C>(P, tile, A, t)[k * P.os] = cmul(res[t * sms + k], cconj(__ldg(w + k)));
+                    dst_of<C>(P, tile, A, t)[k * P.os] = cmul(res[t * sms + gpad(k)], cconj(__ldg(w + k)));
           }
      } else if (kind == GB_KIND_RADER) {
           /* X[0] from slot N of buffer 1; X[g^-k] = x[0] + conv[k] */
@@ -1221,7 +1259,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           for (int idx = threadIdx.x; idx < tb * n; idx += blockDim.x, wk.step()) {
                const int t = wk.t(), j = wk.j();
                if (tile.v0 + t < vn0) {
-                    const C y = (j == 0) ? b1[t * sms + N] : cadd(b0[t * sms + N], res[t * sms + __ldg(lg + j - 1)]);
+                    const C y = (j == 0) ? b1[t * sms + gpad(N)] : cadd(b0[t * sms + gpad(N)], res[t * sms + gpad(__ldg(lg + j - 1))]);
                     dst_of<C>(P, tile, A, t)[j * P.os] = y;
                }
           }
@@ -1234,12 +1272,12 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                const C *__restrict__ th = (const C *)P.tw_half;
                for (int idx = threadIdx.x; idx < tb * nc; idx += blockDim.x) {
                     const int t = idx / nc, k = idx - t * nc;
-                    C a = res[t * sms + (k % N)], b = res[t * sms + ((N - k) % N)];
+                    C a = res[t * sms + gpad((k % N))], b = res[t * sms + gpad(((N - k) % N))];
                     b.y = -b.y;
                     C ev = cscale(cadd(a, b), (R)0.5);
                     C dd = csub(a, b);
                     C od = mk<C>(dd.y * (R)0.5, -dd.x * (R)0.5);
-                    dst[t * sms + k] = cadd(ev, cmul(__ldg(th + k), od));
+                    dst[t * sms + gpad(k)] = cadd(ev, cmul(__ldg(th + k), od));
                }
                __syncthreads();
                src = dst;
@@ -1247,7 +1285,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
           for (int idx = threadIdx.x; idx < tb * nc; idx += blockDim.x) {
                int t, k;
                tile_index(idx, tb, nc, P.store_mode, t, k, P.ltb);
-               if (tile.v0 + t < vn0) dst_of<C>(P, tile, A, t)[k * P.os] = src[t * sms + k];
+               if (tile.v0 + t < vn0) dst_of<C>(P, tile, A, t)[k * P.os] = src[t * sms + gpad(k)];
           }
      } else if (kind == GB_KIND_C2R) {
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x) {
@@ -1255,7 +1293,7 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
                tile_index(idx, tb, N, P.store_mode, t, j, P.ltb);
                if (tile.v0 + t < vn0) {
                     R *r = dst_of<R>(P, tile, A, t);
-                    const C y = res[t * sms + j];
+                    const C y = res[t * sms + gpad(j)];
                     if (!half) r[j * P.os] = y.x;
                     else if (P.real_pairs) ((C *)r)[j] = y;
                     else { r[2 * j * P.os] = y.x; r[(2 * j + 1) * P.os] = y.y; }
@@ -1270,7 +1308,7 @@ __global__ void __launch_bounds__(512) k_gen(const gb_pass P, const void *__rest
 {
      extern __shared__ __align__(16) unsigned char gb_smem[];
      C *b0 = (C *)gb_smem;
-     C *b1 = b0 + P.tb * (P.nfft + 1);
+     C *b1 = b0 + P.tb * gen_sms(P.nfft);
      gen_addr A;
      A.in = in; A.out = out; A.pin = 0; A.pout = 0; A.l2only = 0;
      for (long long blk = blockIdx.x; blk < P.nblocks; blk += gridDim.x) {

@@ -21,9 +21,9 @@ extern "C" const void *gb_reg_kernel_f(int logn, int kind, int dir);
 extern "C" const void *gb_reg_kernel_d(int logn, int kind, int dir);
 extern "C" const void *gb_tma_kernel_f(int logn, int kind, int dir, int groups);
 extern "C" const void *gb_tma_kernel_d(int logn, int kind, int dir, int groups);
-extern "C" const void *gb_tc_kernel(int nfft, int dir);
+extern "C" const void *gb_tc_kernel(int nfft, int dir, int ctas);
 extern "C" const void *gb_cols_tma_kernel(int logn, int dir, int groups);
-extern "C" int gb_tc_smem(int nfft);
+extern "C" int gb_tc_smem(int nfft, int ctas);
 
 namespace gb {
 
@@ -370,7 +370,8 @@ static const void *pick_kernel(const gb_pass *p)
           return p->prec == 4 ? (const void *)k_pointwise<float2> : (const void *)k_pointwise<double2>;
      if (p->kind == GB_KIND_COPY)
           return p->prec == 4 ? (const void *)k_copy<float2> : (const void *)k_copy<double2>;
-     if (p->variant == GB_VAR_TC) return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_tc_kernel(p->nfft, p->sign) : 0;
+     if (p->variant == GB_VAR_TC)
+          return (p->kind == GB_KIND_C2C && p->prec == 4) ? gb_tc_kernel(p->nfft, p->sign, p->groups) : 0;
      if (p->variant == GB_VAR_TMA_COLS) {
           int logn = 0;
           while ((1 << logn) < p->nfft) ++logn;
@@ -413,11 +414,12 @@ static unsigned grid_of(const gb_pass *p, const void *fn)
                cudaGetLastError();
                per = 1;
           }
-          /* the calculator may report one CTA per SM for the tensor-core
-           * kernel, whose registers, shared memory and TMEM (64 columns) leave
-           * room for two; its CTAs never wait on one another, so a second wave
-           * is harmless if they cannot all be resident */
-          if (p->variant == GB_VAR_TC && per < 2) per = 2;
+          /* the calculator may report fewer CTAs per SM for the tensor-core
+           * kernel than its registers, shared memory and TMEM (64 columns)
+           * leave room for (its build's 2 or 3); its CTAs never wait on one
+           * another, so a second wave is harmless if they cannot all be
+           * resident */
+          if (p->variant == GB_VAR_TC && per < p->groups) per = p->groups;
           if (per < 1) per = 1;
           if (g > (long long)per * sms) g = (long long)per * sms;
      }
@@ -614,8 +616,9 @@ extern "C" int gb_launch_pass(const gb_pass *p, const void *in, void *out, void 
                      "strides, a 16-byte aligned input and two shared slots";
           else if (p->variant == GB_VAR_TC && (p->prec != 4 || p->nfft < 256 || p->nfft > 4096 || (p->nfft & (p->nfft - 1)) ||
                                                p->threads != 256 || p->tb != 256 / (p->nfft / 16) ||
-                                               p->smem < gb_tc_smem(p->nfft) || (p->store_mode == GB_MOVE_DIRECT && p->os != 1)))
-               bad = "tensor-core pass needs f32 c2c of 256 to 4096 points (a power of two), 256 threads";
+                                               (p->groups != 2 && p->groups != 3) ||
+                                               p->smem < gb_tc_smem(p->nfft, p->groups) || (p->store_mode == GB_MOVE_DIRECT && p->os != 1)))
+               bad = "tensor-core pass needs f32 c2c of 256 to 4096 points (a power of two), 256 threads, a 2- or 3-CTA build";
           if (bad) {
                snprintf(gb_errbuf, sizeof gb_errbuf, "refused pass (kind %d nfft %d): %s", p->kind, p->nfft, bad);
                return -1;

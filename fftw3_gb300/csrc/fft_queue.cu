@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_queue(const
           if (go) {
                __threadfence();
                C *b0 = (C *)gb_smem;
-               C *b1 = b0 + it.P.tb * (it.P.nfft + 1);
+               C *b1 = b0 + it.P.tb * gen_sms(it.P.nfft);
                tile_t tile;
                tile.bi = it.bi; tile.bo = it.bo; tile.v0 = it.v0; tile.vpost = 0;
                gen_addr A;

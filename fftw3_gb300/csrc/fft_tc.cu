@@ -4,9 +4,11 @@
  * adjacent columns, or the two passes of a 65536 = 256 x 256 four-step with
  * its W_N^(n2 k1) twiddle).  N = 512, 1024, 2048 begin with one FP32 stage
  * of radix 2, 4 or 8, as the register kernels do; every radix-16 stage is a
- * GEMM.  Row tiles of aligned transforms are copied in by the TMA engine
- * (cp.async.bulk) while the previous tile is transformed; two CTAs share an
- * SM.
+ * GEMM.  Two builds: CTAS = 2, two CTAs per SM, row tiles of aligned
+ * transforms copied in by the TMA engine (cp.async.bulk) while the previous
+ * tile is transformed; CTAS = 3, three CTAs per SM (80 registers a thread,
+ * no copy-in buffer), tiles gathered with plain loads while the SM's other
+ * CTAs compute.
  *
  * Per stage, each of the CTA's 256 threads owns one radix-16 butterfly: it
  * gathers its 16 inputs from the shared-memory copy of the transform(s),
@@ -106,8 +108,8 @@ __device__ __forceinline__ void tc_prefetch(const gb_pass &P, const void *in, lo
           bulk_g2s(pre + t * N, (const float2 *)in + tl.bi + (tl.v0 + t) * P.vis[0], (unsigned)(N * 8), bar);
 }
 
-template <int LOGN, int DIR>
-__global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
+template <int LOGN, int DIR, int CTAS>
+__global__ void __launch_bounds__(256, CTAS) k_tc_fft(const gb_pass P, const void *__restrict__ in, void *__restrict__ out)
 {
      constexpr int N = 1 << LOGN;
      constexpr int T = N / 16;           /* butterflies per transform per stage */
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
      unsigned char *As = sm;                           /* 2 groups x 24 KB */
      unsigned char *Bs = sm + 2 * TC_A_BYTES;          /* 6 KB */
      /* the next row tile, copied in by the TMA engine while this one is
-      * transformed (32 KB) */
+      * transformed (32 KB; two-CTA build only) */
      float2 *pre = (float2 *)(sm + 2 * TC_A_BYTES + TC_B_BYTES);
      /* the tile (TB x N complex, 32 KB) shares the A operand's 48 KB: a
       * stage reads it into registers before A is written, and the MMA has
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_fft(const gb_pass P, const void *
      const int g = m >> 7;               /* 128-row MMA group */
 
      /* row tiles of 16-byte aligned transforms arrive by bulk copy */
-     bool pref = P.load_mode == GB_MOVE_ROWS && P.is == 1 && ((unsigned long long)in & 15) == 0;
+     bool pref = CTAS == 2 && P.load_mode == GB_MOVE_ROWS && P.is == 1 && ((unsigned long long)in & 15) == 0;
      for (int d = 0; d < P.nv; ++d) pref = pref && (P.vis[d] & 1) == 0;
 
      /* B: real form of the 16-point DFT matrix for this direction, split
@@ -373,22 +375,29 @@ using namespace gb;
 extern "C" int *gb_device_status_ptr(void);
 
 /* bytes of dynamic shared memory the tensor-core FFT needs: A (shared with
- * the tile), B, and the buffer the next row tile is copied into */
-extern "C" int gb_tc_smem(int nfft)
+ * the tile), B, and (two-CTA build) the buffer the next row tile is copied
+ * into */
+extern "C" int gb_tc_smem(int nfft, int ctas)
 {
-     return (int)(2 * TC_A_BYTES + TC_B_BYTES) + 256 * 16 * 8 + 0 * nfft;
+     return (int)(2 * TC_A_BYTES + TC_B_BYTES) + (ctas == 2 ? 256 * 16 * 8 : 0) + 0 * nfft;
 }
 
-extern "C" const void *gb_tc_kernel(int nfft, int dir)
+template <int CTAS> static const void *tc_kernel(int nfft, int dir)
 {
      switch (nfft) {
-     case 256: return dir < 0 ? (const void *)k_tc_fft<8, -1> : (const void *)k_tc_fft<8, 1>;
-     case 512: return dir < 0 ? (const void *)k_tc_fft<9, -1> : (const void *)k_tc_fft<9, 1>;
-     case 1024: return dir < 0 ? (const void *)k_tc_fft<10, -1> : (const void *)k_tc_fft<10, 1>;
-     case 2048: return dir < 0 ? (const void *)k_tc_fft<11, -1> : (const void *)k_tc_fft<11, 1>;
-     case 4096: return dir < 0 ? (const void *)k_tc_fft<12, -1> : (const void *)k_tc_fft<12, 1>;
+     case 256: return dir < 0 ? (const void *)k_tc_fft<8, -1, CTAS> : (const void *)k_tc_fft<8, 1, CTAS>;
+     case 512: return dir < 0 ? (const void *)k_tc_fft<9, -1, CTAS> : (const void *)k_tc_fft<9, 1, CTAS>;
+     case 1024: return dir < 0 ? (const void *)k_tc_fft<10, -1, CTAS> : (const void *)k_tc_fft<10, 1, CTAS>;
+     case 2048: return dir < 0 ? (const void *)k_tc_fft<11, -1, CTAS> : (const void *)k_tc_fft<11, 1, CTAS>;
+     case 4096: return dir < 0 ? (const void *)k_tc_fft<12, -1, CTAS> : (const void *)k_tc_fft<12, 1, CTAS>;
      default: return 0;
      }
+}
+
+/* the build for ctas CTAs per SM (2 or 3) */
+extern "C" const void *gb_tc_kernel(int nfft, int dir, int ctas)
+{
+     return ctas == 3 ? tc_kernel<3>(nfft, dir) : ctas == 2 ? tc_kernel<2>(nfft, dir) : 0;
 }
 
 /* One-CTA GEMM through the tcgen05 path (device pointers): D = A . B^T,

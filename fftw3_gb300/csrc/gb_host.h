@@ -198,7 +198,7 @@ int gb_rader_omega(void *dst, const int *gpow, int prec, long long p, int sign, 
 const int *gb_table_rader_perm(long long p);
 const void *gb_table_rader_spec(int prec, long long p, int sign);
 int gb_pass_kernel_attrs(const gb_pass *p, int *regs, int *max_threads);
-int gb_tc_smem(int nfft);
+int gb_tc_smem(int nfft, int ctas);
 int gb_tc_selftest(const void *A, const void *B, float *D, int ks);
 
 #endif

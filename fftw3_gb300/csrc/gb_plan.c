@@ -552,7 +552,7 @@ static int config_pass(gb_pass *P, int prec, int kind, long long n, int sign, lo
           if (k < 0) return -1;
           P->nrad = k;
           P->variant = GB_VAR_GEN;
-          sm1 = 2 * (L + 1) * csize(prec);
+          sm1 = 2LL * gb_gen_sms((int)L) * csize(prec);
           if (sm1 > smax) return 1;
           tb = (int)(1024 / nfft); if (tb < 1) tb = 1;
           if (llabs_(is) != 1 || llabs_(os) != 1) { int want = prec == 4 ? 16 : 8; if (tb < want) tb = want; }
@@ -672,18 +672,29 @@ static void count_ops(gb_plan *p, const gb_pass *P, long long howmany)
 #define GB_TC_MAX_STAGES 4
 static void use_tensor_cores(gb_plan *p, gb_pass *P)
 {
-     int i, stages;
+     int i, stages, lm, ctas;
      if (P->kind != GB_KIND_C2C || P->prec != 4 || P->nfft < 256 || P->nfft > 4096 || (P->nfft & (P->nfft - 1)))
           return;
      stages = P->nfft == 4096 ? 3 : 2;
      if (p->tc_stages + stages > GB_TC_MAX_STAGES) return;
      p->tc_stages += stages;
-     if (gb_tc_smem(P->nfft) > smem_max()) return;
+     lm = (P->is == 1 || llabs_(P->vis[0]) != 1) ? GB_MOVE_ROWS : GB_MOVE_COLS;
+     /* CTAs per SM of the build: 2 for unit-stride rows (their next tile is
+      * bulk-copied into a second buffer), 3 for the rest (plain loads, no
+      * second buffer; measured: c2c 65536 four-step 4.49 -> 3.54 ms, rows of
+      * 4096 1.89 with two against 2.05 ms with three); FFTW_GB300_TC_CTAS=2|3
+      * sets it */
+     {
+          const char *e = getenv("FFTW_GB300_TC_CTAS");
+          ctas = (e && (atoi(e) == 2 || atoi(e) == 3)) ? atoi(e) : (lm == GB_MOVE_ROWS && P->is == 1) ? 2 : 3;
+     }
+     if (gb_tc_smem(P->nfft, ctas) > smem_max()) return;
+     P->load_mode = lm;
+     P->groups = ctas;
      P->variant = GB_VAR_TC;
      P->tb = 256 / (P->nfft / 16);
      P->threads = 256;
-     P->smem = gb_tc_smem(P->nfft);
-     P->load_mode = (P->is == 1 || llabs_(P->vis[0]) != 1) ? GB_MOVE_ROWS : GB_MOVE_COLS;
+     P->smem = gb_tc_smem(P->nfft, P->groups);
      P->store_mode = (P->os == 1) ? GB_MOVE_DIRECT : (llabs_(P->vos[0]) == 1) ? GB_MOVE_COLS : GB_MOVE_ROWS;
      P->ntiles0 = (P->vn[0] + P->tb - 1) / P->tb;
      P->nblocks = P->ntiles0;
@@ -1162,7 +1173,9 @@ static void describe(gb_plan *p)
                           P->n, P->nfft, P->variant == GB_VAR_REG ? "reg" : P->variant == GB_VAR_TMA ? "reg-tma" :
                           P->variant == GB_VAR_TMA_COLS ? "cols-tma" :
                           P->variant == GB_VAR_TC ? "tc-split-fp16" : "gen",
-                          (P->variant == GB_VAR_TMA || P->variant == GB_VAR_TMA_COLS) && P->groups == 2 ? " groups=2" : "",
+                          (P->variant == GB_VAR_TMA || P->variant == GB_VAR_TMA_COLS) && P->groups == 2 ? " groups=2"
+                          : P->variant == GB_VAR_TC && P->groups == 3                                     ? " ctas=3"
+                                                                                                          : "",
                           P->tb,
                           P->threads, P->smem, mv[P->load_mode], mv[P->store_mode], P->is, P->os,
                           P->vn[0], P->post_N ? " +twiddle" : "");

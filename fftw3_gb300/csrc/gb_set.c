@@ -96,7 +96,7 @@ static int item_pass(gb_pass *P, int prec, int kind, long long n, int sign, long
      P->variant = GB_VAR_GEN;
      P->tb = tb;
      P->threads = threads;
-     P->smem = 2 * tb * (P->nfft + 1) * 2 * prec;
+     P->smem = 2 * tb * gb_gen_sms(P->nfft) * 2 * prec;
      P->load_mode = cols_in ? GB_MOVE_COLS : GB_MOVE_ROWS;
      P->store_mode = cols_out ? GB_MOVE_COLS : GB_MOVE_ROWS;
      P->is = is; P->os = os;
@@ -229,10 +229,13 @@ static int prime_kind(int prec, long long n, int cap_s, int cap_l, int want, int
      return -1;
 }
 
-/* small-tile queue: 2 x (4096+1) complex64 (2048 complex128) = 65.5 KB,
- * three 256-thread CTAs per SM; large-tile queue: twice that, one 512-thread
- * CTA per SM, only for what the small tiles cannot hold */
+/* small-tile queue: transforms up to 4096 complex64 (2048 complex128) points,
+ * two buffers of 16 (8) x 273 elements (a 256-point transform in the padded
+ * layout, gb_gen_sms) = 69.9 KB, three 256-thread CTAs per SM; large-tile
+ * queue: twice that, one 512-thread CTA per SM, only for what the small tiles
+ * cannot hold */
 static int cap_small(int prec) { return prec == 4 ? 4096 : 2048; }
+static int qbuf(int prec) { return (prec == 4 ? 16 : 8) * gb_gen_sms(256); }
 
 /* Splits n = d * (n / d) of a long length with both factors within a tile
  * and 13-smooth, d ascending (at most maxd of them). */
@@ -345,9 +348,9 @@ static gb_set *build_set(int prec, xform *xs, int nx)
           if (kind >= 0) {
                /* group transforms with the same key */
                gb_pass tmp;
-               int cq = large ? cap_l : cap_s, thr = large ? 512 : 256;
+               int qb = large ? 2 * qbuf(prec) : qbuf(prec), thr = large ? 512 : 256;
                long long nfft = kind == GB_KIND_BLUESTEIN ? pow2_at_least(2 * n - 1) : kind == GB_KIND_RADER ? n - 1 : n;
-               int tbmax = (int)((2LL * (cq + 1) * cs) / (2LL * (nfft + 1) * cs));
+               int tbmax = qb / gb_gen_sms((int)nfft);
                if (tbmax > GB_Q_GROUP) tbmax = GB_Q_GROUP;
                if (cf.tbmax > 0 && cf.tbmax < tbmax) tbmax = cf.tbmax;
                if (tbmax < 1) tbmax = 1;
@@ -383,7 +386,7 @@ static gb_set *build_set(int prec, xform *xs, int nx)
                n2 = n / n1;
                /* columns per tile: the tuner's (a power of two) or 16 (8 double) */
                if (cf.tbmax > 0 && cf.tbmax < tbc && (cf.tbmax & (cf.tbmax - 1)) == 0) tbc = cf.tbmax;
-               while (tbc > 1 && 2LL * tbc * ((n1 > n2 ? n1 : n2) + 1) * cs > 2LL * (cap + 1) * cs) tbc >>= 1;
+               while (tbc > 1 && (long long)tbc * gb_gen_sms((int)(n1 > n2 ? n1 : n2)) > qbuf(prec)) tbc >>= 1;
                /* pass A: columns n2 (stride is), n1-point transforms with
                 * element stride n2*is into scratch [n2][k1] */
                if (item_pass(&pa, prec, GB_KIND_C2C, n1, x->sign, n2 * x->is, 1, n2, x->is, n1, tbc, 1, 0, 256, cf.body,
@@ -644,25 +647,14 @@ static double set_now_s(void)
      return ts.tv_sec + 1e-9 * ts.tv_nsec;
 }
 
-/* ms per execute (best of reps) of a set of cnt transforms of length n on
- * the scratch arrays, under the configuration wisdom now holds for n; 1e30
- * when it does not build or run */
-static double time_candidate(int prec, long long n, int sign, int cnt, char *din, char *dout, cudaStream_t st,
-                             int reps)
+/* ms per execute (best of reps) of the set of transforms xs (on scratch
+ * arrays) under the configurations wisdom now holds; 1e30 when it does not
+ * build or run */
+static double time_xforms(int prec, xform *xs, int cnt, cudaStream_t st, int reps)
 {
-     const int cs = 2 * prec;
-     xform *xs = (xform *)malloc(sizeof(xform) * (size_t)cnt);
-     gb_set *S;
+     gb_set *S = build_set(prec, xs, cnt);
      double best = 1e30;
      int i;
-     if (!xs) return best;
-     for (i = 0; i < cnt; ++i) {
-          xs[i].n = n; xs[i].sign = sign; xs[i].is = 1; xs[i].os = 1;
-          xs[i].in = din + (size_t)i * (size_t)n * cs;
-          xs[i].out = dout + (size_t)i * (size_t)n * cs;
-     }
-     S = build_set(prec, xs, cnt);
-     free(xs);
      if (!S) return best;
      gb_set_stream_of_set(S, st, 1);
      if (!gb_execute_set(S)) {
@@ -686,6 +678,123 @@ static double time_candidate(int prec, long long n, int sign, int cnt, char *din
      return best;
 }
 
+/* a set of cnt transforms of length n alone, packed on the scratch arrays */
+static double time_candidate(int prec, long long n, int sign, int cnt, char *din, char *dout, cudaStream_t st,
+                             int reps)
+{
+     const int cs = 2 * prec;
+     xform *xs = (xform *)malloc(sizeof(xform) * (size_t)cnt);
+     double t;
+     int i;
+     if (!xs) return 1e30;
+     for (i = 0; i < cnt; ++i) {
+          xs[i].n = n; xs[i].sign = sign; xs[i].is = 1; xs[i].os = 1;
+          xs[i].in = din + (size_t)i * (size_t)n * cs;
+          xs[i].out = dout + (size_t)i * (size_t)n * cs;
+     }
+     t = time_xforms(prec, xs, cnt, st, reps);
+     free(xs);
+     return t;
+}
+
+/* Kinds of per-length choice, each of which the whole-set check keeps or
+ * takes back as one. */
+enum { CH_BODY, CH_PRIME, CH_SPLIT, CH_ORDER, CH_TILE, CH_KINDS };
+
+static int entry_has(const gb_wisdom_entry *e, int kind)
+{
+     switch (kind) {
+     case CH_BODY: return e->variant == GB_VAR_REG;
+     case CH_PRIME: return e->variant == GB_KIND_RADER || e->variant == GB_KIND_BLUESTEIN;
+     case CH_SPLIT: return e->n1 != 0;
+     case CH_ORDER: return e->order != 0;
+     default: return e->tb != 0;
+     }
+}
+
+static void entry_reset(gb_wisdom_entry *e, int kind)
+{
+     switch (kind) {
+     case CH_BODY:
+     case CH_PRIME: e->variant = -1; break;
+     case CH_SPLIT: e->n1 = 0; break;
+     case CH_ORDER: e->order = 0; break;
+     default: e->tb = 0; break;
+     }
+}
+
+/* The per-length choices were timed on sets of one length; in the whole
+ * set every item runs from one kernel, whose code for all item bodies
+ * competes for the instruction cache, and items of all lengths share the
+ * SMs.  So each kind of choice (register bodies, prime algorithms, splits,
+ * radix orders, tiles) is timed once more on a scratch copy of the whole
+ * set against the same set without it, and kept only when the whole set
+ * runs faster with it (by more than 1%). */
+typedef struct { long long n, pts; int sign; } lclass;
+
+static void whole_set_check(int prec, const xform *xs, int nx, const lclass *cl, int ncl, cudaStream_t st, int reps)
+{
+     const int cs = 2 * prec;
+     long long tot = 0, off = 0;
+     char *din = 0, *dout = 0;
+     xform *xw = 0;
+     gb_wisdom_entry *ent = 0;
+     int *has = 0, i, k, kind;
+     double best;
+     for (i = 0; i < nx; ++i) tot += xs[i].n;
+     xw = (xform *)malloc(sizeof(xform) * (size_t)nx);
+     ent = (gb_wisdom_entry *)malloc(sizeof(gb_wisdom_entry) * (size_t)ncl);
+     has = (int *)malloc(sizeof(int) * (size_t)ncl);
+     if (!xw || !ent || !has || cudaMalloc((void **)&din, (size_t)tot * cs) != cudaSuccess ||
+         cudaMalloc((void **)&dout, (size_t)tot * cs) != cudaSuccess) {
+          cudaGetLastError();
+          goto done;
+     }
+     cudaMemset(din, 0, (size_t)tot * cs);
+     for (i = 0; i < nx; ++i) {
+          xw[i] = xs[i];
+          xw[i].is = xw[i].os = 1;
+          xw[i].in = din + (size_t)off * cs;
+          xw[i].out = dout + (size_t)off * cs;
+          off += xs[i].n;
+     }
+     /* each length's entry */
+     for (k = 0; k < ncl; ++k) {
+          char key[64];
+          const gb_wisdom_entry *w;
+          set_key(key, sizeof key, prec, cl[k].n);
+          w = gb_wisdom_lookup(key);
+          has[k] = w != 0;
+          if (w) ent[k] = *w;
+     }
+     best = time_xforms(prec, xw, nx, st, reps);
+     for (kind = 0; kind < CH_KINDS; ++kind) {
+          int any = 0;
+          double t;
+          for (k = 0; k < ncl; ++k)
+               if (has[k] && entry_has(&ent[k], kind)) {
+                    gb_wisdom_entry e = ent[k];
+                    entry_reset(&e, kind);
+                    gb_wisdom_store(&e);
+                    any = 1;
+               }
+          if (!any) continue;
+          t = time_xforms(prec, xw, nx, st, reps);
+          for (k = 0; k < ncl; ++k)
+               if (has[k] && entry_has(&ent[k], kind)) {
+                    if (t * 1.01 < best) entry_reset(&ent[k], kind);   /* the set is faster without them */
+                    gb_wisdom_store(&ent[k]);
+               }
+          if (t * 1.01 < best) best = t;
+     }
+done:
+     if (din) cudaFree(din);
+     if (dout) cudaFree(dout);
+     free(xw);
+     free(ent);
+     free(has);
+}
+
 /* a radix order whose stage list differs from the default's */
 static int order_differs(long long n, int order)
 {
@@ -696,8 +805,6 @@ static int order_differs(long long n, int order)
           if (r0[i] != r1[i]) return 1;
      return 0;
 }
-
-typedef struct { long long n, pts; int sign; } lclass;
 
 static int cmp_class_pts(const void *a, const void *b)
 {
@@ -715,7 +822,7 @@ static void tune_set(int prec, const xform *xs, int nx, unsigned flags)
      double t0 = set_now_s(), limit = gb_get_timelimit();
      xform *srt;
      lclass *cl;
-     int ncl = 0, i, k;
+     int ncl = 0, i, k, ntuned = 0;
      long long maxn = 0;
      char *din = 0, *dout = 0;
      cudaStream_t st = 0;
@@ -799,7 +906,9 @@ static void tune_set(int prec, const xform *xs, int nx, unsigned flags)
           }
           strcpy(best_e.key, key);
           gb_wisdom_store(&best_e);
+          ++ntuned;
      }
+     if (ntuned && st) whole_set_check(prec, xs, nx, cl, ncl, st, reps);
 done:
      if (st) cudaStreamDestroy(st);
      if (din) cudaFree(din);

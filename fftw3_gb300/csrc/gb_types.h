@@ -160,6 +160,9 @@ static inline int gb_pad_mult(int nfft)
      return (r == 16 && nfft >= 256) ? 2 : 1;
 }
 static inline int gb_reg_sms(int nfft) { return (nfft + gb_pad_mult(nfft) * (nfft >> 4) + 3) & ~1; }
+/* runtime-radix body layout: element i at i + i/16, transforms nfft + nfft/16 + 1
+ * complex elements apart (two buffers of tb transforms) */
+static inline int gb_gen_sms(int nfft) { return nfft + (nfft >> 4) + 1; }
 /* first-stage radix of a power-of-two length in the register kernels */
 static inline int gb_reg_r0(int nfft)
 {

@@ -41,10 +41,25 @@ def test_tc_gemm_selftest(lib, torch_tc, ks):
     assert lib_.fftw_gb300_device_status() == 0
 
 
+@pytest.fixture(params=["2", "3"])
+def tc_ctas(request, monkeypatch):
+    """The two builds of the tensor-core kernel: two CTAs per SM with bulk
+    copies into a second buffer, three CTAs per SM with plain loads (read
+    when planning)."""
+    monkeypatch.setenv("FFTW_GB300_TC_CTAS", request.param)
+    return request.param
+
+
+def _tc_plan_ok(p, ctas):
+    d = p.describe()
+    assert "tc-split-fp16" in d
+    assert ("ctas=3" in d) == (ctas == "3")
+
+
 @pytest.mark.parametrize("n", [256, 512, 1024, 2048, 4096, 65536])
 @pytest.mark.parametrize("dist", ["normal", "loguniform"])
 @pytest.mark.parametrize("sign", [-1, 1])
-def test_tc_fft_parity(lib, torch_tc, restatement, n, dist, sign):
+def test_tc_fft_parity(lib, torch_tc, restatement, tc_ctas, n, dist, sign):
     """1D batches; 512, 1024 and 2048 begin with an FP32 stage of radix 2,
     4 or 8; 65536 runs as two tensor-core passes of 256 (four-step)."""
     import fftw3_gb300 as g
@@ -60,7 +75,7 @@ def test_tc_fft_parity(lib, torch_tc, restatement, n, dist, sign):
     xi = torch.from_numpy(x).cuda()
     yo = torch.empty_like(xi)
     p = g.plan_many_dft([n], hm, xi.data_ptr(), yo.data_ptr(), sign, g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE, "f")
-    assert "tc-split-fp16" in p.describe()
+    _tc_plan_ok(p, tc_ctas)
     p.execute()
     y = yo.cpu().numpy()
     ref = restatement.c2c(x.astype(np.complex128), [n], sign, "d", nthreads=4)
@@ -69,7 +84,7 @@ def test_tc_fft_parity(lib, torch_tc, restatement, n, dist, sign):
     assert g.load().fftw_gb300_device_status() == 0
 
 
-def test_tc_2d_512(lib, torch_tc, restatement):
+def test_tc_2d_512(lib, torch_tc, restatement, tc_ctas):
     """2D 512 x 512 (the 3D workload's axis length): rows and columns in the
     tensor-core form, each beginning with a radix-2 FP32 stage."""
     import fftw3_gb300 as g
@@ -88,7 +103,7 @@ def test_tc_2d_512(lib, torch_tc, restatement):
     assert g.load().fftw_gb300_device_status() == 0
 
 
-def test_tc_multid_columns(lib, torch_tc, restatement):
+def test_tc_multid_columns(lib, torch_tc, restatement, tc_ctas):
     """2D 256 x 256: the column axis runs through the tensor-core kernel with
     column tiles (strided loads and stores)."""
     import fftw3_gb300 as g
@@ -106,7 +121,7 @@ def test_tc_multid_columns(lib, torch_tc, restatement):
 
 
 @pytest.mark.parametrize("n", [256, 4096, 65536])
-def test_tc_fft_loguniform_large_batch(lib, torch_tc, restatement, n):
+def test_tc_fft_loguniform_large_batch(lib, torch_tc, restatement, tc_ctas, n):
     """The precision-form workload's log-uniform variant (re and im with
     magnitudes 10^U[-3,3) and random signs, generated on the device) at 2^26
     points per length: transforms spread over the whole batch against the
@@ -125,7 +140,7 @@ def test_tc_fft_loguniform_large_batch(lib, torch_tc, restatement, n):
     x = torch.complex(mag(), mag())
     y = torch.empty_like(x)
     p = g.plan_many_dft([n], hm, x.data_ptr(), y.data_ptr(), -1, g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE, "f")
-    assert "tc-split-fp16" in p.describe()
+    _tc_plan_ok(p, tc_ctas)
     p.execute()
     torch.cuda.synchronize()
     sel = np.linspace(0, hm - 1, 16).astype(int)
