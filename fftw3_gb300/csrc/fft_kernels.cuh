@@ -968,7 +968,7 @@ __host__ __device__ constexpr int gen_sms(int nfft) { return nfft + (nfft >> 4) 
 
 template <typename C, int DIR, int RAD>
 __device__ __forceinline__ void gen_stage(const C *src, C *dst, int N, int Ns, int tb, int sms,
-                                          const C *__restrict__ tw)
+                                          const C *__restrict__ tw, const C *__restrict__ tws)
 {
      const int nb = N / RAD;
      const int twstep = N / (Ns * RAD);
@@ -987,8 +987,15 @@ __device__ __forceinline__ void gen_stage(const C *src, C *dst, int N, int Ns, i
 #pragma unroll
           for (int r = 0; r < RAD; ++r) v[r] = s[gpad(j + r * nb)];
           if (Ns > 1) {
+               if (tws) {
+                    /* the stage's rows: consecutive k on consecutive lanes */
+                    const C *w = tws + (Ns - 1) + k;
 #pragma unroll
-               for (int r = 1; r < RAD; ++r) v[r] = cmul(v[r], twid<DIR>(tw, r * k * twstep));
+                    for (int r = 1; r < RAD; ++r) v[r] = cmul(v[r], twid<DIR>(w, (r - 1) * Ns));
+               } else {
+#pragma unroll
+                    for (int r = 1; r < RAD; ++r) v[r] = cmul(v[r], twid<DIR>(tw, r * k * twstep));
+               }
           }
           bfly<RAD, DIR>::run(v);
           const int base = jq * Ns * RAD + k;
@@ -1006,18 +1013,19 @@ __device__ C *gen_fft(C *b0, C *b1, const gb_pass &P, int N, int sms, const C *_
 {
      int Ns = 1;
      C *src = b0, *dst = b1;
+     const C *__restrict__ tws = (const C *)P.tw_gen;
      for (int s = 0; s < P.nrad; ++s) {
           const int r = P.rad[s];
           switch (r) {
-          case 2: gen_stage<C, DIR, 2>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 3: gen_stage<C, DIR, 3>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 4: gen_stage<C, DIR, 4>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 5: gen_stage<C, DIR, 5>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 7: gen_stage<C, DIR, 7>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 8: gen_stage<C, DIR, 8>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 11: gen_stage<C, DIR, 11>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 13: gen_stage<C, DIR, 13>(src, dst, N, Ns, P.tb, sms, tw); break;
-          case 16: gen_stage<C, DIR, 16>(src, dst, N, Ns, P.tb, sms, tw); break;
+          case 2: gen_stage<C, DIR, 2>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 3: gen_stage<C, DIR, 3>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 4: gen_stage<C, DIR, 4>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 5: gen_stage<C, DIR, 5>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 7: gen_stage<C, DIR, 7>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 8: gen_stage<C, DIR, 8>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 11: gen_stage<C, DIR, 11>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 13: gen_stage<C, DIR, 13>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
+          case 16: gen_stage<C, DIR, 16>(src, dst, N, Ns, P.tb, sms, tw, tws); break;
           default: break;
           }
           __syncthreads();
@@ -1108,8 +1116,48 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
      const bool half = (kind == GB_KIND_R2C || kind == GB_KIND_C2R) && (n % 2 == 0);
      const long long vn0 = P.vn[0];
 
+     /* Pointer-stride walks of a c2c tile: a column tile whose tb (a power of
+      * two) divides the block keeps one column t = threadIdx mod tb per thread
+      * and walks its rows j0, j0 + J, ... (J = block / tb); a row tile of
+      * transforms at least a block long goes transform after transform with
+      * the block on consecutive elements.  No index arithmetic per element
+      * but the pad; other shapes walk the general way below. */
+     const bool ld_fast = kind == GB_KIND_C2C &&
+                          ((P.load_mode == GB_MOVE_COLS && P.ltb >= 0 && (blockDim.x & (tb - 1)) == 0) ||
+                           (P.load_mode != GB_MOVE_COLS && N >= (int)blockDim.x));
+     const bool st_fast = kind == GB_KIND_C2C &&
+                          ((P.store_mode == GB_MOVE_COLS && P.ltb >= 0 && (blockDim.x & (tb - 1)) == 0) ||
+                           (P.store_mode != GB_MOVE_COLS && N >= (int)blockDim.x));
+
      /* ---------------- load ---------------- */
-     if (kind == GB_KIND_C2C && !A.l2only) {
+     if (ld_fast) {
+          const bool cols = P.load_mode == GB_MOVE_COLS;
+          const int J = cols ? (int)(blockDim.x >> P.ltb) : (int)blockDim.x;
+          const int t0 = cols ? (int)(threadIdx.x & (tb - 1)) : 0, t1 = cols ? t0 + 1 : tb;
+          const int j0 = cols ? (int)(threadIdx.x >> P.ltb) : (int)threadIdx.x;
+          for (int t = t0; t < t1 && tile.v0 + t < vn0; ++t) {
+               const C *sp = src_of<C>(P, tile, A, t) + (long long)j0 * P.is;
+               const long long ss = (long long)J * P.is;
+               C *dp = b0 + t * sms;
+               if (!A.l2only) {
+                    /* every copy of the thread in flight at once */
+                    for (int j = j0; j < N; j += J, sp += ss) cp_async_elem<C>(dp + gpad(j), sp);
+               } else {
+                    /* written earlier in this launch: through L2 only */
+                    constexpr int U = 4;
+                    for (int j = j0; j < N; j += U * J, sp += U * ss) {
+                         C x[U];
+#pragma unroll
+                         for (int u = 0; u < U; ++u)
+                              if (j + u * J < N) x[u] = __ldcg(sp + u * ss);
+#pragma unroll
+                         for (int u = 0; u < U; ++u)
+                              if (j + u * J < N) dp[gpad(j + u * J)] = x[u];
+                    }
+               }
+          }
+          cp_async_wait_all_groups();
+     } else if (kind == GB_KIND_C2C && !A.l2only) {
           /* complex elements straight into b0, every copy of the thread in
            * flight at once (an input written earlier in the same launch,
            * l2only, takes the register path below: it must not be read
@@ -1232,7 +1280,27 @@ __device__ void gen_tile(const gb_pass &P, const tile_t &tile, const gen_addr &A
      }
 
      /* ---------------- store ---------------- */
-     if (kind == GB_KIND_C2C) {
+     if (st_fast) {
+          const bool cols = P.store_mode == GB_MOVE_COLS;
+          const int J = cols ? (int)(blockDim.x >> P.ltb) : (int)blockDim.x;
+          const int t0 = cols ? (int)(threadIdx.x & (tb - 1)) : 0, t1 = cols ? t0 + 1 : tb;
+          const int j0 = cols ? (int)(threadIdx.x >> P.ltb) : (int)threadIdx.x;
+          for (int t = t0; t < t1 && tile.v0 + t < vn0; ++t) {
+               const long long v = tile.v0 + t;
+               C *op = dst_of<C>(P, tile, A, t) + (long long)j0 * P.os;
+               const long long os = (long long)J * P.os;
+               const C *rp = res + t * sms;
+               /* four-step twiddle exponent (P.post_vdim ? vpost : v) * k, advanced by J */
+               const long long pv = P.post_vdim ? tile.vpost : v;
+               long long m = pv * j0;
+               const long long ms = pv * J;
+               for (int k = j0; k < N; k += J, op += os, m += ms) {
+                    C y = rp[gpad(k)];
+                    if (P.post_N) y = cmul(y, post_twiddle<C>(P, m));
+                    *op = y;
+               }
+          }
+     } else if (kind == GB_KIND_C2C) {
           tile_walk wk(threadIdx.x, tb, N, P.store_mode, blockDim.x);
           for (int idx = threadIdx.x; idx < tb * N; idx += blockDim.x, wk.step()) {
                const int t = wk.t(), k = wk.j();

@@ -64,6 +64,32 @@ __global__ void k_stage_twiddles(C *dst, int N, int len)
      }
 }
 
+/* Stage twiddles of a runtime-radix pass (layout of gb_pass.tw_gen): the
+ * stage of span Ns and radix R holds entries Ns - 1 + (r - 1) Ns + k =
+ * exp(-2 pi i r k / (Ns R)), r = 1..R-1, k < Ns; the same values as the
+ * full table's entries r k N / (Ns R) (FP64, exact octant reduction, rounded
+ * once). */
+struct gen_radices { int n; int r[GB_MAXRAD]; };
+template <typename C>
+__global__ void k_gen_stage_twiddles(C *dst, int N, gen_radices R)
+{
+     typedef typename real_of<C>::T RT;
+     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N - 1; j += gridDim.x * blockDim.x) {
+          int ns = 1;
+          for (int s = 0; s < R.n; ++s) {
+               const int span = ns * R.r[s];
+               if (j < span - 1) {
+                    const int loc = j - (ns - 1), r = loc / ns + 1, k = loc - (r - 1) * ns;
+                    double c, sn;
+                    cexp_fp64((long long)r * k * (N / span), N, -1, &c, &sn);
+                    dst[j] = mk<C>((RT)c, (RT)sn);
+                    break;
+               }
+               ns = span;
+          }
+     }
+}
+
 /* Rows of the four-step twiddle: entry v T + t = exp(-2 pi i v t / N). */
 template <typename C>
 __global__ void k_post_rows(C *dst, long long N, int T, long long count)
@@ -324,6 +350,27 @@ extern "C" int gb_stage_twiddles(void *dst, int prec, int nfft, void *stream)
      if (prec == 4) k_stage_twiddles<float2><<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, nfft, len);
      else k_stage_twiddles<double2><<<blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, nfft, len);
      return gb_check(cudaGetLastError(), "stage twiddle generation");
+}
+
+extern "C" int gb_gen_stage_twiddles(void *dst, int prec, int nfft, const int *rad, int nrad, void *stream)
+{
+     gen_radices R;
+     long long prod = 1;
+     int i;
+     if (nrad < 0 || nrad > GB_MAXRAD) return -1;
+     R.n = nrad;
+     for (i = 0; i < nrad; ++i) {
+          R.r[i] = rad[i];
+          prod *= rad[i];
+     }
+     if (prod != nfft || nfft < 2) {
+          snprintf(gb_errbuf, sizeof gb_errbuf, "runtime-radix stage twiddles: radices do not multiply to %d", nfft);
+          return -1;
+     }
+     const int blocks = (nfft - 1 + 255) / 256;
+     if (prec == 4) k_gen_stage_twiddles<float2><<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)dst, nfft, R);
+     else k_gen_stage_twiddles<double2><<<blocks, 256, 0, (cudaStream_t)stream>>>((double2 *)dst, nfft, R);
+     return gb_check(cudaGetLastError(), "runtime-radix stage twiddle generation");
 }
 
 extern "C" int gb_post_rows(void *dst, int prec, long long N, int T, long long rows, void *stream)

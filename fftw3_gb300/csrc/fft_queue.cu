@@ -107,8 +107,8 @@ __device__ __forceinline__ bool reg_item_at(const gb_pass &P, const tile_t &tile
      }
 }
 
-/* Copy one 496-byte item descriptor into shared memory with 16-byte
- * asynchronous copies (threads 0..30), completed by cp_async_wait_all. */
+/* Copy one item descriptor (512 bytes) into shared memory with 16-byte
+ * asynchronous copies (threads 0..31), completed by cp_async_wait_all. */
 static_assert(sizeof(gb_qitem) % 16 == 0, "queue items are copied in 16-byte pieces");
 __device__ __forceinline__ void item_copy_async(gb_qitem *dst, const gb_qitem *src)
 {

@@ -144,6 +144,29 @@ const void *gb_table_stage_twiddle(int prec, int nfft)
      return p;
 }
 
+/* the stage twiddles of a runtime-radix pass with radix list rad (layout of
+ * gb_pass.tw_gen); keyed on nfft and the list, four bits a radix - 1 */
+static const void *table_gen_stage(int prec, int nfft, const int *rad, int nrad)
+{
+     long long k0 = 0, k1 = nrad;
+     void *p;
+     int i;
+     for (i = 0; i < nrad; ++i) {
+          if (rad[i] < 2 || rad[i] > 16) return 0;
+          if (i < 15) k0 |= (long long)(rad[i] - 1) << (4 * i);
+          else k1 |= (long long)(rad[i] - 1) << (4 * (i - 15) + 8);
+     }
+     p = tab_find(prec, 7, nfft, k0, k1);
+     if (p) return p;
+     p = tab_add(prec, 7, nfft, k0, k1, (size_t)(nfft > 1 ? nfft - 1 : 1) * 2 * prec);
+     if (!p || gb_dry) return p;
+     if (gb_gen_stage_twiddles(p, prec, nfft, rad, nrad, 0) || cudaDeviceSynchronize() != cudaSuccess) {
+          gb_set_error("runtime-radix stage twiddle generation failed: %s", gb_last_cuda_error());
+          return 0;
+     }
+     return p;
+}
+
 /* rows of the four-step twiddle W_N^(v t), v < rows, t < T (gb_pass.post_rows) */
 static const void *table_post_rows(int prec, long long N, int T, long long rows)
 {
@@ -592,6 +615,10 @@ static int pass_tables(gb_pass *P)
      if (P->nfft >= 32 && (P->nfft & (P->nfft - 1)) == 0) {
           P->tw_stage = gb_table_stage_twiddle(prec, P->nfft);
           if (!P->tw_stage) return -1;
+     }
+     if (P->variant == GB_VAR_GEN && P->nrad > 0 && P->nfft > 1) {
+          P->tw_gen = table_gen_stage(prec, P->nfft, P->rad, P->nrad);
+          if (!P->tw_gen) return -1;
      }
      if ((P->kind == GB_KIND_R2C || P->kind == GB_KIND_C2R) && P->n % 2 == 0) {
           P->tw_half = gb_table_twiddle(prec, P->n, P->n / 2 + 1, 1);

@@ -100,6 +100,11 @@ typedef struct gb_pass {
       * bottleneck of double passes).  Stages follow one another
       * (gb_stage_tw_len entries in all). */
      const void *tw_stage;
+     /* runtime-radix passes: the twiddles of each stage (span Ns, radix R) in
+      * rows r = 1..R-1 of Ns entries exp(-2 pi i r k / (Ns R)), k < Ns, the
+      * stage's rows starting at entry Ns - 1 (nfft - 1 entries in all), so a
+      * warp's reads are coalesced; 0 when absent (then read from tw) */
+     const void *tw_gen;
      const void *tw_half; /* r2c/c2r: exp(-2 pi i k / n), k <= n/2 */
      /* four-step: multiply output k of the transform whose index along
       * vector dimension 0 is v by exp(sign 2 pi i v k / post_N).  The
@@ -141,6 +146,7 @@ typedef struct gb_qitem {
      const void *const *pin;
      void *const *pout;
      int wait_ctr, wait_target, signal_ctr, pad_;
+     long long pad2_;   /* the size a multiple of 16 bytes (copied in 16-byte pieces) */
 } gb_qitem;
 
 /* Device status codes written to gb_pass.status. */
@@ -196,6 +202,7 @@ int gb_pass_configure(gb_pass *p, int max_smem_optin);
 int gb_twiddles(void *dst, int prec, long long n, long long count, long long mul, void *stream);
 int gb_stage_twiddles(void *dst, int prec, int nfft, void *stream);
 int gb_post_rows(void *dst, int prec, long long N, int T, long long rows, void *stream);
+int gb_gen_stage_twiddles(void *dst, int prec, int nfft, const int *rad, int nrad, void *stream);
 int gb_cols_tma_smem(int nfft, int tb, int groups);
 #define GB_SPLIT_MAXD 32   /* dims of a split-array problem: vector + transform dims */
 /* split-array pack (pack != 0: re/im strided -> dense complex buf) and
