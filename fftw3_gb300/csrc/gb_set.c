@@ -57,6 +57,10 @@ struct gb_set {
      size_t scratch_bytes;
      void *stream;
      int async;
+     /* the large-tile queue runs beside the small-tile one: a second stream
+      * forked from and joined back into the set's stream inside the capture */
+     cudaStream_t side;
+     cudaEvent_t ev_fork, ev_join;
      cudaGraph_t graph;
      cudaGraphExec_t gexec;
      int nsingle_items, nlong, ntransforms;
@@ -513,18 +517,34 @@ static int build_graph(gb_set *S)
           own = 1;
      } else st = (cudaStream_t)S->stream;
      /* the status word the queue kernels report to is allocated on first
-      * use, which must not happen inside the capture */
+      * use, which must not happen inside the capture; so are the side stream
+      * and its events */
      if (!gb_device_status_ptr()) rc = -1;
+     if (!rc && S->nlarge && !S->side &&
+         (cudaStreamCreateWithFlags(&S->side, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&S->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&S->ev_join, cudaEventDisableTiming) != cudaSuccess))
+          rc = -1;
      if (!rc && cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = -1;
      if (!rc) {
           cudaMemsetAsync(S->d_head, 0, 2 * sizeof(int), st);
           if (S->nctr) cudaMemsetAsync(S->d_ctrs, 0, sizeof(int) * (size_t)S->nctr, st);
-          if (S->nlarge && gb_launch_queue(S->d_items + S->nsmall, S->nlarge, S->d_head + 1, S->d_ctrs, S->prec,
-                                           S->threads_l, S->smem_l, S->grid_l, S->wait_ns, st))
-               rc = -1;
+          if (S->nlarge) {
+               /* the large-tile queue (no item of either queue waits on the
+                * other's) on the side stream, captured first so its CTAs are
+                * placed first; the small-tile queue's persistent CTAs fill
+                * what is left and take the SMs the large tiles free */
+               if (cudaEventRecord(S->ev_fork, st) != cudaSuccess ||
+                   cudaStreamWaitEvent(S->side, S->ev_fork, 0) != cudaSuccess ||
+                   gb_launch_queue(S->d_items + S->nsmall, S->nlarge, S->d_head + 1, S->d_ctrs, S->prec, S->threads_l,
+                                   S->smem_l, S->grid_l, S->wait_ns, S->side) ||
+                   cudaEventRecord(S->ev_join, S->side) != cudaSuccess)
+                    rc = -1;
+          }
           if (S->nsmall && gb_launch_queue(S->d_items, S->nsmall, S->d_head, S->d_ctrs, S->prec, S->threads,
                                            S->smem, S->grid, S->wait_ns, st))
                rc = -1;
+          if (S->nlarge && cudaStreamWaitEvent(st, S->ev_join, 0) != cudaSuccess) rc = -1;
           if (cudaStreamEndCapture(st, &S->graph) != cudaSuccess) rc = -1;
      }
      if (!rc && cudaGraphInstantiate(&S->gexec, S->graph, 0) != cudaSuccess) rc = -1;
@@ -630,6 +650,9 @@ void gb_destroy_set(gb_set *S)
      if (!S) return;
      if (S->gexec) cudaGraphExecDestroy(S->gexec);
      if (S->graph) cudaGraphDestroy(S->graph);
+     if (S->side) cudaStreamDestroy(S->side);
+     if (S->ev_fork) cudaEventDestroy(S->ev_fork);
+     if (S->ev_join) cudaEventDestroy(S->ev_join);
      cudaFree(S->d_items);
      cudaFree(S->d_head);
      cudaFree(S->d_ctrs);
