@@ -157,6 +157,13 @@ GB_EXT(fftwf_, fftwf_plan)
           gb_set_info((const gb_set *)s, nitems, ntransforms, nlong, grid, smem);      \
           return 0;                                                                    \
      }                                                                                 \
+     int PFX_##gb300_set_item_info(SET s, int i, int *kind, int *nfft, int *tb,        \
+                                   int *variant, int *queue, int *role)               \
+     {                                                                                 \
+          return s ? gb_set_item_info((const gb_set *)s, i, kind, nfft, tb, variant,   \
+                                      queue, role)                                     \
+                   : -1;                                                               \
+     }                                                                                 \
      int PFX_##gb300_set_wait_limit(SET s, double seconds)                             \
      {                                                                                 \
           return s ? gb_set_wait_limit((gb_set *)s, seconds) : -1;                     \

@@ -188,6 +188,7 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags);
 int gb_execute_set(gb_set *S);
 void gb_set_stream_of_set(gb_set *S, void *stream, int async);
 void gb_set_info(const gb_set *S, int *nitems, int *ntransforms, int *nlong, int *grid, int *smem);
+int gb_set_item_info(const gb_set *S, int i, int *kind, int *nfft, int *tb, int *variant, int *queue, int *role);
 int gb_set_wait_limit(gb_set *S, double seconds);
 int gb_set_test_stall(gb_set *S, int on);
 void gb_destroy_set(gb_set *S);

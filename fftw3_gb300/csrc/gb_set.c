@@ -63,6 +63,7 @@ struct gb_set {
      cudaEvent_t ev_fork, ev_join;
      cudaGraph_t graph;
      cudaGraphExec_t gexec;
+     gb_qitem *h_items;             /* dry run (no GPU): the items, kept on the host for inspection */
      int nsingle_items, nlong, ntransforms;
      unsigned long long wait_ns;    /* bound on a row tile's wait for its column tiles */
      int stall_item;                /* item whose wait target the test hook raised (-1: none) */
@@ -275,7 +276,7 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
      xform *xs;
      int nx = 0, i;
      const int cs = 2 * prec;
-     if (gb_dry_run() || !gb_cuda_ready()) {
+     if (!gb_dry_run() && !gb_cuda_ready()) {
           gb_set_error("plan sets need a GPU");
           return 0;
      }
@@ -312,7 +313,7 @@ gb_set *gb_mkset(int prec, int nplans, gb_plan *const *plans, unsigned flags)
                     return 0;
                }
           }
-     } else if (!(flags & FFTW_ESTIMATE)) {
+     } else if (!(flags & FFTW_ESTIMATE) && !gb_dry_run()) {
           tune_set(prec, xs, nx, flags);
      }
      S = build_set(prec, xs, nx);
@@ -451,6 +452,18 @@ static gb_set *build_set(int prec, xform *xs, int nx)
      S->wait_ns = 2000000000ull;
      S->stall_item = -1;
      S->scratch_bytes = (size_t)scratch_elems * cs;
+     if (gb_dry_run()) {
+          /* no device: the items stay on the host (gb_set_item_info), the
+           * launch shape is unknown (grid 0) and the set cannot execute */
+          S->h_items = (gb_qitem *)malloc(sizeof(gb_qitem) * (size_t)(S->nitems ? S->nitems : 1));
+          if (!S->h_items) { free(S); goto fail; }
+          memcpy(S->h_items, A, sizeof(gb_qitem) * (size_t)na);
+          memcpy(S->h_items + na, M, sizeof(gb_qitem) * (size_t)nm);
+          memcpy(S->h_items + na + nm, B, sizeof(gb_qitem) * (size_t)nb);
+          memcpy(S->h_items + na + nm + nb, Lg, sizeof(gb_qitem) * (size_t)nl);
+          free(QA.v); free(QM.v); free(QB.v); free(QL.v); free(hptr);
+          return S;
+     }
      S->grid = S->nsmall ? gb_queue_grid(prec, S->threads, S->smem) : 1;
      S->grid_l = S->nlarge ? gb_queue_grid(prec, S->threads_l, S->smem_l) : 1;
      if (S->grid <= 0 || S->grid_l <= 0) { gb_set_error("plan set: queue kernel does not fit (smem %d/%d)", smem, smem_l); free(S); goto fail; }
@@ -559,6 +572,10 @@ static int build_graph(gb_set *S)
 int gb_execute_set(gb_set *S)
 {
      cudaStream_t st = (cudaStream_t)S->stream;
+     if (S->h_items) {
+          gb_set_error("plan set: planned in dry run, cannot execute");
+          return -1;
+     }
      if (build_graph(S)) return -1;
      if (cudaGraphLaunch(S->gexec, st) != cudaSuccess) {
           gb_set_error("plan set: graph launch failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -610,6 +627,10 @@ int gb_set_test_stall(gb_set *S, int on)
 {
      const size_t off = offsetof(gb_qitem, wait_target);
      int i, v;
+     if (S->h_items) {
+          gb_set_error("plan set: planned in dry run");
+          return -1;
+     }
      if (on && S->stall_item < 0) {
           for (i = 0; i < S->nsmall && S->stall_item < 0; ++i) {
                gb_qitem it;
@@ -645,9 +666,41 @@ void gb_set_info(const gb_set *S, int *nitems, int *ntransforms, int *nlong, int
 
 int gb_set_large_items(const gb_set *S) { return S->nlarge; }
 
+/* Item i of the set in queue order (the small-tile queue's items, then the
+ * large-tile queue's): its kind, FFT length, transforms, body (variant),
+ * queue (0 small, 1 large) and role (1 a column tile others wait for, 2 a
+ * row tile that waits, 0 a single).  Returns 0, or -1 for a bad index or a
+ * failed read. */
+int gb_set_item_info(const gb_set *S, int i, int *kind, int *nfft, int *tb, int *variant, int *queue, int *role)
+{
+     gb_qitem it;
+     if (i < 0 || i >= S->nitems) {
+          gb_set_error("plan set: no item %d", i);
+          return -1;
+     }
+     if (S->h_items) it = S->h_items[i];
+     else if (cudaMemcpy(&it, S->d_items + i, sizeof it, cudaMemcpyDeviceToHost) != cudaSuccess) {
+          gb_set_error("plan set: %s", cudaGetErrorString(cudaGetLastError()));
+          return -1;
+     }
+     *kind = it.P.kind;
+     *nfft = it.P.nfft;
+     *tb = it.P.tb;
+     *variant = it.P.variant;
+     *queue = i >= S->nsmall;
+     *role = it.wait_ctr >= 0 ? 2 : it.signal_ctr >= 0 ? 1 : 0;
+     return 0;
+}
+
 void gb_destroy_set(gb_set *S)
 {
      if (!S) return;
+     if (S->h_items) {
+          /* a dry-run set holds no device resources */
+          free(S->h_items);
+          free(S);
+          return;
+     }
      if (S->gexec) cudaGraphExecDestroy(S->gexec);
      if (S->graph) cudaGraphDestroy(S->graph);
      if (S->side) cudaStreamDestroy(S->side);

@@ -77,6 +77,13 @@ extern int PFX##gb300_execute_set(PFX##gb300_set s);                            
 extern int PFX##gb300_set_stream_set(PFX##gb300_set s, void *cuda_stream, int async); \
 extern int PFX##gb300_set_info(PFX##gb300_set s, int *nitems, int *ntransforms,       \
                                int *nlong, int *grid, int *smem);                     \
+/* Item i in queue order: kind (gb_kind), FFT length, transforms, body      \
+ * (variant), queue (0 small tiles, 1 large tiles), role (1 a column tile   \
+ * row tiles wait for, 2 a row tile that waits, 0 a single).  Sets planned  \
+ * under fftw_gb300_set_dry_run(1) keep their items on the host (grid 0,    \
+ * no execute).                                                             */\
+extern int PFX##gb300_set_item_info(PFX##gb300_set s, int i, int *kind, int *nfft,    \
+                                    int *tb, int *variant, int *queue, int *role);    \
 /* Bound (seconds, default 2) on a row tile's device-side wait for the      \
  * column tiles of its transform; a wait that runs out skips the tile and   \
  * sets device status 2.  Test hook: set_test_stall(s, 1) makes the first   \
