@@ -264,3 +264,31 @@ def test_wisdom_groups_and_radix_order(lib):
     finally:
         lib.fftwf_forget_wisdom()
         g.set_dry_run(False)
+
+
+def test_tensor_core_builds(monkeypatch):
+    """FFTW_GB300_TENSOR_CORE plans: unit-stride rows take the two-CTA build
+    (a bulk copy-in buffer, 87 KB of shared memory), the strided passes of a
+    four-step length the three-CTA build (54 KB, no second buffer);
+    FFTW_GB300_TC_CTAS overrides; the four-GEMM-stage budget leaves a third
+    axis of 256^3 in FP32."""
+    TC = 1 << 28
+    monkeypatch.delenv("FFTW_GB300_TC_CTAS", raising=False)
+    rows = g.plan_many_dft([4096], 1024, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE | TC, "f")
+    (ps,) = passes(rows)
+    assert ps["variant"] == 3 and ps["threads"] == 256
+    assert "tc-split-fp16" in rows.describe() and "ctas=3" not in rows.describe()
+    four = g.plan_many_dft([65536], 16, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE | TC, "f")
+    ps4 = passes(four)
+    assert len(ps4) == 2 and all(p["variant"] == 3 for p in ps4)
+    assert four.describe().count("ctas=3") == 2
+    assert all(p["smem"] < rows.passes()[0]["smem"] for p in ps4)
+    monkeypatch.setenv("FFTW_GB300_TC_CTAS", "3")
+    rows3 = g.plan_many_dft([4096], 1024, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE | TC, "f")
+    assert "ctas=3" in rows3.describe()
+    monkeypatch.setenv("FFTW_GB300_TC_CTAS", "2")
+    four2 = g.plan_many_dft([65536], 16, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE | TC, "f")
+    assert "ctas=3" not in four2.describe()
+    monkeypatch.delenv("FFTW_GB300_TC_CTAS")
+    cube = g.plan_many_dft([256, 256, 256], 1, 1 << 20, 1 << 20, -1, g.FFTW_ESTIMATE | TC, "f")
+    assert [p["variant"] for p in passes(cube)].count(3) == 2
