@@ -164,7 +164,11 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_queue(const
           }
           __syncthreads();
           if (go) {
-               __threadfence();
+               /* an item that waited reads what other CTAs wrote in this
+                * launch: thread 0's acquire and the barrier order the reads
+                * after the wait, the fence keeps this thread's own earlier
+                * accesses from passing it; items that do not wait need none */
+               if (it.wait_ctr >= 0) __threadfence();
                C *b0 = (C *)gb_smem;
                C *b1 = b0 + it.P.tb * gen_sms(it.P.nfft);
                tile_t tile;
