@@ -547,6 +547,12 @@ def run_uneven(args):
         lib.fftwf_set_timelimit(-1.0)
     info = [ctypes.c_int() for _ in range(5)]
     lib.fftwf_gb300_set_info(s, *[ctypes.byref(v) for v in info])
+    # queue kernels a graph launch runs: the last item in queue order is in
+    # the large-tile queue when the set has one
+    it = [ctypes.c_int() for _ in range(6)]
+    lib.fftwf_gb300_set_item_info.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 6
+    lib.fftwf_gb300_set_item_info(s, info[0].value - 1, *[ctypes.byref(v) for v in it])
+    kernels_per_step = 2 if it[4].value == 1 else 1
     wis = ctypes.string_at(lib.fftwf_export_wisdom_to_string()).decode()
     tuned = wis.count('"set p4 n')
     # what the set tuner chose: fields variant tb load store n1 groups order
@@ -611,7 +617,9 @@ def run_uneven(args):
         "gbs": round(alg / (ms * 1e-3) / 1e9, 1),
         "roofline": {"bound": "hbm", "achieved": round(alg / (ms * 1e-3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(alg / (ms * 1e-3) / 1e9 / hbm, 4), "traffic": None, "peak_source": src},
-        "gpu_launches": args.steps, "launch_note": "one CUDA graph launch (one work-queue kernel) per step",
+        "gpu_launches": args.steps * kernels_per_step,
+        "launch_note": "one CUDA graph launch per step: the small-tile work-queue kernel, and the large-tile one "
+                       "beside it when the set has items that need 8192-point tiles",
         "loop_baseline": {"value": round(fl / (ms_loop * 1e-3) / 1e9, 2), "ms_per_step": round(ms_loop, 3),
                           "kernel_launches_per_step": loop_launches},
         "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,

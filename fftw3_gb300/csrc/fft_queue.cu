@@ -1,10 +1,12 @@
 /*
  * Work-queue kernel of a plan set: persistent CTAs (as many as fit on the
- * device) claim items from a device queue with one atomic each and run them
- * with the shared-memory tile body of k_gen, or, for power-of-two float items
- * of 64..4096 points, with the register stages of k_reg.  Items of one long transform
- * are ordered column tiles first, row tiles last; a row tile waits for its
- * transform's column tiles on a device counter.  Every wait is bounded
+ * device) claim items from a device queue with one atomic each (one item
+ * ahead) and run them with the shared-memory tile body of k_gen, or, for
+ * power-of-two float items of 64..4096 points whose set asks for it (the set
+ * tuner's wisdom or FFTW_GB300_QUEUE_BODY=reg), with the register stages of
+ * k_reg.  Items of one long transform are ordered column tiles first, row
+ * tiles last; a row tile waits for its transform's column tiles on a device
+ * counter.  Every wait is bounded
  * (wait_ns of wall time, 2 s unless the set says otherwise); a wait that
  * gives up writes GB_STATUS_QUEUE_TIMEOUT to the status word and the item is
  * skipped, so the kernel always finishes.
