@@ -178,3 +178,35 @@ def test_dry_run_set_does_not_execute():
     v = [ctypes.c_int() for _ in range(6)]
     assert item(s, 10 ** 6, *[ctypes.byref(x) for x in v]) == -1
     _destroy(lib, pfx, s)
+
+
+def test_set_wisdom_entries_steer_items():
+    """The set tuner's wisdom entries ("set p4 n<n>": variant, tb, load, store,
+    n1, groups, order), imported as text, steer the items: the register body
+    for a power-of-two length, Rader for a prime, another split for a long
+    length, fewer transforms per item; with an entry for every length the
+    set plans under FFTW_WISDOM_ONLY."""
+    lib = g.load()
+    lib.fftwf_forget_wisdom()
+    head = ctypes.string_at(lib.fftwf_export_wisdom_to_string()).decode().rstrip().rstrip(")")
+    ent = lambda n, *f: '  (gb300-pass "set p4 n%d" %s)\n' % (n, " ".join("#x%x" % (v & 0xffffffff) for v in f))
+    text = head + ent(4096, 0, 0, 0, 0, 0, 0, 0) + ent(97, 5, 0, 0, 0, 0, 0, 0) + \
+        ent(65536, -1, 0, 0, 0, 64, 0, 0) + ent(256, -1, 4, 0, 0, 0, 0, 0) + ")\n"
+    assert lib.fftwf_import_wisdom_from_string(text.encode()) == 1, text
+    lengths = [4096, 97, 65536, 256, 256, 256, 256, 256, 256]
+    lib_, pfx, s, plans = _plan_set(lengths, flags=g.FFTW_ESTIMATE | g.FFTW_WISDOM_ONLY)
+    assert s, g.last_error()
+    items = _items(lib, pfx, s, _info(lib, pfx, s)["nitems"])
+    by = {}
+    for it in items:
+        by.setdefault(it["nfft"], []).append(it)
+    assert all(it["variant"] == GB_VAR_REG for it in by[4096])
+    assert [it["kind"] for it in by[96]] == [GB_KIND_RADER]
+    assert all(it["role"] for it in by[64] + by[1024]) and 64 in by and 1024 in by
+    singles256 = [it for it in by[256] if not it["role"]]
+    assert [it["tb"] for it in singles256] == [4, 2]
+    _destroy(lib, pfx, s)
+    # a length without an entry: refused under FFTW_WISDOM_ONLY
+    lib_, pfx, s, plans = _plan_set(lengths + [1000], flags=g.FFTW_ESTIMATE | g.FFTW_WISDOM_ONLY)
+    assert not s
+    lib.fftwf_forget_wisdom()
