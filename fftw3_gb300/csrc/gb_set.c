@@ -804,8 +804,8 @@ static void entry_reset(gb_wisdom_entry *e, int kind)
  * competes for the instruction cache, and items of all lengths share the
  * SMs.  So each kind of choice (register bodies, prime algorithms, splits,
  * radix orders, tiles) is timed once more on a scratch copy of the whole
- * set against the same set without it, and kept only when the whole set
- * runs faster with it (by more than 1%). */
+ * set against the same set without it, and taken back when the whole set
+ * runs more than 1% faster without it. */
 typedef struct { long long n, pts; int sign; } lclass;
 
 static void whole_set_check(int prec, const xform *xs, int nx, const lclass *cl, int ncl, cudaStream_t st, int reps)
