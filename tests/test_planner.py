@@ -292,3 +292,27 @@ def test_tensor_core_builds(monkeypatch):
     monkeypatch.delenv("FFTW_GB300_TC_CTAS")
     cube = g.plan_many_dft([256, 256, 256], 1, 1 << 20, 1 << 20, -1, g.FFTW_ESTIMATE | TC, "f")
     assert [p["variant"] for p in passes(cube)].count(3) == 2
+
+
+def test_benchmark_workload_passes():
+    """The passes the measured workloads run (kind, FFT length, variant):
+    one bulk-copy fed pass for the unit-stride batches (c2c 4096, c2c 1024
+    double, r2c 16384 on its 8192-point core), tensor-map column passes for
+    both four-step passes of 65536 and 2^20 and for the strided axes of 512^3
+    and of the 8192^2 r2c (whose 8192-point column axis is itself a
+    four-step)."""
+    TMA, COLS = 2, 4
+    def shape(p):
+        return [(x["kind"], x["nfft"], x["variant"]) for x in p.passes()]
+    assert shape(g.plan_many_dft([4096], 65536, 1 << 20, 1 << 32, -1, g.FFTW_ESTIMATE, "f")) == [(0, 4096, TMA)]
+    assert shape(g.plan_many_dft([1024], 4096, 1 << 20, 1 << 32, -1, g.FFTW_ESTIMATE, "d")) == [(0, 1024, TMA)]
+    assert shape(g.plan_many_dft_r2c([16384], 16384, 1 << 20, 1 << 34, g.FFTW_ESTIMATE, "f")) == [(1, 8192, TMA)]
+    assert shape(g.plan_many_dft([65536], 4096, 1 << 20, 1 << 32, -1, g.FFTW_ESTIMATE, "f")) == \
+        [(0, 256, COLS), (0, 256, COLS)]
+    assert shape(g.plan_many_dft([1 << 20], 64, 1 << 20, 1 << 32, -1, g.FFTW_ESTIMATE, "f")) == \
+        [(0, 1024, COLS), (0, 1024, COLS)]
+    assert shape(g.plan_many_dft([512, 512, 512], 1, 1 << 20, 1 << 20, -1, g.FFTW_ESTIMATE, "f")) == \
+        [(0, 512, TMA), (0, 512, COLS), (0, 512, COLS)]
+    r2d = shape(g.plan_many_dft_r2c([8192, 8192], 1, 1 << 20, 1 << 32, g.FFTW_ESTIMATE, "f"))
+    assert r2d[0] == (1, 4096, TMA) and [v for _, _, v in r2d[1:]] == [COLS, COLS]
+    assert r2d[1][1] * r2d[2][1] == 8192
