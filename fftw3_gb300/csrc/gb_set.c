@@ -5,8 +5,9 @@
  * The reference executes a set of transforms as a loop of fftw_execute calls,
  * one plan after another (each a tree of solver applies, api/execute.c:23-27).
  * Here the set compiles to queue items (gb_qitem):
- *   - a transform that fits one CTA's shared memory (2 buffers of nfft+1
- *     complex, nfft <= 4096 single / 2048 double) is a "single"; singles of
+ *   - a transform that fits one CTA's shared memory (2 buffers of
+ *     nfft + nfft/16 + 1 complex, the padded layout; nfft <= 4096 single /
+ *     2048 double) is a "single"; singles of
  *     the same length, sign and strides are grouped into items of up to 32
  *     transforms, each transform with its own array pointers;
  *   - a prime length is a Bluestein single (power-of-two convolution) or, if
