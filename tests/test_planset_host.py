@@ -210,3 +210,30 @@ def test_set_wisdom_entries_steer_items():
     lib_, pfx, s, plans = _plan_set(lengths + [1000], flags=g.FFTW_ESTIMATE | g.FFTW_WISDOM_ONLY)
     assert not s
     lib.fftwf_forget_wisdom()
+
+
+@pytest.mark.parametrize("prec,seed", [("f", 1), ("f", 2), ("f", 3), ("d", 4), ("d", 5)])
+def test_random_sets_cover_every_transform(prec, seed):
+    """Seeded uneven sets in both precisions: every transform is a single
+    (the singles' transforms per item add up) or one long transform; the
+    small-tile queue keeps column tiles, singles, row tiles in that order;
+    every item fits a small- or large-tile buffer."""
+    import bench
+    rng = np.random.default_rng(seed)
+    if prec == "f":
+        lengths = bench.uneven_lengths(rng, 600)
+    else:
+        lengths = bench.uneven_lengths(rng, 400, max_pow2=14, max_smooth=20000, max_prime=2047)
+    lengths += [1, 2, 3]
+    lib, pfx, s, plans = _plan_set(lengths, prec)
+    assert s, g.last_error()
+    info = _info(lib, pfx, s)
+    items = _items(lib, pfx, s, info["nitems"])
+    assert info["ntransforms"] == len(lengths)
+    assert sum(it["tb"] for it in items if it["role"] == 0) + info["nlong"] == len(lengths)
+    roles = [it["role"] for it in items if it["queue"] == 0]
+    assert roles == sorted(roles, key=lambda r: (1, 0, 2).index(r))
+    for it in items:
+        cap = QBUF[prec] * (2 if it["queue"] else 1)
+        assert it["tb"] * gen_sms(it["nfft"]) <= cap or it["tb"] == 1 and gen_sms(it["nfft"]) <= cap, it
+    _destroy(lib, pfx, s)
