@@ -88,6 +88,7 @@ const char fftwf_codelet_optim[] = "sm_103a register/shared-memory stages";
 const char *fftw_gb300_last_error(void) { return gb_last_error(); }
 int fftw_gb300_failures(void) { return __atomic_load_n(&gb_fail_count, __ATOMIC_RELAXED); }
 void fftw_gb300_set_dry_run(int on) { gb_set_dry_run(on); }
+void fftw_gb300_fail_alloc_after(int k) { gb_fail_alloc_after(k); }
 long long fftw_gb300_launch_count(void) { return gb_launch_count(); }
 
 #define GB_EXT(PFX_, PLAN)                                                              \

@@ -124,6 +124,7 @@ void gb_problem_key(const gb_problem *prb, char *key, size_t cap);   /* wisdom k
 void gb_destroy(gb_plan *p);
 int gb_dry_run(void);
 void gb_set_dry_run(int on);
+void gb_fail_alloc_after(int k);   /* test hook: the table allocation after the next k fails once */
 const char *gb_last_error(void);
 void gb_set_error(const char *fmt, ...);
 void gb_lock(void);

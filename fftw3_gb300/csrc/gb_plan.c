@@ -96,10 +96,20 @@ static void *tab_find(int prec, int type, long long a, long long b, long long c)
      return 0;
 }
 
+/* Test hook for the planner's handling of a failed device allocation: the
+ * table allocation after the next k fails once, as a refused cudaMalloc
+ * would (-1: none).  Applies in dry runs too, where tables are not cached. */
+static int fail_alloc_in = -1;
+void gb_fail_alloc_after(int k) { fail_alloc_in = k < 0 ? -1 : k; }
+
 static void *tab_add(int prec, int type, long long a, long long b, long long c, size_t bytes)
 {
      tab *t;
      void *p = 0;
+     if (fail_alloc_in >= 0 && fail_alloc_in-- == 0) {
+          gb_set_error("cudaMalloc(%zu) for a twiddle table failed (injected)", bytes);
+          return 0;
+     }
      if (gb_dry) {
           static char dummy[64];
           return dummy;
@@ -1066,7 +1076,8 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           r1 = config_pass(&s->pass, prec, GB_KIND_C2C, n1, sign, n2 * is, 1, na, va, 0, 1);
           if (r1 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(p, &s->pass);
           s->pass.post_N = n;
-          if (r1 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass A config failed"); b->err = 1; return; }
+          if (r1) { if (!b->err) gb_set_error("four-step pass A config failed"); b->err = 1; return; }
+          if (pass_tables(&s->pass)) { b->err = 1; return; }   /* the table's own message stands */
           count_ops(p, &s->pass, howmany * n2);
           /* pass B: transform over n2 (scratch stride n1), dim0 = k1 */
           vb[nb].n = n1; vb[nb].is = 1; vb[nb].os = os; ++nb;
@@ -1083,7 +1094,8 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           if (nb > GB_MAXV) { gb_set_error("four-step with too many vector dims"); b->err = 1; return; }
           r2 = config_pass(&s->pass, prec, GB_KIND_C2C, n2, sign, n1, n1 * os, nb, vb, 0, 1);
           if (r2 == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(p, &s->pass);
-          if (r2 || pass_tables(&s->pass)) { if (!b->err) gb_set_error("four-step pass B config failed"); b->err = 1; return; }
+          if (r2) { if (!b->err) gb_set_error("four-step pass B config failed"); b->err = 1; return; }
+          if (pass_tables(&s->pass)) { b->err = 1; return; }
           count_ops(p, &s->pass, howmany * n1);
           return;
      }

@@ -28,6 +28,11 @@ extern int fftw_gb300_failures(void);
 /* Dry run: plans are compiled without touching a GPU (no allocation, no
  * launch) so the planner can be inspected on a machine without one. */
 extern void fftw_gb300_set_dry_run(int on);
+/* Test hook: the device table allocation after the next k (k >= 0) fails
+ * once, as a refused cudaMalloc would, so the planner's failure path (a NULL
+ * plan, the message in fftw_gb300_last_error) can be exercised on the host;
+ * -1 cancels.  Works in dry runs. */
+extern void fftw_gb300_fail_alloc_after(int k);
 /* Number of kernels this library has launched since it was loaded. */
 extern long long fftw_gb300_launch_count(void);
 /* Read and clear the device status word: 0 when no kernel reported a

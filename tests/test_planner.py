@@ -316,3 +316,33 @@ def test_benchmark_workload_passes():
     r2d = shape(g.plan_many_dft_r2c([8192, 8192], 1, 1 << 20, 1 << 32, g.FFTW_ESTIMATE, "f"))
     assert r2d[0] == (1, 4096, TMA) and [v for _, _, v in r2d[1:]] == [COLS, COLS]
     assert r2d[1][1] * r2d[2][1] == 8192
+
+
+@pytest.mark.parametrize("after", [0, 1, 3])
+def test_failed_device_allocation_gives_null_plan(lib, after):
+    """A device table allocation that fails (injected on the host, as a
+    refused cudaMalloc would) makes the planner return NULL with the reason in
+    fftw_gb300_last_error, for single-pass, four-step and r2c plans; the
+    injection fires once and the next plan is whole."""
+    lib.fftw_gb300_fail_alloc_after.argtypes = [ctypes.c_int]
+    for make in (lambda: g.plan_many_dft([4096], 64, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f"),
+                 lambda: g.plan_many_dft([1 << 20], 4, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f"),
+                 lambda: g.plan_many_dft_r2c([16384], 8, 1 << 20, 1 << 30, g.FFTW_ESTIMATE, "f")):
+        lib.fftw_gb300_fail_alloc_after(after)
+        try:
+            p = make()
+        except Exception:
+            p = None
+        failed = p is None or not getattr(p, "ptr", None)
+        lib.fftw_gb300_fail_alloc_after(-1)
+        if failed:
+            assert "injected" in g.last_error()
+        q = make()
+        assert q is not None and q.ptr and len(q.passes()) >= 1
+    # the single-pass plan needs more than one table, so the first allocation fails it
+    lib.fftw_gb300_fail_alloc_after(0)
+    with pytest.raises(Exception):
+        p = g.plan_many_dft([4096], 64, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f")
+        if p is None or not p.ptr:
+            raise RuntimeError(g.last_error())
+    lib.fftw_gb300_fail_alloc_after(-1)
