@@ -346,3 +346,30 @@ def test_failed_device_allocation_gives_null_plan(lib, after):
         if p is None or not p.ptr:
             raise RuntimeError(g.last_error())
     lib.fftw_gb300_fail_alloc_after(-1)
+
+
+def test_infeasible_wisdom_still_plans(lib):
+    """Wisdom entries whose configuration cannot apply (an unknown variant, a
+    tile too large for one CTA, a split that does not divide the length,
+    Rader for a prime whose n-1 has a factor above 13) leave the planner to
+    its own choices: every plan builds and stays within the launch limits,
+    as the reference forgets infeasible wisdom and re-plans
+    (api/apiplan.c:51-84)."""
+    lib.fftwf_forget_wisdom()
+    head = ctypes.string_at(lib.fftwf_export_wisdom_to_string()).decode().rstrip().rstrip(")")
+    ent = lambda key, *f: '  (gb300-pass "%s" %s)\n' % (key, " ".join("#x%x" % (v & 0xffffffff) for v in f))
+    cases = [("c2c p4 n4096", 7, 1000, 2, 2, 0, 0, 0), ("c2c p4 n4096", 1, 1000, 0, 0, 0, 0, 0),
+             ("c2c p4 n65536", -1, 0, 0, 0, 3, 0, 0), ("c2c p4 n1021", 5, 0, 0, 0, 0, 0, 0)]
+    for c in cases:
+        lib.fftwf_forget_wisdom()
+        assert lib.fftwf_import_wisdom_from_string((head + ent(*c) + ")\n").encode()) == 1
+        n = int(c[0].split("n")[-1])
+        p = g.plan_many_dft([n], 64, 1 << 20, 1 << 30, -1, g.FFTW_ESTIMATE, "f")
+        ps = p.passes()
+        assert ps and all(x["threads"] <= 1024 and x["smem"] <= 232448 and x["tb"] >= 1 for x in ps), (c, ps)
+        tot = 1
+        for x in ps:
+            if x["kind"] == 0:
+                tot *= x["nfft"]
+        assert tot == n or ps[0]["kind"] == 3, (c, ps)
+    lib.fftwf_forget_wisdom()
