@@ -820,6 +820,30 @@ static gb_step *add_pointwise(builder *b, int pw, long long n, long long nfft, i
 static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is, long long os,
                        int nv, const gb_dim *v_in, int src, int dst, int mid);
 
+/* An f32 r2c / c2r of even n whose half length M is a power of two of
+ * 256..4096 that the multi-pass route can take (unit real stride, even
+ * vector strides, caller arrays on both sides) and whose GEMM stages fit the
+ * plan's tensor-core budget: run it as the half-length c2c in the
+ * tensor-core form plus the hc2c pass (rdft/ct-hc2c.c:31-83). */
+static int tc_split_real(const gb_plan *p, int kind, long long n, long long is, long long os, int nvk,
+                         const gb_dim *v, int src, int dst)
+{
+     const long long M = n / 2;
+     int i;
+     if ((kind != GB_KIND_R2C && kind != GB_KIND_C2R) || p->prb.prec != 4 || n % 2) return 0;
+     if (M < 256 || M > 4096 || (M & (M - 1))) return 0;
+     if (p->tc_stages + (M == 4096 ? 3 : 2) > GB_TC_MAX_STAGES) return 0;
+     /* the route's own intermediate is the first scratch; an r2c may write
+      * the second (the padded rows of a 2D r2c's first pass), the c2c of M
+      * being one pass that needs no intermediate of its own */
+     if (src == GB_BUF_SCRATCH || dst == GB_BUF_SCRATCH || src == GB_BUF_SCRATCH2) return 0;
+     if (dst == GB_BUF_SCRATCH2 && kind != GB_KIND_R2C) return 0;
+     if (kind == GB_KIND_R2C ? is != 1 : os != 1) return 0;
+     for (i = 0; i < nvk; ++i)
+          if ((kind == GB_KIND_R2C ? v[i].is : v[i].os) % 2) return 0;
+     return 1;
+}
+
 static void add_1d(builder *b, int kind, long long n, int sign, long long is, long long os,
                    int nv, const gb_dim *v_in, int src, int dst)
 {
@@ -975,6 +999,11 @@ static void add_1d_mid(builder *b, int kind, long long n, int sign, long long is
           s = &p->step[p->nstep - 1];
      }
      if (rc == 0 && (p->flags & GB_FLAG_TENSOR_CORE)) use_tensor_cores(p, &s->pass);
+     /* the tensor-core form of an even r2c / c2r whose half length is a
+      * power of two the tensor-core kernel takes: the half-length complex
+      * FFT as its own pass (in the tensor-core form) and the hc2c post- or
+      * pre-pass beside it, through the multi-pass route below */
+     if (rc == 0 && (p->flags & GB_FLAG_TENSOR_CORE) && tc_split_real(p, kind, n, is, os, nvk, v, src, dst)) rc = 1;
      if (rc == 0) {
           if (pass_tables(&s->pass)) { b->err = 1; return; }
           count_ops(p, &s->pass, howmany);

@@ -173,3 +173,49 @@ def test_tc_3d_stage_budget(lib, torch_tc, restatement):
     ref = restatement.c2c(x.astype(np.complex128), shape, -1, "d", nthreads=8)
     assert rel_l2_f(a.cpu().numpy(), ref) <= 1e-6
     assert g.load().fftw_gb300_device_status() == 0
+
+
+@pytest.mark.parametrize("n,hm", [(8192, 32), (512, 64)])
+def test_tc_real_forms(lib, torch_tc, restatement, n, hm):
+    """r2c and c2r in the tensor-core form: the half-length c2c as tcgen05
+    GEMM stages beside the hc2c post- / pre-pass; r2c of N(0,1) reals and c2r
+    of that spectrum against the FP64 oracle (float bound)."""
+    import fftw3_gb300 as g
+    torch = torch_tc
+    rng = np.random.default_rng(n + hm)
+    nc = n // 2 + 1
+    x = rng.standard_normal(n * hm).astype(np.float32)
+    xi = torch.from_numpy(x).cuda()
+    yo = torch.empty(hm * nc, dtype=torch.complex64, device="cuda")
+    p = g.plan_many_dft_r2c([n], hm, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE, "f")
+    assert "tc-split-fp16" in p.describe()
+    p.execute()
+    torch.cuda.synchronize()
+    y = yo.cpu().numpy()
+    assert rel_l2(y, restatement.r2c(x.astype(np.float64), [n], "d")) <= 1e-6
+    zi = yo.clone()
+    ro = torch.empty(hm * n, dtype=torch.float32, device="cuda")
+    q = g.plan_many_dft_c2r([n], hm, zi.data_ptr(), ro.data_ptr(), g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE, "f")
+    assert "tc-split-fp16" in q.describe()
+    q.execute()
+    torch.cuda.synchronize()
+    assert rel_l2(ro.cpu().numpy(), restatement.c2r(y.astype(np.complex128), [n], "d")) <= 1e-6
+    assert g.load().fftw_gb300_device_status() == 0
+
+
+def test_tc_real_2d(lib, torch_tc, restatement):
+    """2D r2c 2048^2 in the tensor-core form (rows: the 1024-point half-length
+    c2c as GEMMs and the hc2c pass; columns FP32) against the oracle."""
+    import fftw3_gb300 as g
+    torch = torch_tc
+    rng = np.random.default_rng(2048)
+    x = rng.standard_normal(2048 * 2048).astype(np.float32)
+    xi = torch.from_numpy(x).cuda()
+    yo = torch.empty(2048 * 1025, dtype=torch.complex64, device="cuda")
+    p = g.plan_many_dft_r2c([2048, 2048], 1, xi.data_ptr(), yo.data_ptr(), g.FFTW_ESTIMATE | FFTW_GB300_TENSOR_CORE,
+                            "f")
+    assert "tc-split-fp16" in p.describe()
+    p.execute()
+    torch.cuda.synchronize()
+    assert rel_l2(yo.cpu().numpy(), restatement.r2c(x.astype(np.float64), [2048, 2048], "d")) <= 1e-6
+    assert g.load().fftw_gb300_device_status() == 0

@@ -373,3 +373,24 @@ def test_infeasible_wisdom_still_plans(lib):
                 tot *= x["nfft"]
         assert tot == n or ps[0]["kind"] == 3, (c, ps)
     lib.fftwf_forget_wisdom()
+
+
+def test_real_tensor_core_form(monkeypatch):
+    """FFTW_GB300_TENSOR_CORE r2c / c2r of an even length whose half length is
+    a power of two of 256..4096: the half-length c2c runs in the tensor-core
+    form beside the hc2c post- (r2c) or pre-pass (c2r); the 2D 8192^2 r2c
+    takes it for its rows, the columns stay FP32; without the flag the
+    single fused r2c pass is kept, and r2c 16384 (an 8192-point core) stays
+    FP32."""
+    TC, HC2C = 1 << 28, 6
+    monkeypatch.delenv("FFTW_GB300_TC_CTAS", raising=False)
+    def shape(p):
+        return [(x["kind"], x["nfft"], x["variant"]) for x in p.passes()]
+    assert shape(g.plan_many_dft_r2c([8192], 64, 1 << 20, 1 << 30, g.FFTW_ESTIMATE | TC, "f")) == \
+        [(0, 4096, 3), (HC2C, 4096, 1)]
+    assert shape(g.plan_many_dft_c2r([8192], 64, 1 << 20, 1 << 30, g.FFTW_ESTIMATE | TC, "f")) == \
+        [(HC2C, 4096, 1), (0, 4096, 3)]
+    assert shape(g.plan_many_dft_r2c([8192], 64, 1 << 20, 1 << 30, g.FFTW_ESTIMATE, "f")) == [(1, 4096, 2)]
+    assert shape(g.plan_many_dft_r2c([16384], 64, 1 << 20, 1 << 30, g.FFTW_ESTIMATE | TC, "f")) == [(1, 8192, 2)]
+    r2d = shape(g.plan_many_dft_r2c([8192, 8192], 1, 1 << 20, 1 << 32, g.FFTW_ESTIMATE | TC, "f"))
+    assert r2d[:2] == [(0, 4096, 3), (HC2C, 4096, 1)] and all(v != 3 for _, _, v in r2d[2:])
